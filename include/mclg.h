@@ -1,0 +1,217 @@
+/*
+ * mclg.h -- C ABI of the GB300 time-step engine for the 2-D mantle-convection
+ * code (reference: mingming-li/Mantle_Convection_Lab).
+ *
+ * The reference has no plugin registry or FFI: its "operator API" is the fixed
+ * call sequence of Main.c:58-64 over one global struct G
+ * (global_variables.h:315-422):
+ *     buoyancy_force(); viscosity(); velocity_pressure_KGF_matrix();
+ *     solve_velocity_pressure(); output(); update_temperature();
+ * This header exports the same sequence as plain C functions over an opaque
+ * context that owns the device-resident mesh and fields.  Every function
+ * returns an int status (MCLG_OK == 0); none of them exits the process.
+ * Vectors that cross this boundary use the reference's own layouts:
+ *   node arrays    [nno] in G.node order (sorted global node id, iz + ix*gnoz)
+ *   element arrays [nel] in Morton (G.Mcode) order
+ *   velocity dofs  [neq] in G.id order (u,w interleaved per node, 'V' dofs skipped)
+ *   temperature dofs [heat neq] in G.heat.id order ('T' nodes skipped)
+ * All arrays are plain host memory; the library copies in and out.
+ * The context is stream-ordered on one CUDA stream and not thread-safe.
+ */
+#ifndef MCLG_H
+#define MCLG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+	MCLG_OK = 0,
+	MCLG_CAP_REACHED = 1,   /* an iteration cap was hit (the reference carries on too) */
+	MCLG_NAN = 2,           /* a non-finite value appeared in a solver */
+	MCLG_BREAKDOWN = 3,     /* CG breakdown: zero curvature d.Kd */
+	MCLG_BAD_INPUT = 4,     /* malformed .input, bad sizes or unsupported option */
+	MCLG_CUDA_ERROR = 5,    /* a CUDA call failed; see mclg_last_error() */
+	MCLG_IO_ERROR = 6,      /* a file could not be read or written */
+	MCLG_NO_DEVICE = 7      /* no CUDA device is visible */
+};
+
+#define MCLG_MAX_LEVEL 16
+
+/*
+ * Run configuration.  Field names and defaults follow the .input keys read by
+ * read_input_file() (Input.c:3-99); mclg_config_from_input() parses a .input
+ * file with the reference's getpar rules (Parsing.c:54-141: name=value tokens,
+ * '#' comments, quoted values, last occurrence wins).
+ */
+typedef struct mclg_config {
+	char data_dir[256];      /* data_dir (".")                         Input.c:7 */
+	char solver[8];          /* solver: "cg" | "jc" ("jc")             Input.c:10 */
+	int level;               /* level: finest level + 1 (1)            Input.c:12 */
+	int mg_min_level;        /* mg_min_level (1)                       Input.c:13 */
+	int nprox, nproz;        /* nprox/nproz: must be 1 on one device   Input.c:20-21 */
+	double model_length;     /* model_length (2.0)                     Input.c:23 */
+	double model_height;     /* model_height (1.0)                     Input.c:24 */
+	char top_v_bc[2], bot_v_bc[2], lef_v_bc[2], rig_v_bc[2];  /* "SV".. Input.c:26-29 */
+	double top_v_bc_val[2], bot_v_bc_val[2], lef_v_bc_val[2], rig_v_bc_val[2];
+	char top_T_bc, bot_T_bc, lef_T_bc, rig_T_bc;              /* 'T' / 'F' Input.c:35-38 */
+	double top_T_bc_val, bot_T_bc_val, lef_T_bc_val, rig_T_bc_val;
+	int T_ini;               /* T_ini (1); -2 = seeded synthetic field  Input.c:45 */
+	double T_mantle, T_mantle_perturb;
+	int T_wave_number;
+	double Rayleigh;         /* Rayleigh (1e7)                         Input.c:51 */
+	double A, refT, lower_mantle_jump;   /* Viscosity.c:13-16       Input.c:55-57 */
+	int max_timestep, save_spacing;
+	double Q, theta;         /* internal heating, time-integration theta */
+	int AMR;
+	int cg_precondition;     /* cg_precondition (0)                    Input.c:80 */
+	double accuracy;         /* inner CG tolerance (0.001)              Input.c:83 */
+	int auto_accuracy;
+	double citcom_solver_accu; /* Uzawa tolerance (0.001)               Input.c:85 */
+	int develop_mode;        /* static refinement pattern (1)           Input.c:86 */
+	int check_v_only;
+	int max_citcom_cycle;    /* (375) */
+	int max_cg_cycle;        /* (200) */
+	int zero_P;              /* (1) */
+	int lg_mul, grain_damage; /* must be 0: Lagrange and grain paths are out of scope */
+	char old_T_file[1024];
+	int old_T_timestep;
+	/* seeded synthetic initial temperature (T_ini=-2), see mclg_ic.h */
+	int ic_kind;
+	uint64_t ic_seed;
+	double ic_noise, ic_bl_thickness, ic_mode_amp;
+	int ic_modes;
+	/* GB300 solver options (not in the reference) */
+	int precision;           /* 0 = FP64 replica of the reference's iteration;
+	                            1 = mixed: FP32 multigrid-preconditioned inner CG
+	                                inside FP64 Uzawa + iterative refinement       */
+	double stokes_rtol;      /* mixed mode: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
+	int warm_start;          /* mixed mode: start Uzawa from the previous step's (d,p) */
+	double vis_min, vis_max; /* viscosity clip, applied when vis_max > 0 */
+	int mg_smooth;           /* damped-Jacobi sweeps per V-cycle side (2) */
+	double mg_omega;         /* Jacobi damping (0.6) */
+} mclg_config;
+
+typedef struct mclg_step_stats {
+	int timestep;
+	int uzawa_cycles;        /* outer iterations (Solver.c:131-224) */
+	int cg_cycles;           /* total inner CG iterations this step */
+	int heat_cg_cycles;      /* Update_temperature.c:1140-1354 */
+	int status;              /* worst status seen in this step */
+	double dv, dp;           /* last Uzawa update sizes (Solver.c:202-204) */
+	double dt, model_time;   /* Update_temperature.c:37-42 */
+	double res_momentum;     /* |F - K d - G p|_2 / |F|_2 after the solve */
+	double res_continuity;   /* |G^T d|_2 / |F|_2 after the solve */
+	double ms_stokes, ms_heat, ms_total;  /* device time per phase */
+	long long kernel_launches;            /* kernels launched by this step */
+	double matvec_ms;        /* device time inside the dominant matvec kernel (instrumented runs) */
+	long long matvec_launches;
+} mclg_step_stats;
+
+typedef struct mclg_ctx mclg_ctx;
+
+/* ---- configuration ----------------------------------------------------- */
+/* Defaults of Input.c:3-99 (plus the GB300 options). */
+void mclg_config_defaults(mclg_config *cfg);
+/* sizeof(mclg_config), sizeof(mclg_step_stats): lets a binding check its layout. */
+size_t mclg_config_sizeof(void);
+size_t mclg_step_stats_sizeof(void);
+/* setup_parser + read_input_file (Parsing.c:54-141, Input.c:3-99). */
+int mclg_config_from_input(const char *path, mclg_config *cfg);
+
+/* ---- life cycle -------------------------------------------------------- */
+/* initial_data_structure + get_time_independent_variables (Mesh.c:3-428),
+ * then the mesh block of Main.c:33-52 (build_quad_tree .. assign_matrix_memory)
+ * on the host, and upload of the mesh to the device. */
+int mclg_create(mclg_ctx **ctx, const mclg_config *cfg);
+void mclg_destroy(mclg_ctx *ctx);
+const char *mclg_status_string(int status);
+const char *mclg_last_error(void);
+
+/* ---- the per-step operator sequence (Main.c:55-64) --------------------- */
+int mclg_initial_temperature(mclg_ctx *ctx);               /* Initial_condition.c:3-37 */
+int mclg_buoyancy_force(mclg_ctx *ctx);                    /* Buoyancy.c:3-22 */
+int mclg_viscosity(mclg_ctx *ctx);                         /* Viscosity.c:3-24 */
+int mclg_velocity_pressure_KGF_matrix(mclg_ctx *ctx);      /* Build_matrix.c:4-40 */
+int mclg_solve_velocity_pressure(mclg_ctx *ctx, mclg_step_stats *st); /* Solver.c:3-12 */
+int mclg_update_temperature(mclg_ctx *ctx, mclg_step_stats *st);      /* Update_temperature.c:3-133 */
+/* output(): Output.c:4-156 text files for the current G.timestep. */
+int mclg_output(mclg_ctx *ctx, const char *data_dir, int timestep);
+/* One whole step: buoyancy .. solve, optional output, update_temperature. */
+int mclg_step(mclg_ctx *ctx, int write_output, mclg_step_stats *st);
+/* Same step with the host-buffer round trip a caller without device memory
+ * makes: T (nno doubles, G.node order) is copied in before the step and
+ * T, V (2*nno) and P (nel) are copied out after it. */
+int mclg_step_host(mclg_ctx *ctx, const double *T_in, double *T_out, double *V_out,
+                   double *P_out, mclg_step_stats *st);
+
+/* ---- state access ------------------------------------------------------ */
+enum {
+	MCLG_F_T = 0,        /* [nno] temperature                     G.T[lev]          */
+	MCLG_F_V0 = 1,       /* [nno] horizontal velocity             G.V[lev][0]       */
+	MCLG_F_V1 = 2,       /* [nno] vertical velocity               G.V[lev][1]       */
+	MCLG_F_P = 3,        /* [nel] pressure                        G.p[lev]          */
+	MCLG_F_D = 4,        /* [neq] velocity solution vector        G.d[lev]          */
+	MCLG_F_STRESS = 5,   /* [nno] second-invariant stress         G.stress[lev]     */
+	MCLG_F_VIS = 6,      /* [nno] viscosity                       G.vis[lev]        */
+	MCLG_F_BUOY = 7,     /* [nno] buoyancy                        G.buoyancy[lev]   */
+	MCLG_F_F = 8,        /* [neq] Stokes right-hand side          G.F[lev]          */
+	MCLG_F_KDIAG = 9,    /* [neq] diagonal of K                   G.Kdiag[lev]      */
+	MCLG_F_BAB = 10,     /* [nel] sum_rows G^2/Kdiag              Solver.c:54-64    */
+	MCLG_F_TAU0 = 11,    /* [nel] SUPG tau_x                      G.heat[lev].tau[0] */
+	MCLG_F_TAU1 = 12,    /* [nel] SUPG tau_z                      G.heat[lev].tau[1] */
+	MCLG_F_HEAT_F = 13,  /* [heat neq] heat right-hand side       G.heat[lev].F     */
+	MCLG_F_X0 = 14,      /* [nno] node x                          G.X[lev][0]       */
+	MCLG_F_X1 = 15       /* [nno] node z                          G.X[lev][1]       */
+};
+enum {
+	MCLG_M_SIZES = 0,    /* [8]: nel, nno, neq, heat_neq, nh, gnox, gnoz, max_level */
+	MCLG_M_MCODE = 1,    /* [nel]      G.Mcode[lev]                                  */
+	MCLG_M_NODE = 2,     /* [nno]      G.node[lev]                                   */
+	MCLG_M_IEN = 3,      /* [4*nel]    G.ien[lev][a][e], a-major                      */
+	MCLG_M_ID = 4,       /* [2*nno]    G.id[lev][d][A], d-major                       */
+	MCLG_M_HEAT_ID = 5,  /* [nno]      G.heat[lev].id                                 */
+	MCLG_M_LM = 6,       /* [8*nel]    G.lm[lev][d][a][e], (d,a)-major                */
+	MCLG_M_HANG = 7,     /* [3*nh]     hanging node, parent 0, parent 1 (global ids)  */
+	MCLG_M_VBC = 8,      /* [2*nno]    G.bc.v_bc[lev][d] codes ('V','S','N',...)       */
+	MCLG_M_TBC = 9       /* [nno]      G.bc.T_bc[lev] codes                           */
+};
+/* lev < 0 selects the finest level.  n is the caller's buffer length; the
+ * call fails with MCLG_BAD_INPUT when it does not match the array size. */
+int mclg_get_field(mclg_ctx *ctx, int which, int lev, double *out, size_t n);
+int mclg_set_field(mclg_ctx *ctx, int which, int lev, const double *in, size_t n);
+int mclg_get_mesh(mclg_ctx *ctx, int which, int lev, int *out, size_t n);
+
+/* ---- host-only mesh access (no device needed) ------------------------- */
+/* The mesh block of Main.c:33-52 on the host: quadtree, numbering, BC codes,
+ * hanging nodes.  Usable on a machine without a GPU. */
+typedef struct mclg_mesh_handle mclg_mesh_handle;
+int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg);
+void mclg_mesh_delete(mclg_mesh_handle *h);
+int mclg_mesh_get(const mclg_mesh_handle *h, int which, int lev, int *out, size_t n);
+enum {
+	MCLG_R_X = 0,        /* [2*nno]  G.X[lev][d][A], d-major                    */
+	MCLG_R_JACOBI = 1,   /* [nel]    G.jacobi[lev]                              */
+	MCLG_R_AREA = 2,     /* [nel]    G.eco[lev].area                            */
+	MCLG_R_VBCVAL = 3,   /* [2*nno]  G.bc.v_bc_val[lev][d]                      */
+	MCLG_R_TBCVAL = 4    /* [nno]    G.bc.T_bc_val[lev]                         */
+};
+int mclg_mesh_get_real(const mclg_mesh_handle *h, int which, int lev, double *out, size_t n);
+/* Initial_condition.c:3-136 on level lev (finest when lev < 0). */
+int mclg_mesh_initial_temperature(const mclg_mesh_handle *h, int lev, double *T, size_t n);
+
+/* ---- single operators, for parity tests (finest level unless lev >= 0) -- */
+int mclg_stokes_matvec(mclg_ctx *ctx, int lev, const double *x, double *y);   /* K_prod_d, Solver.c:360-386 */
+int mclg_stokes_G(mclg_ctx *ctx, int lev, const double *p, double *y);        /* G_prod_p, Solver.c:569-591 */
+int mclg_stokes_GT(mclg_ctx *ctx, int lev, const double *x, double *p);       /* GT_prod_d, Solver.c:645-666 */
+enum { MCLG_HEAT_K = 0, MCLG_HEAT_C = 1 };
+int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /* K_prod_d_heat, Update_temperature.c:935-962 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,309 @@
+"""Python binding of the C ABI in include/mclg.h (ctypes; no torch needed).
+
+The reference drives its hot path as a fixed sequence of argument-less calls
+over one global struct (Main.c:55-64).  `Model` exposes the same calls with
+the same names over one device-resident context:
+
+    m = Model(Config.from_input("run.input"))
+    m.initial_temperature()
+    for step in range(cfg.max_timestep + 1):
+        m.buoyancy_force(); m.viscosity(); m.velocity_pressure_KGF_matrix()
+        st = m.solve_velocity_pressure()
+        m.output()                      # every save_spacing steps, Output.c format
+        m.update_temperature()
+
+Every call goes to libmclg.so; if the library is missing or no GPU is
+visible the call raises -- there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libmclg.so")
+
+OK, CAP_REACHED, NAN, BREAKDOWN, BAD_INPUT, CUDA_ERROR, IO_ERROR, NO_DEVICE = range(8)
+
+FIELDS = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoyancy": 7, "F": 8,
+          "Kdiag": 9, "BAB": 10, "tau0": 11, "tau1": 12, "heat_F": 13, "X0": 14, "X1": 15}
+MESH = {"sizes": 0, "Mcode": 1, "node": 2, "ien": 3, "id": 4, "heat_id": 5, "lm": 6, "hang": 7,
+        "v_bc": 8, "T_bc": 9}
+MESH_REAL = {"X": 0, "jacobi": 1, "area": 2, "v_bc_val": 3, "T_bc_val": 4}
+
+
+class MclgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class Config(C.Structure):
+    """mclg_config: the .input keys of Input.c:3-99 plus the GB300 options."""
+    _fields_ = [
+        ("data_dir", C.c_char * 256), ("solver", C.c_char * 8), ("level", C.c_int), ("mg_min_level", C.c_int),
+        ("nprox", C.c_int), ("nproz", C.c_int), ("model_length", C.c_double), ("model_height", C.c_double),
+        ("top_v_bc", C.c_char * 2), ("bot_v_bc", C.c_char * 2), ("lef_v_bc", C.c_char * 2),
+        ("rig_v_bc", C.c_char * 2), ("top_v_bc_val", C.c_double * 2), ("bot_v_bc_val", C.c_double * 2),
+        ("lef_v_bc_val", C.c_double * 2), ("rig_v_bc_val", C.c_double * 2), ("top_T_bc", C.c_char),
+        ("bot_T_bc", C.c_char), ("lef_T_bc", C.c_char), ("rig_T_bc", C.c_char), ("top_T_bc_val", C.c_double),
+        ("bot_T_bc_val", C.c_double), ("lef_T_bc_val", C.c_double), ("rig_T_bc_val", C.c_double),
+        ("T_ini", C.c_int), ("T_mantle", C.c_double), ("T_mantle_perturb", C.c_double),
+        ("T_wave_number", C.c_int), ("Rayleigh", C.c_double), ("A", C.c_double), ("refT", C.c_double),
+        ("lower_mantle_jump", C.c_double), ("max_timestep", C.c_int), ("save_spacing", C.c_int),
+        ("Q", C.c_double), ("theta", C.c_double), ("AMR", C.c_int), ("cg_precondition", C.c_int),
+        ("accuracy", C.c_double), ("auto_accuracy", C.c_int), ("citcom_solver_accu", C.c_double),
+        ("develop_mode", C.c_int), ("check_v_only", C.c_int), ("max_citcom_cycle", C.c_int),
+        ("max_cg_cycle", C.c_int), ("zero_P", C.c_int), ("lg_mul", C.c_int), ("grain_damage", C.c_int),
+        ("old_T_file", C.c_char * 1024), ("old_T_timestep", C.c_int), ("ic_kind", C.c_int),
+        ("ic_seed", C.c_uint64), ("ic_noise", C.c_double), ("ic_bl_thickness", C.c_double),
+        ("ic_mode_amp", C.c_double), ("ic_modes", C.c_int), ("precision", C.c_int),
+        ("stokes_rtol", C.c_double), ("warm_start", C.c_int), ("vis_min", C.c_double),
+        ("vis_max", C.c_double), ("mg_smooth", C.c_int), ("mg_omega", C.c_double),
+    ]
+
+    @classmethod
+    def defaults(cls):
+        c = cls()
+        lib().mclg_config_defaults(C.byref(c))
+        return c
+
+    @classmethod
+    def from_input(cls, path):
+        """setup_parser + read_input_file (Parsing.c:54-141, Input.c:3-99)."""
+        c = cls()
+        _check(lib().mclg_config_from_input(os.fsencode(path), C.byref(c)), "config_from_input")
+        return c
+
+
+class StepStats(C.Structure):
+    _fields_ = [
+        ("timestep", C.c_int), ("uzawa_cycles", C.c_int), ("cg_cycles", C.c_int), ("heat_cg_cycles", C.c_int),
+        ("status", C.c_int), ("dv", C.c_double), ("dp", C.c_double), ("dt", C.c_double),
+        ("model_time", C.c_double), ("res_momentum", C.c_double), ("res_continuity", C.c_double),
+        ("ms_stokes", C.c_double), ("ms_heat", C.c_double), ("ms_total", C.c_double),
+        ("kernel_launches", C.c_longlong), ("matvec_ms", C.c_double), ("matvec_launches", C.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_LIB = None
+
+
+def lib():
+    """Load libmclg.so (built in-tree by __graft_entry__.build()); raise if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise MclgError(BAD_INPUT, f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp, sz = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_size_t
+    sig = {
+        "mclg_config_defaults": (None, [vp]), "mclg_config_from_input": (C.c_int, [C.c_char_p, vp]),
+        "mclg_config_sizeof": (sz, []), "mclg_step_stats_sizeof": (sz, []),
+        "mclg_create": (C.c_int, [C.POINTER(vp), vp]), "mclg_destroy": (None, [vp]),
+        "mclg_status_string": (C.c_char_p, [C.c_int]), "mclg_last_error": (C.c_char_p, []),
+        "mclg_initial_temperature": (C.c_int, [vp]), "mclg_buoyancy_force": (C.c_int, [vp]),
+        "mclg_viscosity": (C.c_int, [vp]), "mclg_velocity_pressure_KGF_matrix": (C.c_int, [vp]),
+        "mclg_solve_velocity_pressure": (C.c_int, [vp, vp]), "mclg_update_temperature": (C.c_int, [vp, vp]),
+        "mclg_output": (C.c_int, [vp, C.c_char_p, C.c_int]), "mclg_step": (C.c_int, [vp, C.c_int, vp]),
+        "mclg_step_host": (C.c_int, [vp, dp, dp, dp, dp, vp]),
+        "mclg_get_field": (C.c_int, [vp, C.c_int, C.c_int, dp, sz]),
+        "mclg_set_field": (C.c_int, [vp, C.c_int, C.c_int, dp, sz]),
+        "mclg_get_mesh": (C.c_int, [vp, C.c_int, C.c_int, ip, sz]),
+        "mclg_mesh_new": (C.c_int, [C.POINTER(vp), vp]), "mclg_mesh_delete": (None, [vp]),
+        "mclg_mesh_get": (C.c_int, [vp, C.c_int, C.c_int, ip, sz]),
+        "mclg_mesh_get_real": (C.c_int, [vp, C.c_int, C.c_int, dp, sz]),
+        "mclg_mesh_initial_temperature": (C.c_int, [vp, C.c_int, dp, sz]),
+        "mclg_stokes_matvec": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_stokes_G": (C.c_int, [vp, C.c_int, dp, dp]),
+        "mclg_stokes_GT": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_heat_matvec": (C.c_int, [vp, C.c_int, dp, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    if L.mclg_config_sizeof() != C.sizeof(Config) or L.mclg_step_stats_sizeof() != C.sizeof(StepStats):
+        raise MclgError(BAD_INPUT, "ctypes layout of mclg_config/mclg_step_stats does not match libmclg.so")
+    _LIB = L
+    return L
+
+
+def _check(rc, what):
+    if rc not in (OK, CAP_REACHED):
+        L = lib()
+        raise MclgError(rc, f"{what}: {L.mclg_status_string(rc).decode()}: {L.mclg_last_error().decode()}")
+    return rc
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Mesh:
+    """Host-only mesh of Main.c:33-52 (quadtree, numbering, BC codes, hanging nodes)."""
+
+    def __init__(self, config):
+        self._h = C.c_void_p()
+        self.config = config
+        _check(lib().mclg_mesh_new(C.byref(self._h), C.byref(config)), "mesh_new")
+        s = self.get("sizes")
+        self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
+
+    def close(self):
+        if self._h:
+            lib().mclg_mesh_delete(self._h)
+            self._h = C.c_void_p()
+
+    __del__ = close
+
+    def _size(self, which, lev):
+        if which == "sizes":
+            return 8
+        s = np.zeros(8, np.int32)
+        _check(lib().mclg_mesh_get(self._h, 0, lev, _iptr(s), 8), "mesh_get")
+        nel, nno, neq, hneq, nh = (int(v) for v in s[:5])
+        return {"Mcode": nel, "node": nno, "ien": 4 * nel, "id": 2 * nno, "heat_id": nno, "lm": 8 * nel,
+                "hang": 3 * nh, "v_bc": 2 * nno, "T_bc": nno, "X": 2 * nno, "jacobi": nel, "area": nel,
+                "v_bc_val": 2 * nno, "T_bc_val": nno}[which]
+
+    def get(self, which, lev=-1):
+        n = self._size(which, lev)
+        if which in MESH_REAL:
+            out = np.zeros(n, np.float64)
+            _check(lib().mclg_mesh_get_real(self._h, MESH_REAL[which], lev, _dptr(out), n), "mesh_get_real")
+            return out
+        out = np.zeros(n, np.int32)
+        _check(lib().mclg_mesh_get(self._h, MESH[which], lev, _iptr(out), n), "mesh_get")
+        return out
+
+    def initial_temperature(self, lev=-1):
+        n = self._size("node", lev)
+        out = np.zeros(n, np.float64)
+        _check(lib().mclg_mesh_initial_temperature(self._h, lev, _dptr(out), n), "mesh_initial_temperature")
+        return out
+
+
+class Model:
+    """One device-resident model; method names follow the reference's calls."""
+
+    def __init__(self, config):
+        self.config = config
+        self._c = C.c_void_p()
+        _check(lib().mclg_create(C.byref(self._c), C.byref(config)), "create")
+        s = self.mesh("sizes")
+        self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
+        self.timestep = 0
+
+    def close(self):
+        if self._c:
+            lib().mclg_destroy(self._c)
+            self._c = C.c_void_p()
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- the Main.c:55-64 sequence ---
+    def initial_temperature(self):
+        _check(lib().mclg_initial_temperature(self._c), "initial_temperature")
+        self.timestep = 0
+
+    def buoyancy_force(self):
+        _check(lib().mclg_buoyancy_force(self._c), "buoyancy_force")
+
+    def viscosity(self):
+        _check(lib().mclg_viscosity(self._c), "viscosity")
+
+    def velocity_pressure_KGF_matrix(self):
+        _check(lib().mclg_velocity_pressure_KGF_matrix(self._c), "velocity_pressure_KGF_matrix")
+
+    def solve_velocity_pressure(self):
+        st = StepStats()
+        _check(lib().mclg_solve_velocity_pressure(self._c, C.byref(st)), "solve_velocity_pressure")
+        return st
+
+    def update_temperature(self):
+        st = StepStats()
+        _check(lib().mclg_update_temperature(self._c, C.byref(st)), "update_temperature")
+        self.timestep += 1
+        return st
+
+    def output(self, data_dir=None, timestep=None):
+        d = None if data_dir is None else os.fsencode(data_dir)
+        _check(lib().mclg_output(self._c, d, self.timestep if timestep is None else timestep), "output")
+
+    def step(self, write_output=False):
+        st = StepStats()
+        _check(lib().mclg_step(self._c, int(bool(write_output)), C.byref(st)), "step")
+        self.timestep += 1
+        return st
+
+    def step_host(self, T_in, T_out, V_out, P_out):
+        st = StepStats()
+        _check(lib().mclg_step_host(self._c, _dptr(T_in), _dptr(T_out), _dptr(V_out), _dptr(P_out),
+                                    C.byref(st)), "step_host")
+        self.timestep += 1
+        return st
+
+    # --- state ---
+    def _fsize(self, which):
+        return {"T": self.nno, "V0": self.nno, "V1": self.nno, "P": self.nel, "d": self.neq,
+                "stress": self.nno, "vis": self.nno, "buoyancy": self.nno, "F": self.neq, "Kdiag": self.neq,
+                "BAB": self.nel, "tau0": self.nel, "tau1": self.nel, "heat_F": self.heat_neq,
+                "X0": self.nno, "X1": self.nno}[which]
+
+    def get(self, which):
+        out = np.zeros(self._fsize(which), np.float64)
+        _check(lib().mclg_get_field(self._c, FIELDS[which], -1, _dptr(out), out.size), f"get {which}")
+        return out
+
+    def set(self, which, values):
+        a = np.ascontiguousarray(values, np.float64)
+        _check(lib().mclg_set_field(self._c, FIELDS[which], -1, _dptr(a), a.size), f"set {which}")
+
+    def mesh(self, which, lev=-1):
+        if which == "sizes":
+            n = 8
+        else:
+            n = {"Mcode": self.nel, "node": self.nno, "ien": 4 * self.nel, "id": 2 * self.nno,
+                 "heat_id": self.nno, "lm": 8 * self.nel, "hang": 3 * self.nh, "v_bc": 2 * self.nno,
+                 "T_bc": self.nno}[which]
+        out = np.zeros(n, np.int32)
+        _check(lib().mclg_get_mesh(self._c, MESH[which], lev, _iptr(out), n), f"mesh {which}")
+        return out
+
+    # --- single operators ---
+    def stokes_matvec(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.neq)
+        _check(lib().mclg_stokes_matvec(self._c, -1, _dptr(x), _dptr(y)), "stokes_matvec")
+        return y
+
+    def stokes_G(self, p):
+        p = np.ascontiguousarray(p, np.float64)
+        y = np.zeros(self.neq)
+        _check(lib().mclg_stokes_G(self._c, -1, _dptr(p), _dptr(y)), "stokes_G")
+        return y
+
+    def stokes_GT(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        p = np.zeros(self.nel)
+        _check(lib().mclg_stokes_GT(self._c, -1, _dptr(x), _dptr(p)), "stokes_GT")
+        return p
+
+    def heat_matvec(self, which, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.heat_neq)
+        _check(lib().mclg_heat_matvec(self._c, {"K": 0, "C": 1}[which], _dptr(x), _dptr(y)), "heat_matvec")
+        return y

@@ -1,0 +1,998 @@
+// C ABI of the engine (include/mclg.h): context life cycle, the Main.c:55-64
+// operator sequence, field access and single-operator entry points.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+#include "mclg_dev.cuh"
+#include "../host/mclg_host.h"
+
+namespace mclg {
+void upload_shape_tables(const ShapeTables &s, cudaStream_t st);
+void *uzawa_kernel_ptr();
+void *heat_cg_kernel_ptr();
+__global__ void k_buoy_rowavg(DevLevel L, const double *T, double Ra, double *avg);
+__global__ void k_buoy_vis(DevLevel L, const double *T, double Ra, const double *avg, double Aexp, double refT,
+                           double lm_jump, double vmin, double vmax, double *buoy, double *vis);
+__global__ void k_assemble_stokes(DevLevel L, const double *vis, const double *buoy, double4 *K, double2 *F,
+                                  double2 *Kdiag);
+__global__ void k_bab(DevLevel L, const double2 *Kdiag, double *bab);
+__global__ void k_stress_elem(DevLevel L, const double *vis, const double2 *V, double *se);
+__global__ void k_elem_to_node(DevLevel L, const double *pe, double *pn);
+__global__ void k_kmul(DevLevel L, const double4 *K, const double2 *x, double2 *y);
+__global__ void k_gmul(DevLevel L, const double *p, double2 *y);
+__global__ void k_gtmul(DevLevel L, const double2 *u, double *p);
+__global__ void k_tau(DevLevel L, const double2 *V, double accuracy, double *tau0, double *tau1,
+                      unsigned long long *mins);
+__global__ void k_assemble_heat(DevLevel L, const double2 *V, const double *tau0, const double *tau1, double Q,
+                                double *HK, double *HC, double *HF);
+__global__ void k_heat_dt(DevLevel L, const double2 *V, unsigned long long *mins);
+__global__ void k_heat_system(DevLevel L, const unsigned long long *mins, double theta, const double *T,
+                              const double *HK, const double *HC, const double *HF, double *HA, double *B,
+                              double *x0, double *idiag, StepScalars *sc);
+__global__ void k_heat_writeback(DevLevel L, const double *x, double *T);
+__global__ void k_heat_mul(DevLevel L, const double *M, const double *x, double *y);
+__global__ void k_inv_diag2(int n, const double2 *d, double2 *inv);
+}  // namespace mclg
+
+using namespace mclg;
+
+struct DevLevelBuf {
+	int *node, *ienl, *elev, *p2n_cnt, *p2n_el, *p2n_a, *nb, *hang_ni, *hang_ci0, *hang_ci1, *cell_elem;
+	unsigned char *kslot, *self_slot;
+	double *dxh, *dzh, *jac, *area, *vbcval, *tbcval, *X, *dx, *dz;
+	char *vbc, *tbc;
+};
+
+struct mclg_ctx {
+	mclg_config cfg;
+	mclg_mesh mesh;
+	int fl;                       // finest level index
+	cudaStream_t st;
+	cudaEvent_t ev[6];
+	int num_sms;
+	int coop_uzawa, coop_heat;    // cooperative grid sizes
+	DevLevelBuf lb;
+	DevLevel L;
+	// fields (finest level)
+	double *T, *vis, *buoy, *avg, *stress, *stress_e;
+	double2 *V;
+	// Stokes
+	double4 *K;
+	double2 *F, *Kdiag, *idiag, *d, *u1, *Ah, *r, *s, *dd, *q, *xt;
+	double *bab, *p, *pe[8];
+	// heat
+	double *tau0, *tau1, *HK, *HC, *HF, *HA, *HB, *hx, *hidiag, *hr, *hs, *hd, *hq;
+	unsigned long long *mins;
+	double *red_part;
+	StepScalars *sc;              // device
+	StepScalars *sc_host;         // pinned
+	int timestep;
+	int p_initialized;
+	long long launches;
+	// scratch for the parity API
+	double *tmpA, *tmpB;
+};
+
+static int cuda_fail(cudaError_t e, const char *what)
+{
+	mclg_set_error("%s: %s", what, cudaGetErrorString(e));
+	return MCLG_CUDA_ERROR;
+}
+
+#define CK(call)                                  \
+	do {                                          \
+		cudaError_t e_ = (call);                  \
+		if (e_ != cudaSuccess)                    \
+			return cuda_fail(e_, #call);          \
+	} while (0)
+
+template <class T>
+static cudaError_t dalloc(T **p, size_t n)
+{
+	return cudaMalloc((void **)p, (n + 1) * sizeof(T));
+}
+
+template <class T>
+static cudaError_t upload(T **p, const T *h, size_t n, cudaStream_t st)
+{
+	cudaError_t e = dalloc(p, n);
+	if (e != cudaSuccess)
+		return e;
+	if (n == 0)
+		return cudaSuccess;
+	return cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+static void shape_tables(ShapeTables &S)
+{
+	// Shape_function.c:17-121
+	const double BETA = 1.0 / sqrt(3.0);
+	const double pts[4][2] = {{-1.0, -1.0}, {-1.0, 1.0}, {1.0, 1.0}, {1.0, -1.0}};
+	for (int d = 0; d < 4; d++) {
+		const double xi = pts[d][0] * BETA, eta = pts[d][1] * BETA;
+		S.N[0][d] = 0.25 * (1 - xi) * (1 - eta);
+		S.N[1][d] = 0.25 * (1 - xi) * (1 + eta);
+		S.N[2][d] = 0.25 * (1 + xi) * (1 + eta);
+		S.N[3][d] = 0.25 * (1 + xi) * (1 - eta);
+		S.dNdxi[0][d] = 0.25 * (-1.0) * (1 - eta);
+		S.dNdxi[1][d] = 0.25 * (-1.0) * (1 + eta);
+		S.dNdxi[2][d] = 0.25 * (1.0) * (1 + eta);
+		S.dNdxi[3][d] = 0.25 * (1.0) * (1 - eta);
+		S.dNdeta[0][d] = 0.25 * (1.0 - xi) * (-1.0);
+		S.dNdeta[1][d] = 0.25 * (1.0 - xi) * (1.0);
+		S.dNdeta[2][d] = 0.25 * (1.0 + xi) * (1.0);
+		S.dNdeta[3][d] = 0.25 * (1.0 + xi) * (-1.0);
+	}
+	const double xi = 0.0, eta = 0.0;
+	S.dNdxi_c[0] = 0.25 * (-1.0) * (1 - eta);
+	S.dNdxi_c[1] = 0.25 * (-1.0) * (1 + eta);
+	S.dNdxi_c[2] = 0.25 * (1.0) * (1 + eta);
+	S.dNdxi_c[3] = 0.25 * (1.0) * (1 - eta);
+	S.dNdeta_c[0] = 0.25 * (1.0 - xi) * (-1.0);
+	S.dNdeta_c[1] = 0.25 * (1.0 - xi) * (1.0);
+	S.dNdeta_c[2] = 0.25 * (1.0 + xi) * (1.0);
+	S.dNdeta_c[3] = 0.25 * (1.0 + xi) * (-1.0);
+}
+
+static int upload_level(mclg_ctx *c, int lev)
+{
+	const mclg_mesh &m = c->mesh;
+	const mclg_level &H = m.lev[lev];
+	DevLevelBuf &b = c->lb;
+	const size_t ne = H.nel, nn = H.nno, nh = H.nh;
+	cudaStream_t st = c->st;
+	std::vector<int> ienl(H.ienl, H.ienl + 4 * ne);
+	std::vector<unsigned char> self(nn);
+	for (size_t A = 0; A < nn; A++) {
+		self[A] = 0;
+		for (int k = 0; k < H.nb_cnt[A]; k++)
+			if (H.nb[(size_t)k * nn + A] == (int)A)
+				self[A] = (unsigned char)k;
+	}
+	CK(upload(&b.node, H.node, nn, st));
+	CK(upload(&b.ienl, H.ienl, 4 * ne, st));
+	CK(upload(&b.elev, H.elev, ne, st));
+	CK(upload(&b.p2n_cnt, H.p2n_cnt, nn, st));
+	CK(upload(&b.p2n_el, H.p2n_el, 4 * nn, st));
+	CK(upload(&b.p2n_a, H.p2n_a, 4 * nn, st));
+	CK(upload(&b.nb, H.nb, (size_t)H.nbw * nn, st));
+	CK(upload(&b.kslot, H.kslot, 16 * ne, st));
+	CK(upload(&b.self_slot, self.data(), nn, st));
+	CK(upload(&b.hang_ni, H.hang_ni, nh, st));
+	CK(upload(&b.hang_ci0, H.hang_ci0, nh, st));
+	CK(upload(&b.hang_ci1, H.hang_ci1, nh, st));
+	CK(upload(&b.cell_elem, H.cell_elem, (size_t)(m.gnox - 1) * (m.gnoz - 1), st));
+	CK(upload(&b.dxh, H.dx_dxi, ne, st));
+	CK(upload(&b.dzh, H.dz_deta, ne, st));
+	CK(upload(&b.jac, H.jacobi, ne, st));
+	CK(upload(&b.area, H.area, ne, st));
+	CK(upload(&b.vbc, H.v_bc, 2 * nn, st));
+	CK(upload(&b.vbcval, H.v_bc_val, 2 * nn, st));
+	CK(upload(&b.tbc, H.T_bc, nn, st));
+	CK(upload(&b.tbcval, H.T_bc_val, nn, st));
+	CK(upload(&b.X, H.X, 2 * nn, st));
+	CK(upload(&b.dx, m.dx, MCLG_MAX_LEVEL, st));
+	CK(upload(&b.dz, m.dz, MCLG_MAX_LEVEL, st));
+	CK(cudaStreamSynchronize(st));
+	DevLevel &L = c->L;
+	L.nel = (int)ne;
+	L.nno = (int)nn;
+	L.nbw = H.nbw;
+	L.nh = H.nh;
+	L.hang_chained = H.hang_chained;
+	L.gnox = m.gnox;
+	L.gnoz = m.gnoz;
+	L.fine_level = m.max_level - 1;
+	L.node = b.node;
+	L.ienl = b.ienl;
+	L.elev = b.elev;
+	L.dxh = b.dxh;
+	L.dzh = b.dzh;
+	L.jac = b.jac;
+	L.area = b.area;
+	L.vbc = b.vbc;
+	L.vbcval = b.vbcval;
+	L.tbc = b.tbc;
+	L.tbcval = b.tbcval;
+	L.X = b.X;
+	L.p2n_cnt = b.p2n_cnt;
+	L.p2n_el = b.p2n_el;
+	L.p2n_a = b.p2n_a;
+	L.nb = b.nb;
+	L.self_slot = b.self_slot;
+	L.kslot = b.kslot;
+	L.hang_ni = b.hang_ni;
+	L.hang_ci0 = b.hang_ci0;
+	L.hang_ci1 = b.hang_ci1;
+	L.cell_elem = b.cell_elem;
+	L.dx = b.dx;
+	L.dz = b.dz;
+	return MCLG_OK;
+}
+
+static int coop_blocks(void *kernel, int num_sms, int work)
+{
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess || per_sm < 1)
+		return 0;
+	int maxb = per_sm * num_sms;
+	int need = (work + kBlock - 1) / kBlock;
+	int nb = need < maxb ? need : maxb;
+	if (nb > kMaxCoopBlocks)
+		nb = kMaxCoopBlocks;
+	return nb < 1 ? 1 : nb;
+}
+
+extern "C" {
+
+const char *mclg_status_string(int s)
+{
+	switch (s) {
+	case MCLG_OK: return "ok";
+	case MCLG_CAP_REACHED: return "iteration cap reached";
+	case MCLG_NAN: return "non-finite value in a solver";
+	case MCLG_BREAKDOWN: return "CG breakdown";
+	case MCLG_BAD_INPUT: return "bad input";
+	case MCLG_CUDA_ERROR: return "CUDA error";
+	case MCLG_IO_ERROR: return "I/O error";
+	case MCLG_NO_DEVICE: return "no CUDA device";
+	default: return "unknown status";
+	}
+}
+
+void mclg_destroy(mclg_ctx *c);
+
+int mclg_create(mclg_ctx **out, const mclg_config *cfg)
+{
+	if (out == NULL || cfg == NULL)
+		return MCLG_BAD_INPUT;
+	*out = NULL;
+	if (cfg->lg_mul != 0 || cfg->grain_damage != 0) {
+		mclg_set_error("lg_mul and grain_damage paths are not part of this engine (set both to 0)");
+		return MCLG_BAD_INPUT;
+	}
+	if (strcmp(cfg->solver, "cg") != 0 && strcmp(cfg->solver, "jc") != 0) {
+		mclg_set_error("solver=\"%s\": this engine runs \"cg\" and \"jc\"", cfg->solver);
+		return MCLG_BAD_INPUT;
+	}
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+		cudaGetLastError();
+		mclg_set_error("no CUDA device visible");
+		return MCLG_NO_DEVICE;
+	}
+	mclg_ctx *c = (mclg_ctx *)calloc(1, sizeof(mclg_ctx));
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	c->cfg = *cfg;
+	int rc = mclg_mesh_build(&c->mesh, cfg);
+	if (rc != MCLG_OK) {
+		mclg_mesh_free(&c->mesh);
+		free(c);
+		return rc;
+	}
+	c->fl = c->mesh.max_level - 1;
+	*out = c;
+#define CKD(call)                                  \
+	do {                                           \
+		cudaError_t e_ = (call);                   \
+		if (e_ != cudaSuccess) {                   \
+			int r_ = cuda_fail(e_, #call);         \
+			mclg_destroy(c);                       \
+			*out = NULL;                           \
+			return r_;                             \
+		}                                          \
+	} while (0)
+	CKD(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+	for (int i = 0; i < 6; i++)
+		CKD(cudaEventCreate(&c->ev[i]));
+	int dev = 0;
+	CKD(cudaGetDevice(&dev));
+	CKD(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
+	int coop = 0;
+	CKD(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+	if (!coop) {
+		mclg_set_error("device does not support cooperative launch");
+		mclg_destroy(c);
+		*out = NULL;
+		return MCLG_NO_DEVICE;
+	}
+	rc = upload_level(c, c->fl);
+	if (rc != MCLG_OK) {
+		mclg_destroy(c);
+		*out = NULL;
+		return rc;
+	}
+	ShapeTables S;
+	shape_tables(S);
+	upload_shape_tables(S, c->st);
+	const size_t nn = c->L.nno, ne = c->L.nel, nbw = c->L.nbw;
+	CKD(dalloc(&c->T, nn));
+	CKD(dalloc(&c->vis, nn));
+	CKD(dalloc(&c->buoy, nn));
+	CKD(dalloc(&c->avg, (size_t)c->mesh.gnoz));
+	CKD(dalloc(&c->stress, nn));
+	CKD(dalloc(&c->stress_e, ne));
+	CKD(dalloc(&c->V, nn));
+	CKD(dalloc(&c->K, nbw * nn));
+	CKD(dalloc(&c->F, nn));
+	CKD(dalloc(&c->Kdiag, nn));
+	CKD(dalloc(&c->idiag, nn));
+	CKD(dalloc(&c->d, nn));
+	CKD(dalloc(&c->u1, nn));
+	CKD(dalloc(&c->Ah, nn));
+	CKD(dalloc(&c->r, nn));
+	CKD(dalloc(&c->s, nn));
+	CKD(dalloc(&c->dd, nn));
+	CKD(dalloc(&c->q, nn));
+	CKD(dalloc(&c->xt, nn));
+	CKD(dalloc(&c->bab, ne));
+	CKD(dalloc(&c->p, ne));
+	for (int i = 0; i < 8; i++)
+		CKD(dalloc(&c->pe[i], ne));
+	CKD(dalloc(&c->tau0, ne));
+	CKD(dalloc(&c->tau1, ne));
+	CKD(dalloc(&c->HK, nbw * nn));
+	CKD(dalloc(&c->HC, nbw * nn));
+	CKD(dalloc(&c->HA, nbw * nn));
+	CKD(dalloc(&c->HF, nn));
+	CKD(dalloc(&c->HB, nn));
+	CKD(dalloc(&c->hx, nn));
+	CKD(dalloc(&c->hidiag, nn));
+	CKD(dalloc(&c->hr, nn));
+	CKD(dalloc(&c->hs, nn));
+	CKD(dalloc(&c->hd, nn));
+	CKD(dalloc(&c->hq, nn));
+	CKD(dalloc(&c->mins, 2));
+	CKD(dalloc(&c->red_part, (size_t)2 * kMaxCoopBlocks * kRedWidth));
+	CKD(dalloc(&c->sc, 1));
+	CKD(dalloc(&c->tmpA, 2 * nn + ne));
+	CKD(dalloc(&c->tmpB, 2 * nn + ne));
+	CKD(cudaMallocHost((void **)&c->sc_host, sizeof(StepScalars)));
+	CKD(cudaMemsetAsync(c->sc, 0, sizeof(StepScalars), c->st));
+	CKD(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
+	CKD(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
+	CKD(cudaMemsetAsync(c->V, 0, nn * sizeof(double2), c->st));
+	CKD(cudaMemsetAsync(c->T, 0, nn * sizeof(double), c->st));
+	const int work = (int)(nn > ne ? nn : ne);
+	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(), c->num_sms, work);
+	c->coop_heat = coop_blocks(heat_cg_kernel_ptr(), c->num_sms, (int)nn);
+	if (c->coop_uzawa < 1 || c->coop_heat < 1) {
+		mclg_set_error("cooperative occupancy query failed");
+		mclg_destroy(c);
+		*out = NULL;
+		return MCLG_CUDA_ERROR;
+	}
+	CKD(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+#undef CKD
+}
+
+void mclg_destroy(mclg_ctx *c)
+{
+	if (c == NULL)
+		return;
+	if (c->st)
+		cudaStreamSynchronize(c->st);
+	void *ptrs[] = {c->lb.node, c->lb.ienl, c->lb.elev, c->lb.p2n_cnt, c->lb.p2n_el, c->lb.p2n_a, c->lb.nb,
+	                c->lb.hang_ni, c->lb.hang_ci0, c->lb.hang_ci1, c->lb.cell_elem, c->lb.kslot, c->lb.self_slot,
+	                c->lb.dxh, c->lb.dzh, c->lb.jac, c->lb.area, c->lb.vbcval, c->lb.tbcval, c->lb.X, c->lb.dx,
+	                c->lb.dz, c->lb.vbc, c->lb.tbc, c->T, c->vis, c->buoy, c->avg, c->stress, c->stress_e, c->V,
+	                c->K, c->F, c->Kdiag, c->idiag, c->d, c->u1, c->Ah, c->r, c->s, c->dd, c->q, c->xt, c->bab,
+	                c->p, c->tau0, c->tau1, c->HK, c->HC, c->HF, c->HA, c->HB, c->hx, c->hidiag, c->hr, c->hs,
+	                c->hd, c->hq, c->mins, c->red_part, c->sc, c->tmpA, c->tmpB};
+	for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++)
+		if (ptrs[i])
+			cudaFree(ptrs[i]);
+	for (int i = 0; i < 8; i++)
+		if (c->pe[i])
+			cudaFree(c->pe[i]);
+	if (c->sc_host)
+		cudaFreeHost(c->sc_host);
+	for (int i = 0; i < 6; i++)
+		if (c->ev[i])
+			cudaEventDestroy(c->ev[i]);
+	if (c->st)
+		cudaStreamDestroy(c->st);
+	mclg_mesh_free(&c->mesh);
+	free(c);
+}
+
+static int blocks_for(size_t n)
+{
+	return (int)((n + kBlock - 1) / kBlock);
+}
+
+static int check_launch(mclg_ctx *c, const char *what)
+{
+	cudaError_t e = cudaGetLastError();
+	c->launches++;
+	if (e != cudaSuccess)
+		return cuda_fail(e, what);
+	return MCLG_OK;
+}
+
+int mclg_initial_temperature(mclg_ctx *c)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	const mclg_level &H = c->mesh.lev[c->fl];
+	std::vector<double> T(H.nno);
+	int rc = mclg_host_initial_temperature(&c->mesh, &c->cfg, c->fl, T.data());
+	if (rc != MCLG_OK)
+		return rc;
+	CK(cudaMemcpyAsync(c->T, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	c->timestep = 0;
+	double zero = 0.0;
+	CK(cudaMemcpy(&c->sc->model_time, &zero, sizeof zero, cudaMemcpyHostToDevice));
+	return MCLG_OK;
+}
+
+static int launch_buoy_vis(mclg_ctx *c)
+{
+	const mclg_config &f = c->cfg;
+	k_buoy_rowavg<<<c->mesh.gnoz, kBlock, 0, c->st>>>(c->L, c->T, f.Rayleigh, c->avg);
+	int rc = check_launch(c, "k_buoy_rowavg");
+	if (rc)
+		return rc;
+	k_buoy_vis<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->T, f.Rayleigh, c->avg, f.A, f.refT,
+	                                                       f.lower_mantle_jump, f.vis_min, f.vis_max, c->buoy,
+	                                                       c->vis);
+	return check_launch(c, "k_buoy_vis");
+}
+
+int mclg_buoyancy_force(mclg_ctx *c)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	return launch_buoy_vis(c);
+}
+
+int mclg_viscosity(mclg_ctx *c)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	return launch_buoy_vis(c);
+}
+
+int mclg_velocity_pressure_KGF_matrix(mclg_ctx *c)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	k_assemble_stokes<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->vis, c->buoy, c->K, c->F, c->Kdiag);
+	int rc = check_launch(c, "k_assemble_stokes");
+	if (rc)
+		return rc;
+	k_inv_diag2<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L.nno, c->Kdiag, c->idiag);
+	if ((rc = check_launch(c, "k_inv_diag2")))
+		return rc;
+	k_bab<<<blocks_for(c->L.nel), kBlock, 0, c->st>>>(c->L, c->Kdiag, c->bab);
+	return check_launch(c, "k_bab");
+}
+
+static int status_from_bits(int bits)
+{
+	if (bits & 2)
+		return MCLG_NAN;
+	if (bits & 4)
+		return MCLG_BREAKDOWN;
+	if (bits & 1)
+		return MCLG_CAP_REACHED;
+	return MCLG_OK;
+}
+
+static int read_scalars(mclg_ctx *c)
+{
+	CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+static int launch_uzawa(mclg_ctx *c)
+{
+	const mclg_config &f = c->cfg;
+	const size_t nn = c->L.nno;
+	// initial_d_p (Solver.c:251-278): d = 0 every step; p = 0 unless kept
+	CK(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
+	if (!(c->p_initialized && f.AMR == 0 && f.zero_P == 0))
+		CK(cudaMemsetAsync(c->p, 0, c->L.nel * sizeof(double), c->st));
+	c->p_initialized = 1;
+	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
+	UzawaArgs a;
+	memset(&a, 0, sizeof a);
+	a.L = c->L;
+	a.K = c->K;
+	a.idiag = c->idiag;
+	a.F = c->F;
+	a.bab = c->bab;
+	a.d = c->d;
+	a.u1 = c->u1;
+	a.Ah = c->Ah;
+	a.r = c->r;
+	a.s = c->s;
+	a.dd = c->dd;
+	a.q = c->q;
+	a.xt = c->xt;
+	a.V = c->V;
+	a.p = c->p;
+	a.r0 = c->pe[0];
+	a.r1 = c->pe[1];
+	a.r2 = c->pe[2];
+	a.z0 = c->pe[3];
+	a.z1 = c->pe[4];
+	a.s1 = c->pe[5];
+	a.s2 = c->pe[6];
+	a.Ahp = c->pe[7];
+	a.red.part = c->red_part;
+	a.red.flip = 0;
+	a.sc = c->sc;
+	a.max_citcom = f.max_citcom_cycle;
+	a.max_cg = f.max_cg_cycle;
+	a.precond = f.cg_precondition;
+	a.check_v_only = f.check_v_only;
+	a.solver_jc = strcmp(f.solver, "jc") == 0;
+	a.auto_accuracy = f.auto_accuracy;
+	a.neq = c->mesh.lev[c->fl].neq;
+	a.citcom_accu = f.citcom_solver_accu;
+	a.accuracy = f.accuracy;
+	void *args[] = {&a};
+	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(), dim3(c->coop_uzawa), dim3(kBlock), args, 0, c->st));
+	c->launches++;
+	return MCLG_OK;
+}
+
+static int launch_stress(mclg_ctx *c)
+{
+	k_stress_elem<<<blocks_for(c->L.nel), kBlock, 0, c->st>>>(c->L, c->vis, c->V, c->stress_e);
+	int rc = check_launch(c, "k_stress_elem");
+	if (rc)
+		return rc;
+	k_elem_to_node<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->stress_e, c->stress);
+	return check_launch(c, "k_elem_to_node");
+}
+
+static void fill_stats_stokes(mclg_ctx *c, mclg_step_stats *st)
+{
+	if (st == NULL)
+		return;
+	const StepScalars &s = *c->sc_host;
+	st->timestep = c->timestep;
+	st->uzawa_cycles = s.uzawa_cycles;
+	st->cg_cycles = s.cg_cycles;
+	st->dv = s.dv;
+	st->dp = s.dp;
+	st->res_momentum = s.res_m;
+	st->res_continuity = s.res_c;
+	st->status = status_from_bits(s.status);
+}
+
+int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	int rc = launch_uzawa(c);
+	if (rc)
+		return rc;
+	if ((rc = launch_stress(c)))
+		return rc;
+	if ((rc = read_scalars(c)))
+		return rc;
+	fill_stats_stokes(c, st);
+	return MCLG_OK;
+}
+
+static int launch_heat(mclg_ctx *c)
+{
+	const mclg_config &f = c->cfg;
+	const DevLevel &L = c->L;
+	int rc;
+	k_tau<<<blocks_for(L.nel), kBlock, 0, c->st>>>(L, c->V, f.accuracy, c->tau0, c->tau1, c->mins);
+	if ((rc = check_launch(c, "k_tau")))
+		return rc;
+	k_assemble_heat<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->V, c->tau0, c->tau1, f.Q, c->HK, c->HC, c->HF);
+	if ((rc = check_launch(c, "k_assemble_heat")))
+		return rc;
+	k_heat_dt<<<blocks_for(L.nel), kBlock, 0, c->st>>>(L, c->V, c->mins);
+	if ((rc = check_launch(c, "k_heat_dt")))
+		return rc;
+	k_heat_system<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->mins, f.theta, c->T, c->HK, c->HC, c->HF, c->HA,
+	                                                        c->HB, c->hx, c->hidiag, c->sc);
+	if ((rc = check_launch(c, "k_heat_system")))
+		return rc;
+	HeatArgs a;
+	memset(&a, 0, sizeof a);
+	a.op.L = L;
+	a.op.HA = c->HA;
+	a.op.idiag = c->hidiag;
+	a.B = c->HB;
+	a.x = c->hx;
+	a.r = c->hr;
+	a.s = c->hs;
+	a.d = c->hd;
+	a.q = c->hq;
+	a.red.part = c->red_part;
+	a.red.flip = 0;
+	a.sc = c->sc;
+	a.max_cycle = 1000;
+	a.precond = f.cg_precondition;
+	a.accu = 1e-3;
+	void *args[] = {&a};
+	CK(cudaLaunchCooperativeKernel(heat_cg_kernel_ptr(), dim3(c->coop_heat), dim3(kBlock), args, 0, c->st));
+	c->launches++;
+	k_heat_writeback<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->hx, c->T);
+	return check_launch(c, "k_heat_writeback");
+}
+
+int mclg_update_temperature(mclg_ctx *c, mclg_step_stats *st)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	int rc = launch_heat(c);
+	if (rc)
+		return rc;
+	if ((rc = read_scalars(c)))
+		return rc;
+	if (st) {
+		st->heat_cg_cycles = c->sc_host->heat_cycles;
+		st->dt = c->sc_host->dt;
+		st->model_time = c->sc_host->model_time;
+		int s2 = status_from_bits(c->sc_host->status);
+		if (s2 != MCLG_OK && st->status == MCLG_OK)
+			st->status = s2;
+	}
+	c->timestep++;
+	return MCLG_OK;
+}
+
+int mclg_output(mclg_ctx *c, const char *dir, int timestep)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	const size_t nn = c->L.nno;
+	std::vector<double> T(nn), V(2 * nn), V0(nn), V1(nn), S(nn), vis(nn);
+	CK(cudaMemcpyAsync(T.data(), c->T, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(V.data(), c->V, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(S.data(), c->stress, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(vis.data(), c->vis, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	for (size_t i = 0; i < nn; i++) {
+		V0[i] = V[2 * i];
+		V1[i] = V[2 * i + 1];
+	}
+	return mclg_write_output(dir ? dir : c->cfg.data_dir, timestep, &c->mesh.lev[c->fl], T.data(), V0.data(),
+	                         V1.data(), S.data(), vis.data());
+}
+
+int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	mclg_step_stats local;
+	if (st == NULL)
+		st = &local;
+	memset(st, 0, sizeof *st);
+	const long long l0 = c->launches;
+	int rc;
+	CK(cudaEventRecord(c->ev[0], c->st));
+	if ((rc = launch_buoy_vis(c)))
+		return rc;
+	if ((rc = mclg_velocity_pressure_KGF_matrix(c)))
+		return rc;
+	if ((rc = launch_uzawa(c)))
+		return rc;
+	if ((rc = launch_stress(c)))
+		return rc;
+	CK(cudaEventRecord(c->ev[1], c->st));
+	if (write_output && c->cfg.save_spacing > 0 && c->timestep % c->cfg.save_spacing == 0) {
+		if ((rc = mclg_output(c, NULL, c->timestep)))
+			return rc;
+	}
+	CK(cudaEventRecord(c->ev[2], c->st));
+	if ((rc = launch_heat(c)))
+		return rc;
+	CK(cudaEventRecord(c->ev[3], c->st));
+	if ((rc = read_scalars(c)))
+		return rc;
+	fill_stats_stokes(c, st);
+	const StepScalars &s = *c->sc_host;
+	st->heat_cg_cycles = s.heat_cycles;
+	st->dt = s.dt;
+	st->model_time = s.model_time;
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+	st->ms_stokes = ms;
+	cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+	st->ms_heat = ms;
+	cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
+	st->ms_total = ms;
+	st->kernel_launches = c->launches - l0;
+	c->timestep++;
+	return MCLG_OK;
+}
+
+int mclg_step_host(mclg_ctx *c, const double *T_in, double *T_out, double *V_out, double *P_out,
+                   mclg_step_stats *st)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	const size_t nn = c->L.nno, ne = c->L.nel;
+	if (T_in)
+		CK(cudaMemcpyAsync(c->T, T_in, nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	int rc = mclg_step(c, 0, st);
+	if (rc)
+		return rc;
+	if (T_out)
+		CK(cudaMemcpyAsync(T_out, c->T, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	if (V_out)
+		CK(cudaMemcpyAsync(V_out, c->V, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	if (P_out)
+		CK(cudaMemcpyAsync(P_out, c->p, ne * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+// ---- field access --------------------------------------------------------
+static int field_info(mclg_ctx *c, int which, size_t *n, void **dptr, int *kind)
+{
+	const mclg_level &H = c->mesh.lev[c->fl];
+	// kind: 0 node scalar, 1 element scalar, 2 velocity eq vector (node double2 on device),
+	//       3 node double2 component 0, 4 component 1, 5 heat eq vector (node scalar)
+	switch (which) {
+	case MCLG_F_T: *n = H.nno; *dptr = c->T; *kind = 0; break;
+	case MCLG_F_V0: *n = H.nno; *dptr = c->V; *kind = 3; break;
+	case MCLG_F_V1: *n = H.nno; *dptr = c->V; *kind = 4; break;
+	case MCLG_F_P: *n = H.nel; *dptr = c->p; *kind = 1; break;
+	case MCLG_F_D: *n = H.neq; *dptr = c->d; *kind = 2; break;
+	case MCLG_F_STRESS: *n = H.nno; *dptr = c->stress; *kind = 0; break;
+	case MCLG_F_VIS: *n = H.nno; *dptr = c->vis; *kind = 0; break;
+	case MCLG_F_BUOY: *n = H.nno; *dptr = c->buoy; *kind = 0; break;
+	case MCLG_F_F: *n = H.neq; *dptr = c->F; *kind = 2; break;
+	case MCLG_F_KDIAG: *n = H.neq; *dptr = c->Kdiag; *kind = 2; break;
+	case MCLG_F_BAB: *n = H.nel; *dptr = c->bab; *kind = 1; break;
+	case MCLG_F_TAU0: *n = H.nel; *dptr = c->tau0; *kind = 1; break;
+	case MCLG_F_TAU1: *n = H.nel; *dptr = c->tau1; *kind = 1; break;
+	case MCLG_F_HEAT_F: *n = H.heat_neq; *dptr = c->HF; *kind = 5; break;
+	case MCLG_F_X0: *n = H.nno; *dptr = c->lb.X; *kind = 0; break;
+	case MCLG_F_X1: *n = H.nno; *dptr = c->lb.X + H.nno; *kind = 0; break;
+	default:
+		mclg_set_error("unknown field %d", which);
+		return MCLG_BAD_INPUT;
+	}
+	return MCLG_OK;
+}
+
+static int download_raw(mclg_ctx *c, void *dptr, size_t bytes, std::vector<double> &buf)
+{
+	buf.resize(bytes / sizeof(double) + 1);
+	CK(cudaMemcpyAsync(buf.data(), dptr, bytes, cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+int mclg_get_field(mclg_ctx *c, int which, int lev, double *out, size_t n)
+{
+	if (c == NULL || out == NULL)
+		return MCLG_BAD_INPUT;
+	if (lev >= 0 && lev != c->fl) {
+		mclg_set_error("only the finest level (%d) is resident on the device", c->fl);
+		return MCLG_BAD_INPUT;
+	}
+	size_t need;
+	void *dptr;
+	int kind, rc;
+	if ((rc = field_info(c, which, &need, &dptr, &kind)))
+		return rc;
+	if (n != need) {
+		mclg_set_error("field %d has %zu entries, buffer has %zu", which, need, n);
+		return MCLG_BAD_INPUT;
+	}
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t nn = H.nno;
+	std::vector<double> buf;
+	if (kind == 0 || kind == 1) {
+		CK(cudaMemcpyAsync(out, dptr, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+		CK(cudaStreamSynchronize(c->st));
+		return MCLG_OK;
+	}
+	if (kind == 5) {
+		if ((rc = download_raw(c, dptr, nn * sizeof(double), buf)))
+			return rc;
+		for (size_t A = 0; A < nn; A++)
+			if (H.heat_id[A] >= 0)
+				out[H.heat_id[A]] = buf[A];
+		return MCLG_OK;
+	}
+	if ((rc = download_raw(c, dptr, 2 * nn * sizeof(double), buf)))
+		return rc;
+	if (kind == 3 || kind == 4) {
+		for (size_t A = 0; A < nn; A++)
+			out[A] = buf[2 * A + (kind - 3)];
+		return MCLG_OK;
+	}
+	for (size_t A = 0; A < nn; A++)
+		for (int d = 0; d < 2; d++) {
+			const int eq = H.id[d * nn + A];
+			if (eq >= 0)
+				out[eq] = buf[2 * A + d];
+		}
+	return MCLG_OK;
+}
+
+int mclg_set_field(mclg_ctx *c, int which, int lev, const double *in, size_t n)
+{
+	if (c == NULL || in == NULL)
+		return MCLG_BAD_INPUT;
+	if (lev >= 0 && lev != c->fl) {
+		mclg_set_error("only the finest level (%d) is resident on the device", c->fl);
+		return MCLG_BAD_INPUT;
+	}
+	size_t need;
+	void *dptr;
+	int kind, rc;
+	if ((rc = field_info(c, which, &need, &dptr, &kind)))
+		return rc;
+	if (n != need) {
+		mclg_set_error("field %d has %zu entries, buffer has %zu", which, need, n);
+		return MCLG_BAD_INPUT;
+	}
+	if (which != MCLG_F_T && which != MCLG_F_P && which != MCLG_F_D && which != MCLG_F_VIS &&
+	    which != MCLG_F_V0 && which != MCLG_F_V1) {
+		mclg_set_error("field %d is derived and cannot be set", which);
+		return MCLG_BAD_INPUT;
+	}
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t nn = H.nno;
+	if (kind == 0 || kind == 1) {
+		CK(cudaMemcpyAsync(dptr, in, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+		CK(cudaStreamSynchronize(c->st));
+		if (which == MCLG_F_P)
+			c->p_initialized = 1;
+		return MCLG_OK;
+	}
+	std::vector<double> buf;
+	if ((rc = download_raw(c, dptr, 2 * nn * sizeof(double), buf)))
+		return rc;
+	if (kind == 3 || kind == 4) {
+		for (size_t A = 0; A < nn; A++)
+			buf[2 * A + (kind - 3)] = in[A];
+	} else {
+		for (size_t A = 0; A < nn; A++)
+			for (int d = 0; d < 2; d++) {
+				const int eq = H.id[d * nn + A];
+				buf[2 * A + d] = eq >= 0 ? in[eq] : 0.0;
+			}
+	}
+	CK(cudaMemcpyAsync(dptr, buf.data(), 2 * nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t n);
+
+int mclg_get_mesh(mclg_ctx *c, int which, int lev, int *out, size_t n)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	return mclg_host_mesh_get(&c->mesh, which, lev, out, n);
+}
+
+// ---- single operators ----------------------------------------------------
+static int eq_to_node(mclg_ctx *c, const double *x, double *dev)
+{
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t nn = H.nno;
+	std::vector<double> buf(2 * nn, 0.0);
+	for (size_t A = 0; A < nn; A++)
+		for (int d = 0; d < 2; d++) {
+			const int eq = H.id[d * nn + A];
+			if (eq >= 0)
+				buf[2 * A + d] = x[eq];
+		}
+	CK(cudaMemcpyAsync(dev, buf.data(), 2 * nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+static int node_to_eq(mclg_ctx *c, const double *dev, double *y)
+{
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t nn = H.nno;
+	std::vector<double> buf(2 * nn);
+	CK(cudaMemcpyAsync(buf.data(), dev, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	for (size_t A = 0; A < nn; A++)
+		for (int d = 0; d < 2; d++) {
+			const int eq = H.id[d * nn + A];
+			if (eq >= 0)
+				y[eq] = buf[2 * A + d];
+		}
+	return MCLG_OK;
+}
+
+static int check_lev(mclg_ctx *c, int lev)
+{
+	if (lev >= 0 && lev != c->fl) {
+		mclg_set_error("only the finest level (%d) is resident on the device", c->fl);
+		return MCLG_BAD_INPUT;
+	}
+	return MCLG_OK;
+}
+
+int mclg_stokes_matvec(mclg_ctx *c, int lev, const double *x, double *y)
+{
+	if (c == NULL || x == NULL || y == NULL || check_lev(c, lev))
+		return MCLG_BAD_INPUT;
+	int rc = eq_to_node(c, x, c->tmpA);
+	if (rc)
+		return rc;
+	k_kmul<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->K, (const double2 *)c->tmpA, (double2 *)c->tmpB);
+	if ((rc = check_launch(c, "k_kmul")))
+		return rc;
+	return node_to_eq(c, c->tmpB, y);
+}
+
+int mclg_stokes_G(mclg_ctx *c, int lev, const double *p, double *y)
+{
+	if (c == NULL || p == NULL || y == NULL || check_lev(c, lev))
+		return MCLG_BAD_INPUT;
+	CK(cudaMemcpyAsync(c->tmpA, p, c->L.nel * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	k_gmul<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->tmpA, (double2 *)c->tmpB);
+	int rc = check_launch(c, "k_gmul");
+	if (rc)
+		return rc;
+	return node_to_eq(c, c->tmpB, y);
+}
+
+int mclg_stokes_GT(mclg_ctx *c, int lev, const double *x, double *p)
+{
+	if (c == NULL || x == NULL || p == NULL || check_lev(c, lev))
+		return MCLG_BAD_INPUT;
+	int rc = eq_to_node(c, x, c->tmpA);
+	if (rc)
+		return rc;
+	k_gtmul<<<blocks_for(c->L.nel), kBlock, 0, c->st>>>(c->L, (const double2 *)c->tmpA, c->tmpB);
+	if ((rc = check_launch(c, "k_gtmul")))
+		return rc;
+	CK(cudaMemcpyAsync(p, c->tmpB, c->L.nel * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+int mclg_heat_matvec(mclg_ctx *c, int which, const double *x, double *y)
+{
+	if (c == NULL || x == NULL || y == NULL || (which != MCLG_HEAT_K && which != MCLG_HEAT_C))
+		return MCLG_BAD_INPUT;
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t nn = H.nno;
+	std::vector<double> buf(nn, 0.0);
+	for (size_t A = 0; A < nn; A++)
+		if (H.heat_id[A] >= 0)
+			buf[A] = x[H.heat_id[A]];
+	CK(cudaMemcpyAsync(c->tmpA, buf.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	k_heat_mul<<<blocks_for(nn), kBlock, 0, c->st>>>(c->L, which == MCLG_HEAT_K ? c->HK : c->HC, c->tmpA, c->tmpB);
+	int rc = check_launch(c, "k_heat_mul");
+	if (rc)
+		return rc;
+	CK(cudaMemcpyAsync(buf.data(), c->tmpB, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	for (size_t A = 0; A < nn; A++)
+		if (H.heat_id[A] >= 0)
+			y[H.heat_id[A]] = buf[A];
+	return MCLG_OK;
+}
+
+}  // extern "C"
+
+namespace mclg {
+__global__ void k_inv_diag2(int n, const double2 *__restrict__ d, double2 *__restrict__ inv)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const double2 v = d[i];
+	inv[i] = make_double2(1.0 / v.x, 1.0 / v.y);
+}
+}  // namespace mclg

@@ -1,0 +1,82 @@
+/*
+ * Host-side mesh, numbering and I/O of the GB300 engine (C, no CUDA).
+ *
+ * One mclg_mesh holds what the reference keeps per MG level in its global G
+ * (global_variables.h:315-422) for a single rank: Morton leaf codes, the
+ * sorted node list, ien/id/lm numbering, boundary codes, hanging-node
+ * constraints, element geometry and the node->element map.  Everything here
+ * is built once per mesh on the host and then uploaded to the device.
+ */
+#ifndef MCLG_HOST_H
+#define MCLG_HOST_H
+
+#include "mclg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCLG_LEVEL_BITS 4
+#define MCLG_NB_MAX 25     /* max distinct neighbour nodes of a node (2:1 meshes need <= 21) */
+
+typedef struct mclg_level {
+	int nel, nno;
+	int *Mcode;            /* [nel]  (morton << 4) | element level             Tree.c:340-358 */
+	int *node;             /* [nno]  sorted global node ids                    Construct_ien_id_lm.c:43-66 */
+	int *ien;              /* [4*nel] global node ids, ien[a*nel + e]          Construct_ien_id_lm.c:3-41 */
+	int *ienl;             /* [4*nel] local node indices (node_index(ien))     */
+	int *elev;             /* [nel]  element level (Mcode_lev)                 */
+	int *id;               /* [2*nno] velocity equation or -1, id[d*nno + A]   Construct_ien_id_lm.c:79-115 */
+	int neq;
+	int *heat_id;          /* [nno]  temperature equation or -1                Construct_ien_id_lm.c:117-144 */
+	int heat_neq;
+	char *v_bc;            /* [2*nno] velocity BC codes                        Boundary_condition.c:58-110 */
+	double *v_bc_val;      /* [2*nno] */
+	char *T_bc;            /* [nno]                                            Boundary_condition.c:10-56 */
+	double *T_bc_val;      /* [nno] */
+	double *X;             /* [2*nno] node coordinates, X[d*nno + A]           Mesh.c:430-452 */
+	double *dx_dxi, *dz_deta, *jacobi, *area;  /* [nel] Shape_function.c:123-167, Construct_ien_id_lm.c:198-218 */
+	int nh;                /* hanging nodes                                     Connection.c:59-276 */
+	int *hang_node, *hang_c0, *hang_c1;   /* global ids */
+	int *hang_ni, *hang_ci0, *hang_ci1;   /* local indices */
+	int hang_chained;      /* 1 when a parent of some hanging node is itself hanging */
+	int *p2n_cnt;          /* [nno] number of elements touching a node          Construct_ien_id_lm.c:220-244 */
+	int *p2n_el;           /* [4*nno] element ids in ascending order, p2n_el[k*nno + A] */
+	int *p2n_a;            /* [4*nno] local corner index of the node in that element */
+	int nbw;               /* neighbour-list width (max over nodes) */
+	int *nb;               /* [nbw*nno] sorted neighbour nodes, nb[k*nno + A], padded with A */
+	int *nb_cnt;           /* [nno] */
+	unsigned char *kslot;  /* [16*nel] slot of corner b in the neighbour list of corner a, kslot[(a*4+b)*nel + e] */
+	int *cell_elem;        /* [(gnox-1)*(gnoz-1)] element covering fine cell (ix,iz), cell_elem[ix*(gnoz-1)+iz] */
+} mclg_level;
+
+typedef struct mclg_mesh {
+	int min_level, max_level;   /* MG levels [min_level, max_level) */
+	int gnox, gnoz;
+	int max_elx[MCLG_MAX_LEVEL], max_nel[MCLG_MAX_LEVEL];
+	double dx[MCLG_MAX_LEVEL], dz[MCLG_MAX_LEVEL];
+	double length, height;
+	int uniform;                /* finest level is a uniform grid (no hanging nodes) */
+	mclg_level lev[MCLG_MAX_LEVEL];
+} mclg_mesh;
+
+/* Build the mesh the way Main.c:33-52 does on its first step, for one rank. */
+int mclg_mesh_build(mclg_mesh *m, const mclg_config *cfg);
+void mclg_mesh_free(mclg_mesh *m);
+/* Binary search in the sorted node list (node_index, Array_work.c:106-129). */
+int mclg_node_index(const mclg_level *L, int gid);
+
+/* Initial temperature on one level (Initial_condition.c:3-136, plus T_ini=-2). */
+int mclg_host_initial_temperature(const mclg_mesh *m, const mclg_config *cfg, int lev, double *T);
+
+/* Output.c:31-156 text files for one step. */
+int mclg_write_output(const char *data_dir, int timestep, const mclg_level *L,
+                      const double *T, const double *V0, const double *V1,
+                      const double *stress, const double *vis);
+
+void mclg_set_error(const char *fmt, ...);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,176 @@
+/*
+ * Host-only C ABI over the mesh builder: lets a caller (or a test on a
+ * machine without a GPU) read the numbering that the device path uses.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include "mclg_host.h"
+
+struct mclg_mesh_handle {
+	mclg_mesh mesh;
+	mclg_config cfg;
+};
+
+int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg)
+{
+	int rc;
+	mclg_mesh_handle *p;
+	if (h == NULL || cfg == NULL)
+		return MCLG_BAD_INPUT;
+	*h = NULL;
+	p = (mclg_mesh_handle *)calloc(1, sizeof *p);
+	if (p == NULL)
+		return MCLG_BAD_INPUT;
+	p->cfg = *cfg;
+	rc = mclg_mesh_build(&p->mesh, cfg);
+	if (rc != MCLG_OK) {
+		mclg_mesh_free(&p->mesh);
+		free(p);
+		return rc;
+	}
+	*h = p;
+	return MCLG_OK;
+}
+
+void mclg_mesh_delete(mclg_mesh_handle *h)
+{
+	if (h == NULL)
+		return;
+	mclg_mesh_free(&h->mesh);
+	free(h);
+}
+
+static const mclg_level *pick_level(const mclg_mesh *m, int lev)
+{
+	if (lev < 0)
+		lev = m->max_level - 1;
+	if (lev < m->min_level || lev >= m->max_level)
+		return NULL;
+	return &m->lev[lev];
+}
+
+/* shared by mclg_mesh_get and mclg_get_mesh */
+int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t n)
+{
+	const mclg_level *L = pick_level(m, lev);
+	size_t ne, nn, i, need;
+	if (L == NULL || out == NULL) {
+		mclg_set_error("level %d is not a level of this mesh", lev);
+		return MCLG_BAD_INPUT;
+	}
+	ne = (size_t)L->nel;
+	nn = (size_t)L->nno;
+	switch (which) {
+	case MCLG_M_SIZES: need = 8; break;
+	case MCLG_M_MCODE: need = ne; break;
+	case MCLG_M_NODE: need = nn; break;
+	case MCLG_M_IEN: need = 4 * ne; break;
+	case MCLG_M_ID: need = 2 * nn; break;
+	case MCLG_M_HEAT_ID: need = nn; break;
+	case MCLG_M_LM: need = 8 * ne; break;
+	case MCLG_M_HANG: need = 3 * (size_t)L->nh; break;
+	case MCLG_M_VBC: need = 2 * nn; break;
+	case MCLG_M_TBC: need = nn; break;
+	default:
+		mclg_set_error("unknown mesh array %d", which);
+		return MCLG_BAD_INPUT;
+	}
+	if (n != need) {
+		mclg_set_error("mesh array %d has %zu entries, buffer has %zu", which, need, n);
+		return MCLG_BAD_INPUT;
+	}
+	switch (which) {
+	case MCLG_M_SIZES:
+		out[0] = L->nel; out[1] = L->nno; out[2] = L->neq; out[3] = L->heat_neq;
+		out[4] = L->nh; out[5] = m->gnox; out[6] = m->gnoz; out[7] = m->max_level;
+		break;
+	case MCLG_M_MCODE: memcpy(out, L->Mcode, ne * sizeof(int)); break;
+	case MCLG_M_NODE: memcpy(out, L->node, nn * sizeof(int)); break;
+	case MCLG_M_IEN: memcpy(out, L->ien, 4 * ne * sizeof(int)); break;
+	case MCLG_M_ID: memcpy(out, L->id, 2 * nn * sizeof(int)); break;
+	case MCLG_M_HEAT_ID: memcpy(out, L->heat_id, nn * sizeof(int)); break;
+	case MCLG_M_LM: {
+		size_t d, a, e;
+		for (d = 0; d < 2; d++)
+			for (a = 0; a < 4; a++)
+				for (e = 0; e < ne; e++)
+					out[(d * 4 + a) * ne + e] = L->id[d * nn + (size_t)L->ienl[a * ne + e]];
+		break;
+	}
+	case MCLG_M_HANG:
+		for (i = 0; i < (size_t)L->nh; i++) {
+			out[i] = L->hang_node[i];
+			out[L->nh + i] = L->hang_c0[i];
+			out[2 * (size_t)L->nh + i] = L->hang_c1[i];
+		}
+		break;
+	case MCLG_M_VBC:
+		for (i = 0; i < 2 * nn; i++)
+			out[i] = (unsigned char)L->v_bc[i];
+		break;
+	case MCLG_M_TBC:
+		for (i = 0; i < nn; i++)
+			out[i] = (unsigned char)L->T_bc[i];
+		break;
+	}
+	return MCLG_OK;
+}
+
+int mclg_mesh_get(const mclg_mesh_handle *h, int which, int lev, int *out, size_t n)
+{
+	if (h == NULL)
+		return MCLG_BAD_INPUT;
+	return mclg_host_mesh_get(&h->mesh, which, lev, out, n);
+}
+
+int mclg_mesh_get_real(const mclg_mesh_handle *h, int which, int lev, double *out, size_t n)
+{
+	const mclg_level *L;
+	size_t need, ne, nn;
+	if (h == NULL || out == NULL)
+		return MCLG_BAD_INPUT;
+	L = pick_level(&h->mesh, lev);
+	if (L == NULL) {
+		mclg_set_error("level %d is not a level of this mesh", lev);
+		return MCLG_BAD_INPUT;
+	}
+	ne = (size_t)L->nel;
+	nn = (size_t)L->nno;
+	switch (which) {
+	case MCLG_R_X: need = 2 * nn; break;
+	case MCLG_R_JACOBI: need = ne; break;
+	case MCLG_R_AREA: need = ne; break;
+	case MCLG_R_VBCVAL: need = 2 * nn; break;
+	case MCLG_R_TBCVAL: need = nn; break;
+	default:
+		mclg_set_error("unknown mesh array %d", which);
+		return MCLG_BAD_INPUT;
+	}
+	if (n != need) {
+		mclg_set_error("mesh array %d has %zu entries, buffer has %zu", which, need, n);
+		return MCLG_BAD_INPUT;
+	}
+	switch (which) {
+	case MCLG_R_X: memcpy(out, L->X, need * sizeof(double)); break;
+	case MCLG_R_JACOBI: memcpy(out, L->jacobi, need * sizeof(double)); break;
+	case MCLG_R_AREA: memcpy(out, L->area, need * sizeof(double)); break;
+	case MCLG_R_VBCVAL: memcpy(out, L->v_bc_val, need * sizeof(double)); break;
+	case MCLG_R_TBCVAL: memcpy(out, L->T_bc_val, need * sizeof(double)); break;
+	}
+	return MCLG_OK;
+}
+
+int mclg_mesh_initial_temperature(const mclg_mesh_handle *h, int lev, double *T, size_t n)
+{
+	const mclg_level *L;
+	if (h == NULL || T == NULL)
+		return MCLG_BAD_INPUT;
+	if (lev < 0)
+		lev = h->mesh.max_level - 1;
+	L = pick_level(&h->mesh, lev);
+	if (L == NULL || n != (size_t)L->nno) {
+		mclg_set_error("bad level or buffer size");
+		return MCLG_BAD_INPUT;
+	}
+	return mclg_host_initial_temperature(&h->mesh, &h->cfg, lev, T);
+}

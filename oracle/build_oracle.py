@@ -1,0 +1,29 @@
+"""Build the CPU oracle (test infrastructure): oracle/liboracle.so from oracle.c.
+
+Compiled with -ffp-contract=off so that x86 and Arm hosts evaluate every
+expression with the same roundings, and with OpenMP when the compiler has it
+(the CPU baseline may use all host cores; one thread keeps the reference's
+summation order).
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+
+
+def build():
+    if os.path.exists(LIB) and os.path.getmtime(LIB) > os.path.getmtime(SRC):
+        return LIB
+    base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", LIB, "-lm"]
+    p = subprocess.run(base[:1] + ["-fopenmp"] + base[1:], capture_output=True, text=True)
+    if p.returncode != 0:
+        p = subprocess.run(base, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + p.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build())

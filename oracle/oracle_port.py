@@ -1,0 +1,167 @@
+"""ctypes driver of the CPU oracle (oracle/oracle.c) -- test infrastructure.
+
+The mesh arrays (ien, node list, BC codes, hanging nodes) come from the host
+mesh builder of the engine, which tests pin bit-exact against the
+reference's own arrays; everything numerical is recomputed here on the CPU.
+
+    r = run("case.input", steps=3)      # dict of T, V0, V1, P, d, stress, vis, stats per step
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from build_oracle import LIB, build  # noqa: E402
+
+_L = None
+GET = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoyancy": 7, "F": 8, "Kdiag": 9,
+       "tau0": 10, "tau1": 11, "heat_F": 12}
+
+
+def lib():
+    global _L
+    if _L is None:
+        build()
+        _L = C.CDLL(LIB)
+        vp = C.c_void_p
+        _L.orc_new.restype = vp
+        _L.orc_new.argtypes = [C.c_int] * 5 + [vp] * 8 + [C.c_int] + [vp] * 7
+        for n in ("orc_free", "orc_set_T", "orc_step", "orc_stokes", "orc_assemble", "orc_kmul", "orc_gmul",
+                  "orc_gtmul"):
+            getattr(_L, n).restype = None
+        _L.orc_free.argtypes = [vp]
+        _L.orc_set_T.argtypes = [vp, vp]
+        _L.orc_step.argtypes = [vp, vp]
+        _L.orc_stokes.argtypes = [vp, vp]
+        _L.orc_assemble.argtypes = [vp]
+        _L.orc_kmul.argtypes = [vp, vp, vp]
+        _L.orc_gmul.argtypes = [vp, vp, vp]
+        _L.orc_gtmul.argtypes = [vp, vp, vp]
+        _L.orc_get.restype = C.c_int
+        _L.orc_get.argtypes = [vp, C.c_int, vp]
+        _L.orc_sizes.argtypes = [vp, vp]
+        _L.orc_cg_sample.restype = C.c_int
+        _L.orc_cg_sample.argtypes = [vp, C.c_int]
+    return _L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """One CPU model built from a .input file (or a Config) and the engine's host mesh."""
+
+    def __init__(self, cfg, threads=1):
+        from mantle_convection_lab_gb300.api import Config, Mesh
+        if isinstance(cfg, (str, os.PathLike)):
+            cfg = Config.from_input(cfg)
+        self.cfg = cfg
+        m = Mesh(cfg)
+        fl = m.max_level - 1
+        nel, nno = m.nel, m.nno
+        node = m.get("node")
+        ien = m.get("ien")
+        pos = np.searchsorted(node, ien)
+        self._keep = []
+        k = self._keep.append
+        self.ienl = np.ascontiguousarray(pos, np.int32); k(self.ienl)
+        self.elev = np.ascontiguousarray(m.get("Mcode") & 15, np.int32); k(self.elev)
+        self.node = node.astype(np.int32); k(self.node)
+        self.X = m.get("X"); k(self.X)
+        self.vbc = np.ascontiguousarray(m.get("v_bc").astype(np.uint8)); k(self.vbc)
+        self.vbcval = m.get("v_bc_val"); k(self.vbcval)
+        self.tbc = np.ascontiguousarray(m.get("T_bc").astype(np.uint8)); k(self.tbc)
+        self.tbcval = m.get("T_bc_val"); k(self.tbcval)
+        hang = m.get("hang").reshape(3, -1) if m.nh else np.zeros((3, 0), np.int32)
+        self.hang = np.ascontiguousarray(np.searchsorted(node, hang), np.int32); k(self.hang)
+        nh = hang.shape[1]
+        L, H = cfg.model_length, cfg.model_height
+        dx = np.array([L / (1 << l) for l in range(16)]); k(dx)
+        dz = np.array([H / (1 << l) for l in range(16)]); k(dz)
+        dpar = np.array([cfg.Rayleigh, cfg.A, cfg.refT, cfg.lower_mantle_jump, cfg.Q, cfg.theta, cfg.accuracy,
+                         cfg.citcom_solver_accu, cfg.vis_min, cfg.vis_max]); k(dpar)
+        ipar = np.array([cfg.max_citcom_cycle, cfg.max_cg_cycle, cfg.cg_precondition, cfg.check_v_only,
+                         int(cfg.solver == b"jc"), cfg.zero_P, cfg.AMR, cfg.auto_accuracy, threads],
+                        np.int32); k(ipar)
+        hp = [self.hang[i] if nh else np.zeros(1, np.int32) for i in range(3)]
+        self._keep.extend(hp)
+        self._o = lib().orc_new(nel, nno, m.gnox, m.gnoz, fl, _p(self.ienl), _p(self.elev), _p(self.node),
+                                _p(self.X), _p(self.vbc), _p(self.vbcval), _p(self.tbc), _p(self.tbcval), nh,
+                                _p(hp[0]), _p(hp[1]), _p(hp[2]), _p(dx), _p(dz), _p(dpar), _p(ipar))
+        sz = np.zeros(4, np.int32)
+        lib().orc_sizes(self._o, _p(sz))
+        self.nel, self.nno, self.neq, self.hneq = map(int, sz)
+        self.mesh = m
+        self.set_T(m.initial_temperature())
+
+    def close(self):
+        if self._o:
+            lib().orc_free(self._o)
+            self._o = None
+
+    __del__ = close
+
+    def set_T(self, T):
+        self._T = np.ascontiguousarray(T, np.float64)
+        lib().orc_set_T(self._o, _p(self._T))
+
+    def step(self):
+        st = np.zeros(7)
+        lib().orc_step(self._o, _p(st))
+        return {"uzawa_cycles": int(st[0]), "cg_cycles": int(st[1]), "heat_cg_cycles": int(st[2]),
+                "dt": st[3], "model_time": st[4], "res_m": st[5], "res_c": st[6]}
+
+    def stokes(self):
+        st = np.zeros(7)
+        lib().orc_stokes(self._o, _p(st))
+        return {"uzawa_cycles": int(st[0]), "cg_cycles": int(st[1]), "res_m": st[5], "res_c": st[6]}
+
+    def assemble(self):
+        lib().orc_assemble(self._o)
+
+    def get(self, name):
+        n = {"P": self.nel, "tau0": self.nel, "tau1": self.nel, "d": self.neq, "F": self.neq, "Kdiag": self.neq,
+             "heat_F": self.hneq}.get(name, self.nno)
+        out = np.zeros(n)
+        lib().orc_get(self._o, GET[name], _p(out))
+        return out
+
+    def kmul(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.neq)
+        lib().orc_kmul(self._o, _p(x), _p(y))
+        return y
+
+    def gmul(self, p):
+        p = np.ascontiguousarray(p, np.float64)
+        y = np.zeros(self.neq)
+        lib().orc_gmul(self._o, _p(p), _p(y))
+        return y
+
+    def gtmul(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        p = np.zeros(self.nel)
+        lib().orc_gtmul(self._o, _p(x), _p(p))
+        return p
+
+    def cg_sample(self, n):
+        return lib().orc_cg_sample(self._o, n)
+
+
+def run(path, steps=1, threads=1):
+    """Run `steps` time steps from the configured initial temperature."""
+    o = Oracle(path, threads)
+    out = {"stats": []}
+    for _ in range(steps):
+        out["stats"].append(o.step())
+    for k in ("T", "V0", "V1", "P", "d", "stress", "vis"):
+        out[k] = o.get(k)
+    o.close()
+    return out
