@@ -108,8 +108,8 @@ typedef struct mclg_step_stats {
 	double res_continuity;   /* |G^T d|_2 / |F|_2 after the solve */
 	double ms_stokes, ms_heat, ms_total;  /* device time per phase */
 	long long kernel_launches;            /* kernels launched by this step */
-	double matvec_ms;        /* device time inside the dominant matvec kernel (instrumented runs) */
-	long long matvec_launches;
+	double solver_kernel_ms; /* device time of the Stokes solver kernel(s) of this step (CUDA events) */
+	long long solver_kernel_launches;
 } mclg_step_stats;
 
 typedef struct mclg_ctx mclg_ctx;

@@ -82,7 +82,8 @@ class StepStats(C.Structure):
         ("status", C.c_int), ("dv", C.c_double), ("dp", C.c_double), ("dt", C.c_double),
         ("model_time", C.c_double), ("res_momentum", C.c_double), ("res_continuity", C.c_double),
         ("ms_stokes", C.c_double), ("ms_heat", C.c_double), ("ms_total", C.c_double),
-        ("kernel_launches", C.c_longlong), ("matvec_ms", C.c_double), ("matvec_launches", C.c_longlong),
+        ("kernel_launches", C.c_longlong), ("solver_kernel_ms", C.c_double),
+        ("solver_kernel_launches", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -9,12 +9,7 @@
 
 namespace mclg {
 
-__constant__ ShapeTables cS;
-
-void upload_shape_tables(const ShapeTables &s, cudaStream_t st)
-{
-	cudaMemcpyToSymbolAsync(cS, &s, sizeof s, 0, cudaMemcpyHostToDevice, st);
-}
+MCLG_SHAPE_UPLOAD(upload_shape_tables_elem)
 
 // ---- buoyancy: Ra*T minus its horizontal average (Buoyancy.c:3-22) -------
 // get_node_horiz_avg (Parallel.c:354-437) interpolates Ra*T at every fine-grid

@@ -10,7 +10,7 @@
 
 namespace mclg {
 
-extern __constant__ ShapeTables cS;
+MCLG_SHAPE_UPLOAD(upload_shape_tables_heat)
 
 // calculate_artificial_diffusivity (Update_temperature.c:241-291)
 // Thread 0 also seeds the two minima of advection_dt with its 1e10 start value.

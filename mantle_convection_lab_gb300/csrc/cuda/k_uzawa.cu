@@ -8,7 +8,7 @@
 
 namespace mclg {
 
-extern __constant__ ShapeTables cS;
+MCLG_SHAPE_UPLOAD(upload_shape_tables_uzawa)
 
 // ---- the assembled operator in node-block-ELL form ----------------------
 // y_A = sum_k K[k][A] x[nb[k][A]]: the reference's K_prod_d (Solver.c:360-386)

@@ -9,7 +9,9 @@
 #include "../host/mclg_host.h"
 
 namespace mclg {
-void upload_shape_tables(const ShapeTables &s, cudaStream_t st);
+void upload_shape_tables_elem(const ShapeTables &s, cudaStream_t st);
+void upload_shape_tables_uzawa(const ShapeTables &s, cudaStream_t st);
+void upload_shape_tables_heat(const ShapeTables &s, cudaStream_t st);
 void *uzawa_kernel_ptr();
 void *heat_cg_kernel_ptr();
 __global__ void k_buoy_rowavg(DevLevel L, const double *T, double Ra, double *avg);
@@ -307,7 +309,9 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 	}
 	ShapeTables S;
 	shape_tables(S);
-	upload_shape_tables(S, c->st);
+	upload_shape_tables_elem(S, c->st);
+	upload_shape_tables_uzawa(S, c->st);
+	upload_shape_tables_heat(S, c->st);
 	const size_t nn = c->L.nno, ne = c->L.nel, nbw = c->L.nbw;
 	CKD(dalloc(&c->T, nn));
 	CKD(dalloc(&c->vis, nn));
@@ -681,8 +685,10 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 		return rc;
 	if ((rc = mclg_velocity_pressure_KGF_matrix(c)))
 		return rc;
+	CK(cudaEventRecord(c->ev[4], c->st));
 	if ((rc = launch_uzawa(c)))
 		return rc;
+	CK(cudaEventRecord(c->ev[5], c->st));
 	if ((rc = launch_stress(c)))
 		return rc;
 	CK(cudaEventRecord(c->ev[1], c->st));
@@ -708,6 +714,9 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 	st->ms_heat = ms;
 	cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
 	st->ms_total = ms;
+	cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+	st->solver_kernel_ms = ms;
+	st->solver_kernel_launches = 1;
 	st->kernel_launches = c->launches - l0;
 	c->timestep++;
 	return MCLG_OK;

@@ -35,6 +35,17 @@ struct ShapeTables {
 	double dNdeta_c[4];
 };
 
+// The tables live in constant memory.  Without relocatable device code a
+// __constant__ symbol is private to its translation unit, so every .cu file
+// that reads cS holds its own copy and exports an upload function defined
+// with MCLG_SHAPE_UPLOAD; the context fills all of them at creation.
+static __constant__ ShapeTables cS;
+#define MCLG_SHAPE_UPLOAD(fn)                                                     \
+	void fn(const ShapeTables &s, cudaStream_t st)                                \
+	{                                                                             \
+		cudaMemcpyToSymbolAsync(cS, &s, sizeof s, 0, cudaMemcpyHostToDevice, st); \
+	}
+
 // Device copy of one mesh level (pointers into device memory).
 struct DevLevel {
 	int nel, nno, nbw, nh, hang_chained, gnox, gnoz, fine_level;

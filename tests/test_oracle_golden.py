@@ -1,0 +1,47 @@
+"""The CPU oracle (oracle/oracle.c) against the reference's own dumps.
+
+With one thread the oracle sums in the reference's order; on these fixtures it
+reproduces the reference bit for bit (the tolerance is only there for hosts
+whose libm rounds exp/cosh/sinh differently).
+"""
+import numpy as np
+import pytest
+from conftest import golden, golden_input, rel
+
+import oracle_port
+
+TOL = 1e-12
+
+
+@pytest.mark.parametrize("case,steps", [("cfg1_l5", 4), ("hang11v_l6", 1), ("vc_l6", 1), ("dev12_l7", 1)])
+def test_oracle_steps(case, steps):
+    g = golden(case)
+    o = oracle_port.Oracle(golden_input(case))
+    for s in range(steps):
+        st = o.step()
+        assert st["uzawa_cycles"] == g["series/uzawa_cycles"][s]
+        # the reference also prints a count for initial_T_dot's solve before step 0
+        assert st["heat_cg_cycles"] == g["series/heat_cg_cycles"][s + 1]
+        assert rel(st["dt"], g["series/dt"][s]) < TOL
+        assert rel(o.get("V0"), g[f"step{s:04d}/V0"]) < TOL
+        assert rel(o.get("V1"), g[f"step{s:04d}/V1"]) < TOL
+        assert rel(o.get("P"), g[f"step{s:04d}/p"]) < TOL
+        assert rel(o.get("d"), g[f"step{s:04d}/d"]) < TOL
+        assert rel(o.get("stress"), g[f"step{s:04d}/stress"]) < TOL
+        assert rel(o.get("T"), g[f"heat{s:04d}/T"]) < TOL
+        assert rel(st["res_m"], g["series/res_m"][s]) < 1e-6
+
+
+@pytest.mark.parametrize("case", ["cfg1_l5", "hang11_l6", "vc_l6"])
+def test_oracle_operators(case):
+    g = golden(case)
+    o = oracle_port.Oracle(golden_input(case))
+    o.assemble()
+    lev = o.mesh.max_level - 1
+    assert rel(o.get("F"), g[f"ops/F@{lev}"]) < TOL
+    assert rel(o.get("Kdiag"), g[f"ops/Kdiag@{lev}"]) < TOL
+    assert rel(o.get("vis"), g[f"ops/vis@{lev}"]) < TOL
+    assert rel(o.get("buoyancy"), g[f"ops/buoyancy@{lev}"]) < TOL
+    assert rel(o.kmul(g[f"ops/probe_x@{lev}"]), g[f"ops/Kx@{lev}"]) < TOL
+    assert rel(o.gmul(g[f"ops/probe_p@{lev}"]), g[f"ops/Gp@{lev}"]) < TOL
+    assert rel(o.gtmul(g[f"ops/probe_x@{lev}"]), g[f"ops/GTx@{lev}"]) < TOL
