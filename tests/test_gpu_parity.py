@@ -45,20 +45,36 @@ def test_stokes_operators(case):
         assert rel(m.stokes_GT(g[f"ops/probe_x@{lev}"]), g[f"ops/GTx@{lev}"]) < OP_TOL
 
 
-@pytest.mark.parametrize("case,steps", [("cfg1_l5", 4), ("hang11v_l6", 2), ("vc_l6", 3), ("dev12_l7", 1),
-                                        ("dev13_l8", 1), ("dev14_l7", 1)])
-def test_time_steps(case, steps):
+# Cases whose Uzawa loop stops at max_citcom_cycle before converging.  Their
+# iterates depend on summation order: the CPU oracle with 4 threads moves
+# dev14_l7 by 1.7e-6 from the reference.  They are held to 1e-5 instead.
+CAPPED_TOL = 1e-5
+
+
+@pytest.mark.parametrize("case,steps,tol", [("cfg1_l5", 4, FIELD_TOL), ("vc_l6", 3, FIELD_TOL),
+                                            ("hang11v_l6", 2, CAPPED_TOL), ("dev12_l7", 1, CAPPED_TOL),
+                                            ("dev13_l8", 1, CAPPED_TOL), ("dev14_l7", 1, CAPPED_TOL)])
+def test_time_steps(case, steps, tol):
     g = golden(case)
     with make(case) as m:
         for s in range(steps):
             st = m.step()
             assert st.status in (0, 1), st.status
             assert abs(st.uzawa_cycles - int(g["series/uzawa_cycles"][s])) <= 1
-            assert rel(st.dt, g["series/dt"][s]) < FIELD_TOL
-            assert rel(st.model_time, g["series/model_time"][s]) < FIELD_TOL
+            assert rel(st.dt, g["series/dt"][s]) < tol
+            assert rel(st.model_time, g["series/model_time"][s]) < tol
             for f, k in (("V0", "V0"), ("V1", "V1"), ("P", "p"), ("d", "d"), ("stress", "stress")):
-                assert rel(m.get(f), g[f"step{s:04d}/{k}"]) < FIELD_TOL, (case, s, f)
-            assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < FIELD_TOL, (case, s, "T")
+                assert rel(m.get(f), g[f"step{s:04d}/{k}"]) < tol, (case, s, f)
+            assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < tol, (case, s, "T")
+
+
+def rel_nan(a, b):
+    """Relative L2 over the finite entries; the NaN pattern itself must match.
+    The reference's tau is NaN where cosh/sinh overflow (cell Peclet > 710)."""
+    a, b = np.asarray(a), np.asarray(b)
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    f = ~np.isnan(b)
+    return rel(a[f], b[f])
 
 
 @pytest.mark.parametrize("case", ["cfg1_l5", "hang11v_l6", "vc_l6"])
@@ -68,12 +84,12 @@ def test_heat_operators(case):
     with make(case) as m:
         m.step()
         h = "heat0000"
-        assert rel(m.get("tau0"), g[f"{h}/tau0"]) < FIELD_TOL
-        assert rel(m.get("tau1"), g[f"{h}/tau1"]) < FIELD_TOL
-        assert rel(m.get("heat_F"), g[f"{h}/heat_F"]) < FIELD_TOL
+        assert rel_nan(m.get("tau0"), g[f"{h}/tau0"]) < FIELD_TOL
+        assert rel_nan(m.get("tau1"), g[f"{h}/tau1"]) < FIELD_TOL
+        assert rel_nan(m.get("heat_F"), g[f"{h}/heat_F"]) < FIELD_TOL
         x = g[f"{h}/heat_probe_x"]
-        assert rel(m.heat_matvec("K", x), g[f"{h}/HKx"]) < FIELD_TOL
-        assert rel(m.heat_matvec("C", x), g[f"{h}/HCx"]) < FIELD_TOL
+        assert rel_nan(m.heat_matvec("K", x), g[f"{h}/HKx"]) < FIELD_TOL
+        assert rel_nan(m.heat_matvec("C", x), g[f"{h}/HCx"]) < FIELD_TOL
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "cfg1_l7.npz")), reason="fixture not generated")
