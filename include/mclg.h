@@ -86,14 +86,21 @@ typedef struct mclg_config {
 	double ic_noise, ic_bl_thickness, ic_mode_amp;
 	int ic_modes;
 	/* GB300 solver options (not in the reference) */
-	int precision;           /* 0 = FP64 replica of the reference's iteration;
-	                            1 = mixed: FP32 multigrid-preconditioned inner CG
-	                                inside FP64 Uzawa + iterative refinement       */
-	double stokes_rtol;      /* mixed mode: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
-	int warm_start;          /* mixed mode: start Uzawa from the previous step's (d,p) */
+	int precision;           /* 0 "fp64": FP64 replica of the reference's iteration;
+	                            1 "mixed": FP32 multigrid-preconditioned inner CG inside the
+	                                FP64 Uzawa loop and FP64 iterative refinement (uniform meshes);
+	                            2 "fp64mg": the same converged solver with FP64 inner solves */
+	double stokes_rtol;      /* converged solvers: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
+	int warm_start;          /* converged solvers: start from the previous step's (d,p) */
 	double vis_min, vis_max; /* viscosity clip, applied when vis_max > 0 */
 	int mg_smooth;           /* damped-Jacobi sweeps per V-cycle side (2) */
 	double mg_omega;         /* Jacobi damping (0.6) */
+	int mg_coarse;           /* elements per side of the coarsest grid (4; 2..8) */
+	double outer_rtol;       /* Uzawa reduction per refinement pass (1e-3) */
+	double inner_rtol;       /* inner CG reduction (1e-4) */
+	int max_refine, max_outer, max_inner;  /* caps (20, 500, 200) */
+	int mg_eta_avg;          /* coarse viscosity: 0 injection, 1 full-weighted mean, 2 log-mean (2) */
+	int mg_block_n;          /* grids of at most this many elements per side run in one block (8) */
 } mclg_config;
 
 typedef struct mclg_step_stats {
@@ -110,6 +117,7 @@ typedef struct mclg_step_stats {
 	long long kernel_launches;            /* kernels launched by this step */
 	double solver_kernel_ms; /* device time of the Stokes solver kernel(s) of this step (CUDA events) */
 	long long solver_kernel_launches;
+	int refine_passes;       /* converged solvers: FP64 refinement passes (0 for the replica) */
 } mclg_step_stats;
 
 typedef struct mclg_ctx mclg_ctx;

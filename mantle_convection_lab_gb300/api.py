@@ -60,6 +60,9 @@ class Config(C.Structure):
         ("ic_mode_amp", C.c_double), ("ic_modes", C.c_int), ("precision", C.c_int),
         ("stokes_rtol", C.c_double), ("warm_start", C.c_int), ("vis_min", C.c_double),
         ("vis_max", C.c_double), ("mg_smooth", C.c_int), ("mg_omega", C.c_double),
+        ("mg_coarse", C.c_int), ("outer_rtol", C.c_double), ("inner_rtol", C.c_double),
+        ("max_refine", C.c_int), ("max_outer", C.c_int), ("max_inner", C.c_int),
+        ("mg_eta_avg", C.c_int), ("mg_block_n", C.c_int),
     ]
 
     @classmethod
@@ -83,7 +86,7 @@ class StepStats(C.Structure):
         ("model_time", C.c_double), ("res_momentum", C.c_double), ("res_continuity", C.c_double),
         ("ms_stokes", C.c_double), ("ms_heat", C.c_double), ("ms_total", C.c_double),
         ("kernel_launches", C.c_longlong), ("solver_kernel_ms", C.c_double),
-        ("solver_kernel_launches", C.c_longlong),
+        ("solver_kernel_launches", C.c_longlong), ("refine_passes", C.c_int),
     ]
 
     def as_dict(self):

@@ -124,19 +124,21 @@ __device__ __forceinline__ void gauss_eta(const DevLevel &L, const double *__res
 	}
 }
 
-// One thread per node: block row of K, F and Kdiag.
+// One thread per node: block row of K, F and Kdiag.  With withK == 0 only F
+// is formed (the matrix-free solvers never need the assembled K).
 __global__ void __launch_bounds__(kBlock) k_assemble_stokes(DevLevel L, const double *__restrict__ vis,
                                                             const double *__restrict__ buoy,
                                                             double4 *__restrict__ K, double2 *__restrict__ F,
-                                                            double2 *__restrict__ Kdiag)
+                                                            double2 *__restrict__ Kdiag, int withK)
 {
 	const int A = blockIdx.x * blockDim.x + threadIdx.x;
 	if (A >= L.nno)
 		return;
 	const int nno = L.nno, nel = L.nel, cnt = L.p2n_cnt[A];
 	const bool fr[2] = {vfree(L, A, 0), vfree(L, A, 1)};
-	for (int k = 0; k < L.nbw; k++)
-		K[(size_t)k * nno + A] = make_double4(0.0, 0.0, 0.0, 0.0);
+	if (withK)
+		for (int k = 0; k < L.nbw; k++)
+			K[(size_t)k * nno + A] = make_double4(0.0, 0.0, 0.0, 0.0);
 	double f[2] = {0.0, 0.0};
 	// pass 1: K entries and Dirichlet lifting (K_matrix, Build_matrix.c:42-115)
 	for (int s = 0; s < cnt; s++) {
@@ -150,6 +152,8 @@ __global__ void __launch_bounds__(kBlock) k_assemble_stokes(DevLevel L, const do
 			for (int j = 0; j < 2; j++)
 				for (int b = 0; b < 4; b++) {
 					const int B = L.ienl[b * nel + e];
+					if (!withK && vfree(L, B, j))
+						continue;
 					const double kv = ke_entry(etag, dxh, dzh, jac, a, i, b, j);
 					if (vfree(L, B, j)) {
 						const int slot = L.kslot[(a * 4 + b) * nel + e];
@@ -206,6 +210,8 @@ __global__ void __launch_bounds__(kBlock) k_assemble_stokes(DevLevel L, const do
 		}
 	}
 	F[A] = make_double2(fr[0] ? f[0] : 0.0, fr[1] ? f[1] : 0.0);
+	if (!withK)
+		return;
 	// Kdiag (Build_matrix.c:740-744): the self slot of the block row
 	double2 dg = make_double2(1.0, 1.0);
 	{

@@ -14,9 +14,15 @@ MCLG_SHAPE_UPLOAD(upload_shape_tables_heat)
 
 // calculate_artificial_diffusivity (Update_temperature.c:241-291)
 // Thread 0 also seeds the two minima of advection_dt with its 1e10 start value.
+// xi = coth(alpha) - 1/alpha.  The reference evaluates cosh(alpha)/sinh(alpha),
+// which overflows to inf/inf = NaN for |alpha| > 710; the heat solve then
+// stops at iteration 0 and T silently stays unchanged.  With safe != 0,
+// |alpha| > 20 uses coth = sign(alpha): for 20 < |alpha| <= 710 the reference's
+// ratio already rounds to exactly +-1, so results only differ where the
+// reference produces NaN.
 __global__ void __launch_bounds__(kBlock) k_tau(DevLevel L, const double2 *__restrict__ V, double accuracy,
                                                 double *__restrict__ tau0, double *__restrict__ tau1,
-                                                unsigned long long *__restrict__ mins)
+                                                unsigned long long *__restrict__ mins, int safe)
 {
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if (e == 0) {
@@ -36,7 +42,12 @@ __global__ void __launch_bounds__(kBlock) k_tau(DevLevel L, const double2 *__res
 			u[d] += 0.25 * (d == 0 ? v.x : v.y);
 		}
 		const double alpha = 0.5 * u[d] * Ld[d] / 1.0;
-		xi[d] = fabs(alpha) < accuracy ? 0.0 : cosh(alpha) / sinh(alpha) - 1.0 / alpha;
+		if (fabs(alpha) < accuracy)
+			xi[d] = 0.0;
+		else if (safe && fabs(alpha) > 20.0)
+			xi[d] = copysign(1.0, alpha) - 1.0 / alpha;
+		else
+			xi[d] = cosh(alpha) / sinh(alpha) - 1.0 / alpha;
 	}
 	const double us = u[0] * u[0] + u[1] * u[1];
 	const double kh = (xi[0] * u[0] * Ld[0] + xi[1] * u[1] * Ld[1]) * 0.5;

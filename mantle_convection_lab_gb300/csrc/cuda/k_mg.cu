@@ -1,0 +1,748 @@
+// Converged Stokes solve for uniform meshes: FP64 iterative refinement around
+// the reference's Uzawa iteration, whose inner velocity solves run as
+// multigrid-preconditioned CG in TI (float for the mixed-precision solver,
+// double for the plain FP64 one).  One persistent cooperative kernel per
+// time step; every loop has a cap.
+//
+//   refinement (FP64):  R = [F - K d - G p ; G^T d],  stop when |R|/|F| < rtol
+//   correction:        the Uzawa loop of citcom_solver (Solver.c:14-249) on
+//                      [K G; G^T 0][dd; dp] = [R_m; -R_c], preconditioned by
+//                      dividing by BAB (the reference multiplies by BAB,
+//                      Solver.c:133-134, which squares the viscosity contrast
+//                      instead of cancelling it), run to outer_rtol
+//   inner K^-1:         CG preconditioned by one V(nu,nu) cycle: damped Jacobi
+//                      smoothing, full-weighting restriction R = P^T, bilinear
+//                      prolongation P (coincident / edge / centre weights 1,
+//                      1/2, 1/4 as in interp_error, Solver.c:1009-1143),
+//                      re-discretised coarse operators with injected
+//                      viscosity, dense inverse on the coarsest grid.
+//
+// The operator is matrix-free.  A tile of 8 x 32 nodes stages its patch of
+// nodal velocity and viscosity (10 x 34 nodes) in shared memory, computes the
+// three stress components at the 4 Gauss points of each of its 9 x 33
+// elements into shared memory, then every thread gathers the two rows of its
+// own node from its 4 elements in a fixed order (deterministic, no atomics).
+// With D = diag(2 eta, 2 eta, eta) and unit-Jacobian derivatives
+// Dx = dN/dxi * sqrt(r), Dz = dN/deta / sqrt(r), r = dz/dx, this is exactly
+// the element matrix of get_element_K (Build_matrix.c:192-271).
+#include <math.h>
+#include "k_mg.cuh"
+
+namespace mclg {
+
+MCLG_SHAPE_UPLOAD(upload_shape_tables_mg)
+
+
+template <class T>
+struct OpTab {
+	T N[4][4], Dx[4][4], Dz[4][4];
+};
+__constant__ OpTab<float> cTf;
+__constant__ OpTab<double> cTd;
+template <class T> __device__ __forceinline__ const OpTab<T> &tab();
+template <> __device__ __forceinline__ const OpTab<float> &tab<float>() { return cTf; }
+template <> __device__ __forceinline__ const OpTab<double> &tab<double>() { return cTd; }
+
+// Fill the unit-Jacobian tables: r = dz/dx of the (square-per-level) elements.
+void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st)
+{
+	OpTab<double> d;
+	OpTab<float> f;
+	const double sr = sqrt(r);
+	for (int a = 0; a < 4; a++)
+		for (int g = 0; g < 4; g++) {
+			d.N[a][g] = S.N[a][g];
+			d.Dx[a][g] = S.dNdxi[a][g] * sr;
+			d.Dz[a][g] = S.dNdeta[a][g] / sr;
+			f.N[a][g] = (float)d.N[a][g];
+			f.Dx[a][g] = (float)d.Dx[a][g];
+			f.Dz[a][g] = (float)d.Dz[a][g];
+		}
+	cudaMemcpyToSymbolAsync(cTd, &d, sizeof d, 0, cudaMemcpyHostToDevice, st);
+	cudaMemcpyToSymbolAsync(cTf, &f, sizeof f, 0, cudaMemcpyHostToDevice, st);
+}
+
+// ---- small helpers ----------------------------------------------------------
+__device__ __forceinline__ void barrier(cg::grid_group &g, bool grid)
+{
+	if (grid)
+		g.sync();
+	else
+		__syncthreads();
+}
+
+__device__ __forceinline__ void span(bool grid, int &start, int &stride)
+{
+	if (grid) {
+		start = blockIdx.x * blockDim.x + threadIdx.x;
+		stride = gridDim.x * blockDim.x;
+	} else {
+		start = threadIdx.x;
+		stride = blockDim.x;
+	}
+}
+
+__device__ __forceinline__ unsigned spread_bits(unsigned v)
+{
+	v &= 0xffffu;
+	v = (v | (v << 8)) & 0x00ff00ffu;
+	v = (v | (v << 4)) & 0x0f0f0f0fu;
+	v = (v | (v << 2)) & 0x33333333u;
+	v = (v | (v << 1)) & 0x55555555u;
+	return v;
+}
+
+// Morton index of element (ex, ez) on a uniform mesh: x in the odd bits
+// (morton, Tree.c:447-456).
+__device__ __forceinline__ int morton(int ex, int ez)
+{
+	return (int)((spread_bits((unsigned)ex) << 1) | spread_bits((unsigned)ez));
+}
+
+// ---- the tiled matrix-free operator ----------------------------------------
+#include "k_tile.cuh"
+
+// Inverse diagonal of the level operator (the element diagonals summed).
+template <class T, class V>
+__device__ void level_invdiag(bool grid, int N, const unsigned char *mask, const T *eta, V *invD, double2 *kdiag64)
+{
+	const OpTab<T> &O = tab<T>();
+	const int n = N + 1;
+	int i0, st;
+	span(grid, i0, st);
+	for (int A = i0; A < n * n; A += st) {
+		const int ix = A / n, iz = A - ix * n;
+		T du = 0, dw = 0;
+		const int eox[4] = {ix - 1, ix - 1, ix, ix}, eoz[4] = {iz - 1, iz, iz, iz - 1}, ea[4] = {2, 3, 0, 1};
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const int ex = eox[q], ez = eoz[q];
+			if (ex < 0 || ex >= N || ez < 0 || ez >= N)
+				continue;
+			const T e[4] = {eta[ez + ex * n], eta[ez + 1 + ex * n], eta[ez + 1 + (ex + 1) * n], eta[ez + (ex + 1) * n]};
+			const int a = ea[q];
+#pragma unroll
+			for (int g = 0; g < 4; g++) {
+				T eg = 0;
+#pragma unroll
+				for (int c = 0; c < 4; c++)
+					eg += O.N[c][g] * e[c];
+				du += 2 * eg * O.Dx[a][g] * O.Dx[a][g] + eg * O.Dz[a][g] * O.Dz[a][g];
+				dw += 2 * eg * O.Dz[a][g] * O.Dz[a][g] + eg * O.Dx[a][g] * O.Dx[a][g];
+			}
+		}
+		const unsigned m = mask[A];
+		V v;
+		v.x = (m & 1u) ? T(0) : T(1) / du;
+		v.y = (m & 2u) ? T(0) : T(1) / dw;
+		invD[A] = v;
+		if (kdiag64)
+			kdiag64[A] = make_double2((m & 1u) ? 1.0 : (double)du, (m & 2u) ? 1.0 : (double)dw);
+	}
+}
+
+// b_c = P^T r_f over the coarse nodes (full weighting 1, 1/2, 1/4).
+template <class T, class V>
+__device__ void restrict_res(bool grid, const MGLevel<T> &F, const MGLevel<T> &C)
+{
+	int i0, st;
+	span(grid, i0, st);
+	for (int A = i0; A < C.n * C.n; A += st) {
+		const int cx = A / C.n, cz = A - cx * C.n;
+		T su = 0, sw = 0;
+#pragma unroll
+		for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
+			for (int dz = -1; dz <= 1; dz++) {
+				const int fx = 2 * cx + dx, fz = 2 * cz + dz;
+				if (fx < 0 || fx >= F.n || fz < 0 || fz >= F.n)
+					continue;
+				const T wgt = (dx == 0 ? T(1) : T(0.5)) * (dz == 0 ? T(1) : T(0.5));
+				const V r = F.r[fz + fx * F.n];
+				su += wgt * r.x;
+				sw += wgt * r.y;
+			}
+		const unsigned m = C.mask[A];
+		V o;
+		o.x = (m & 1u) ? T(0) : su;
+		o.y = (m & 2u) ? T(0) : sw;
+		C.b[A] = o;
+	}
+}
+
+// out = x_f + P x_c (bilinear).
+template <class T, class V>
+__device__ void prolong_add(bool grid, const MGLevel<T> &F, const V *xf, V *out, const MGLevel<T> &C, const V *xc)
+{
+	int i0, st;
+	span(grid, i0, st);
+	for (int A = i0; A < F.n * F.n; A += st) {
+		const int fx = A / F.n, fz = A - fx * F.n;
+		const int x0 = fx >> 1, z0 = fz >> 1, x1 = (fx + 1) >> 1, z1 = (fz + 1) >> 1;
+		const V a = xc[z0 + x0 * C.n], b = xc[z1 + x0 * C.n], c = xc[z0 + x1 * C.n], d = xc[z1 + x1 * C.n];
+		const T cu = T(0.25) * ((a.x + b.x) + (c.x + d.x)), cw = T(0.25) * ((a.y + b.y) + (c.y + d.y));
+		const unsigned m = F.mask[A];
+		V o = xf[A];
+		o.x = (m & 1u) ? T(0) : o.x + cu;
+		o.y = (m & 2u) ? T(0) : o.y + cw;
+		out[A] = o;
+	}
+}
+
+// x = omega D^-1 b (first smoothing sweep from a zero guess).
+template <class T, class V>
+__device__ void jacobi_first(bool grid, int n, const V *b, const V *invD, V *x, T omega)
+{
+	int i0, st;
+	span(grid, i0, st);
+	for (int A = i0; A < n * n; A += st) {
+		const V bv = b[A], dv = invD[A];
+		V o;
+		o.x = omega * dv.x * bv.x;
+		o.y = omega * dv.y * bv.y;
+		x[A] = o;
+	}
+}
+
+// ---- coarsest grid: dense inverse -------------------------------------------
+// Assemble the coarsest operator densely (FP64), put identity rows on the
+// Dirichlet dofs and invert it by Gauss-Jordan; block 0 only.
+template <class T>
+__device__ void coarse_build(MGHier<T> &H)
+{
+	const MGLevel<T> &L = H.lv[H.nlev - 1];
+	const OpTab<double> &O = tab<double>();
+	const int nd = H.cnd, n = L.n, N = L.N, w2 = 2 * nd;
+	double *M = H.cwork;
+	for (int k = threadIdx.x; k < nd * w2; k += blockDim.x)
+		M[k] = ((k % w2) == nd + k / w2) ? 1.0 : 0.0;
+	__syncthreads();
+	for (int e = 0; e < N * N; e++) {
+		const int ex = e / N, ez = e - ex * N;
+		const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
+		if (threadIdx.x < 64) {
+			const int p = threadIdx.x >> 3, q = threadIdx.x & 7;
+			const int a = p >> 1, i = p & 1, b = q >> 1, j = q & 1;
+			double kv = 0.0;
+			for (int g = 0; g < 4; g++) {
+				double eg = 0.0;
+				for (int c = 0; c < 4; c++)
+					eg += O.N[c][g] * (double)L.eta[cn[c]];
+				double t;
+				if (i == 0 && j == 0)
+					t = 2 * O.Dx[a][g] * O.Dx[b][g] + O.Dz[a][g] * O.Dz[b][g];
+				else if (i == 1 && j == 1)
+					t = 2 * O.Dz[a][g] * O.Dz[b][g] + O.Dx[a][g] * O.Dx[b][g];
+				else if (i == 0)
+					t = O.Dz[a][g] * O.Dx[b][g];
+				else
+					t = O.Dx[a][g] * O.Dz[b][g];
+				kv += eg * t;
+			}
+			M[(2 * cn[a] + i) * w2 + 2 * cn[b] + j] += kv;
+		}
+		__syncthreads();
+	}
+	// Dirichlet rows and columns -> identity
+	for (int k = threadIdx.x; k < nd * nd; k += blockDim.x) {
+		const int r = k / nd, c = k - r * nd;
+		const bool dr = (L.mask[r >> 1] >> (r & 1)) & 1u, dc = (L.mask[c >> 1] >> (c & 1)) & 1u;
+		if (dr || dc)
+			M[r * w2 + c] = (r == c) ? 1.0 : 0.0;
+	}
+	__syncthreads();
+	// Gauss-Jordan on [M | I]; the operator is SPD, no pivoting needed
+	for (int k = 0; k < nd; k++) {
+		__shared__ double piv;
+		if (threadIdx.x == 0)
+			piv = M[k * w2 + k];
+		__syncthreads();
+		for (int c = threadIdx.x; c < w2; c += blockDim.x)
+			M[k * w2 + c] /= piv;
+		__syncthreads();
+		for (int idx = threadIdx.x; idx < nd * w2; idx += blockDim.x) {
+			const int r = idx / w2, c = idx - r * w2;
+			if (r != k) {
+				const double f = M[r * w2 + k];
+				if (c != k)
+					M[r * w2 + c] -= f * M[k * w2 + c];
+			}
+		}
+		__syncthreads();
+		for (int r = threadIdx.x; r < nd; r += blockDim.x)
+			if (r != k)
+				M[r * w2 + k] = 0.0;
+		__syncthreads();
+	}
+	for (int k = threadIdx.x; k < nd * nd; k += blockDim.x)
+		H.cinv[k] = (T)M[(k / nd) * w2 + nd + (k % nd)];
+	__syncthreads();
+}
+
+template <class T, class V>
+__device__ void coarse_solve(const MGHier<T> &H, V *x)
+{
+	const MGLevel<T> &L = H.lv[H.nlev - 1];
+	const int nd = H.cnd;
+	const T *b = reinterpret_cast<const T *>(L.b);
+	T *xo = reinterpret_cast<T *>(x);
+	for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+		T s = 0;
+		for (int j = 0; j < nd; j++)
+			s += H.cinv[i * nd + j] * b[j];
+		xo[i] = s;
+	}
+	__syncthreads();
+}
+
+// ---- one V(nu,nu) cycle: out0 = B rhs0 -----------------------------------------
+// Levels below nblk run on the whole grid (grid barriers); the small levels
+// from nblk down run inside block 0 alone (block barriers).  Every block walks
+// the same buffer bookkeeping so that all of them know where each level's
+// result lies; only the active blocks do the work.
+template <class T>
+__device__ void level_down(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, int l,
+                           const typename V2T<T>::t *rhs0, bool grid, bool active, typename V2T<T>::t **xcur)
+{
+	typedef typename V2T<T>::t V;
+	const MGLevel<T> &L = H.lv[l];
+	const V *b = (l == 0) ? rhs0 : L.b;
+	V *x = L.xa, *xt = L.xb;
+	if (H.nu == 1) {
+		if (active) {
+			jacobi_first<T, V>(grid, L.n, b, L.invD, x, H.omega);
+			barrier(g, grid);
+		}
+	} else {
+		// sweep 1 (from zero) fused into sweep 2
+		if (active) {
+			tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr, XS_ZERO);
+			barrier(g, grid);
+		}
+		for (int s = 2; s < H.nu; s++) {
+			if (active) {
+				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, xt, PASS_SMOOTH, H.omega, nullptr);
+				barrier(g, grid);
+			}
+			V *tmp = x;
+			x = xt;
+			xt = tmp;
+		}
+	}
+	if (active) {
+		tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
+		barrier(g, grid);
+		restrict_res<T, V>(grid, L, H.lv[l + 1]);
+		barrier(g, grid);
+	}
+	xcur[l] = x;
+}
+
+template <class T>
+__device__ void level_up(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, int l,
+                         const typename V2T<T>::t *rhs0, typename V2T<T>::t *out0, bool grid, bool active,
+                         typename V2T<T>::t **xcur)
+{
+	typedef typename V2T<T>::t V;
+	const MGLevel<T> &L = H.lv[l];
+	const V *b = (l == 0) ? rhs0 : L.b;
+	V *x = xcur[l];
+	V *xt = (x == L.xa) ? L.xb : L.xa;
+	const MGLevel<T> &C = H.lv[l + 1];
+	// the coarse-grid correction x + P xc is formed inside the first post-smoothing sweep
+	for (int s = 0; s < H.nu; s++) {
+		V *dst = (l == 0 && s == H.nu - 1) ? out0 : xt;
+		if (active) {
+			if (s == 0)
+				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr,
+				                XS_PROLONG, xcur[l + 1], C.n);
+			else
+				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr);
+			barrier(g, grid);
+		}
+		xt = x;
+		x = dst;
+	}
+	xcur[l] = x;
+}
+
+template <class T>
+__device__ void vcycle(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, const typename V2T<T>::t *rhs0,
+                       typename V2T<T>::t *out0)
+{
+	typedef typename V2T<T>::t V;
+	V *xcur[kMaxLev];
+	const int lc = H.nlev - 1;
+	const int nb = H.nblk < lc ? H.nblk : lc;   // first block-local level; the coarsest always is
+	const bool b0 = blockIdx.x == 0;
+	for (int l = 0; l < lc; l++)
+		level_down<T>(g, sm, H, l, rhs0, l < nb, l < nb || b0, xcur);
+	if (b0)
+		coarse_solve<T, V>(H, H.lv[lc].xa);
+	xcur[lc] = H.lv[lc].xa;
+	for (int l = lc - 1; l >= 0; l--) {
+		if (l == nb - 1)
+			g.sync();   // block 0's coarse-level results become visible to every block
+		level_up<T>(g, sm, H, l, rhs0, out0, l < nb, l < nb || b0, xcur);
+	}
+	if (nb == 0)
+		g.sync();
+}
+
+// ---- inner solve: CG preconditioned by one V-cycle, all in T -----------------
+template <class T>
+__device__ int pcg_inner(cg::grid_group &g, unsigned char *sm, GridRed &red, const MGHier<T> &H,
+                         const typename V2T<T>::t *b, typename V2T<T>::t *x, double rtol, int maxit)
+{
+	typedef typename V2T<T>::t V;
+	const MGLevel<T> &L = H.lv[0];
+	const int nn = L.n * L.n;
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	V *r = H.pr, *z = H.pz, *p = H.pp, *q = H.pq;
+	double bb[1] = {0.0};
+	for (int A = tid; A < nn; A += nth) {
+		const V bv = b[A];
+		r[A] = bv;
+		V zero;
+		zero.x = T(0);
+		zero.y = T(0);
+		x[A] = zero;
+		bb[0] += (double)bv.x * bv.x + (double)bv.y * bv.y;
+	}
+	grid_reduce<1>(g, red, bb, 0u);
+	if (!(bb[0] > 0.0))
+		return 0;
+	vcycle<T>(g, sm, H, r, z);
+	double rz[1] = {0.0};
+	for (int A = tid; A < nn; A += nth) {
+		const V rv = r[A], zv = z[A];
+		rz[0] += (double)rv.x * zv.x + (double)rv.y * zv.y;
+		p[A] = zv;
+	}
+	grid_reduce<1>(g, red, rz, 0u);
+	double rho = rz[0];
+	int it = 0;
+	while (it < maxit) {
+		double pq[1];
+		tile_pass<T, V>(sm, true, L.N, L.mask, L.eta, p, nullptr, nullptr, q, PASS_MATVEC, T(0), pq);
+		grid_reduce<1>(g, red, pq, 0u);
+		const double alpha = rho / pq[0];
+		double rr[1] = {0.0};
+		for (int A = tid; A < nn; A += nth) {
+			V xv = x[A], rv = r[A];
+			const V pv = p[A], qv = q[A];
+			xv.x += (T)alpha * pv.x;
+			xv.y += (T)alpha * pv.y;
+			rv.x -= (T)alpha * qv.x;
+			rv.y -= (T)alpha * qv.y;
+			x[A] = xv;
+			r[A] = rv;
+			rr[0] += (double)rv.x * rv.x + (double)rv.y * rv.y;
+		}
+		grid_reduce<1>(g, red, rr, 0u);
+		it++;
+		if (!(rr[0] > rtol * rtol * bb[0]) || !isfinite(alpha))
+			break;
+		vcycle<T>(g, sm, H, r, z);
+		double rz2[1] = {0.0};
+		for (int A = tid; A < nn; A += nth) {
+			const V rv = r[A], zv = z[A];
+			rz2[0] += (double)rv.x * zv.x + (double)rv.y * zv.y;
+		}
+		grid_reduce<1>(g, red, rz2, 0u);
+		const double beta = rz2[0] / rho;
+		rho = rz2[0];
+		for (int A = tid; A < nn; A += nth) {
+			const V zv = z[A];
+			V pv = p[A];
+			pv.x = zv.x + (T)beta * pv.x;
+			pv.y = zv.y + (T)beta * pv.y;
+			p[A] = pv;
+		}
+		g.sync();
+	}
+	g.sync();
+	return it;
+}
+
+// ---- FP64 operators on the fine uniform mesh -----------------------------------
+__device__ __forceinline__ void g_entries(double hx, double hz, int a, double &g0, double &g1)
+{
+	element_g(cS, hz, hx, a, g0, g1);
+}
+
+// y = G s at every node (masked); s in Morton order.
+__device__ void gmul64(int N0, const unsigned char *mask, double hx, double hz, const double *s, double2 *y,
+                       int tid, int nth)
+{
+	const int n = N0 + 1;
+	for (int A = tid; A < n * n; A += nth) {
+		const int ix = A / n, iz = A - ix * n;
+		double s0 = 0.0, s1 = 0.0;
+		const int eox[4] = {ix - 1, ix - 1, ix, ix}, eoz[4] = {iz - 1, iz, iz, iz - 1}, ea[4] = {2, 3, 0, 1};
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const int ex = eox[q], ez = eoz[q];
+			if (ex < 0 || ex >= N0 || ez < 0 || ez >= N0)
+				continue;
+			double g0, g1;
+			g_entries(hx, hz, ea[q], g0, g1);
+			const double se = s[morton(ex, ez)];
+			s0 += g0 * se;
+			s1 += g1 * se;
+		}
+		const unsigned m = mask[A];
+		y[A] = make_double2((m & 1u) ? 0.0 : s0, (m & 2u) ? 0.0 : s1);
+	}
+}
+
+// (G^T u)_e at element (ex, ez), free dofs in ascending equation order.
+__device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask, double hx, double hz,
+                                               const double2 *u, int ex, int ez)
+{
+	const int n = N0 + 1;
+	const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
+	double s = 0.0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		double g0, g1;
+		g_entries(hx, hz, a, g0, g1);
+		const double2 ua = u[cn[a]];
+		const unsigned m = mask[cn[a]];
+		if (!(m & 1u))
+			s += g0 * ua.x;
+		if (!(m & 2u))
+			s += g1 * ua.y;
+	}
+	return s;
+}
+
+// ---- the persistent kernel ----------------------------------------------------
+template <class TI>
+__global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
+{
+	typedef typename V2T<TI>::t VI;
+	cg::grid_group g = cg::this_grid();
+	__shared__ __align__(16) unsigned char sm[kSmemBytes];
+	GridRed red = a.red;
+	MGHier<TI> &H = a.H;
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	int *status = &a.sc->status;
+
+	// -- per-step setup: viscosity on every level, inverse diagonals, BAB, coarse inverse
+	for (int A = tid; A < nn; A += nth)
+		H.lv[0].eta[A] = (TI)a.vis[A];
+	g.sync();
+	for (int l = 1; l < H.nlev; l++) {
+		const MGLevel<TI> &C = H.lv[l], &F = H.lv[l - 1];
+		for (int A = tid; A < C.n * C.n; A += nth) {
+			const int cx = A / C.n, cz = A - cx * C.n;
+			if (H.eta_avg == 0) {
+				C.eta[A] = F.eta[2 * cz + 2 * cx * F.n];
+			} else {
+				double s = 0.0, wsum = 0.0;
+				for (int dx = -1; dx <= 1; dx++)
+					for (int dz = -1; dz <= 1; dz++) {
+						const int fx = 2 * cx + dx, fz = 2 * cz + dz;
+						if (fx < 0 || fx >= F.n || fz < 0 || fz >= F.n)
+							continue;
+						const double w = (dx == 0 ? 1.0 : 0.5) * (dz == 0 ? 1.0 : 0.5);
+						const double ev = (double)F.eta[fz + fx * F.n];
+						s += w * (H.eta_avg == 2 ? log(ev) : ev);
+						wsum += w;
+					}
+				s /= wsum;
+				C.eta[A] = (TI)(H.eta_avg == 2 ? exp(s) : s);
+			}
+		}
+		g.sync();
+	}
+	for (int l = 0; l < H.nlev; l++)
+		level_invdiag<TI, VI>(true, H.lv[l].N, H.lv[l].mask, H.lv[l].eta, H.lv[l].invD, nullptr);
+	level_invdiag<double, double2>(true, N0, a.mask0, a.vis, a.invD64, a.kdiag64);
+	g.sync();
+	for (int e = tid; e < ne; e += nth) {
+		const int ex = e / N0, ez = e - ex * N0;
+		const int cn[4] = {ez + ex * n0, ez + 1 + ex * n0, ez + 1 + (ex + 1) * n0, ez + (ex + 1) * n0};
+		double s = 0.0;
+#pragma unroll
+		for (int c = 0; c < 4; c++) {
+			const int ac = kSortedCorner[c];
+			double g0, g1;
+			g_entries(a.hx, a.hz, ac, g0, g1);
+			const double2 kd = a.kdiag64[cn[ac]];
+			const unsigned m = a.mask0[cn[ac]];
+			if (!(m & 1u))
+				s += g0 * g0 / kd.x;
+			if (!(m & 2u))
+				s += g1 * g1 / kd.y;
+		}
+		a.bab[morton(ex, ez)] = s;
+	}
+	if (blockIdx.x == 0)
+		coarse_build<TI>(H);
+	g.sync();
+
+	int refine = 0, outer_total = 0, inner_total = 0;
+	double res_m = 0.0, res_c = 0.0, fnorm = 1.0;
+	while (true) {
+		// -- FP64 residual R = [F - K d - G p ; G^T d]
+		tile_pass<double, double2>(sm, true, N0, a.mask0, a.vis, a.d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0,
+		                           nullptr);
+		gmul64(N0, a.mask0, a.hx, a.hz, a.p, a.R, tid, nth);
+		g.sync();
+		double rs[3] = {0.0, 0.0, 0.0};
+		for (int A = tid; A < nn; A += nth) {
+			const double2 f = a.F[A], kd = a.Kd[A], gp = a.R[A];
+			const double2 r = make_double2(f.x - kd.x - gp.x, f.y - kd.y - gp.y);
+			a.R[A] = r;
+			rs[0] += r.x * r.x + r.y * r.y;
+			rs[2] += f.x * f.x + f.y * f.y;
+		}
+		for (int e = tid; e < ne; e += nth) {
+			const int ex = e / N0, ez = e - ex * N0;
+			const double c = gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.d, ex, ez);
+			a.Rc[morton(ex, ez)] = c;
+			rs[1] += c * c;
+		}
+		grid_reduce<3>(g, red, rs, 0u);
+		fnorm = sqrt(rs[2]);
+		res_m = sqrt(rs[0]) / fnorm;
+		res_c = sqrt(rs[1]) / fnorm;
+		const double res = sqrt(rs[0] + rs[1]) / fnorm;
+		if (!(res >= a.rtol) || refine >= a.max_refine || !isfinite(res))
+			break;
+		refine++;
+
+		// -- correction solve: Uzawa on [K G; G^T 0][dd; dp] = [R_m; -R_c]
+		VI *bI = H.lv[0].b, *xI = H.px;   // level-0 buffers double as CG input/output here
+		for (int A = tid; A < nn; A += nth) {
+			const double2 r = a.R[A];
+			VI v;
+			v.x = (TI)r.x;
+			v.y = (TI)r.y;
+			bI[A] = v;
+		}
+		g.sync();
+		inner_total += pcg_inner<TI>(g, sm, red, H, bI, xI, a.inner_rtol, a.max_inner);
+		for (int A = tid; A < nn; A += nth) {
+			const VI v = xI[A];
+			a.dd[A] = make_double2((double)v.x, (double)v.y);
+		}
+		g.sync();
+		double *r0 = a.r0, *r1 = a.r1, *r2 = a.r2, *z0 = a.z0, *z1 = a.z1, *s1 = a.s1, *s2 = a.s2;
+		double c0[1] = {0.0};
+		for (int e = tid; e < ne; e += nth) {
+			const int ex = e / N0, ez = e - ex * N0;
+			const int me = morton(ex, ez);
+			const double v = a.Rc[me] + gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.dd, ex, ez);
+			r1[me] = v;
+			a.dpv[me] = 0.0;
+			c0[0] += v * v;
+		}
+		grid_reduce<1>(g, red, c0, 0u);
+		const double rnorm0 = sqrt(c0[0]);
+		double rnorm = rnorm0;
+		int cycle = 0;
+		while (cycle < a.max_outer && rnorm > a.outer_rtol * rnorm0 && rnorm > 0.0) {
+			double rz[2] = {0.0, 0.0};
+			for (int e = tid; e < ne; e += nth) {
+				const double z = r1[e] / a.bab[e];
+				z1[e] = z;
+				rz[0] += r1[e] * z;
+				if (cycle > 0)
+					rz[1] += r0[e] * z0[e];
+			}
+			grid_reduce<2>(g, red, rz, 0u);
+			const double delta = cycle == 0 ? 0.0 : rz[0] / rz[1];
+			for (int e = tid; e < ne; e += nth)
+				s2[e] = cycle == 0 ? z1[e] : z1[e] + delta * s1[e];
+			g.sync();
+			gmul64(N0, a.mask0, a.hx, a.hz, s2, a.u1, tid, nth);
+			for (int A = tid; A < nn; A += nth) {
+				const double2 v = a.u1[A];
+				VI w;
+				w.x = (TI)v.x;
+				w.y = (TI)v.y;
+				bI[A] = w;
+			}
+			g.sync();
+			inner_total += pcg_inner<TI>(g, sm, red, H, bI, xI, a.inner_rtol, a.max_inner);
+			for (int A = tid; A < nn; A += nth) {
+				const VI v = xI[A];
+				a.u1[A] = make_double2((double)v.x, (double)v.y);
+			}
+			g.sync();
+			double sa[1] = {0.0};
+			for (int e = tid; e < ne; e += nth) {
+				const int ex = e / N0, ez = e - ex * N0;
+				const int me = morton(ex, ez);
+				const double t = gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.u1, ex, ez);
+				a.Ahp[me] = t;
+				sa[0] += s2[me] * t;
+			}
+			grid_reduce<1>(g, red, sa, 0u);
+			const double alpha = rz[0] / sa[0];
+			double rr[1] = {0.0};
+			for (int e = tid; e < ne; e += nth) {
+				const double v = r1[e] - alpha * a.Ahp[e];
+				r2[e] = v;
+				a.dpv[e] += alpha * s2[e];
+				rr[0] += v * v;
+			}
+			for (int A = tid; A < nn; A += nth) {
+				const double2 u = a.u1[A];
+				double2 v = a.dd[A];
+				v.x -= alpha * u.x;
+				v.y -= alpha * u.y;
+				a.dd[A] = v;
+			}
+			grid_reduce<1>(g, red, rr, 0u);
+			rnorm = sqrt(rr[0]);
+			cycle++;
+			double *sh = s1; s1 = s2; s2 = sh;
+			sh = r0; r0 = r1; r1 = r2; r2 = sh;
+			sh = z0; z0 = z1; z1 = sh;
+			if (!isfinite(alpha) || !isfinite(rnorm)) {
+				if (tid == 0)
+					atomicOr(status, 2);
+				break;
+			}
+		}
+		outer_total += cycle;
+		// apply the correction in FP64
+		for (int A = tid; A < nn; A += nth) {
+			const double2 c = a.dd[A];
+			double2 v = a.d[A];
+			v.x += c.x;
+			v.y += c.y;
+			a.d[A] = v;
+		}
+		for (int e = tid; e < ne; e += nth)
+			a.p[e] += a.dpv[e];
+		g.sync();
+	}
+	if (refine >= a.max_refine && tid == 0)
+		atomicOr(status, 1);
+	// nodal velocity (v_to_nodes, Solver.c:1319-1343)
+	for (int A = tid; A < nn; A += nth) {
+		const double2 dv = a.d[A];
+		const unsigned m = a.mask0[A];
+		a.V[A] = make_double2((m & 1u) ? a.vbcval[A] : dv.x, (m & 2u) ? a.vbcval[nn + A] : dv.y);
+	}
+	if (tid == 0) {
+		a.sc->uzawa_cycles = outer_total;
+		a.sc->cg_cycles = inner_total;
+		a.sc->refine_passes = refine;
+		a.sc->res_m = res_m;
+		a.sc->res_c = res_c;
+		a.sc->dv = 0.0;
+		a.sc->dp = 0.0;
+	}
+}
+
+void *stokes_mg_kernel(int fp64) { return fp64 ? (void *)k_stokes_mg<double> : (void *)k_stokes_mg<float>; }
+
+}  // namespace mclg

@@ -5,7 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <vector>
-#include "mclg_dev.cuh"
+#include "k_mg.cuh"
 #include "../host/mclg_host.h"
 
 namespace mclg {
@@ -18,7 +18,10 @@ __global__ void k_buoy_rowavg(DevLevel L, const double *T, double Ra, double *av
 __global__ void k_buoy_vis(DevLevel L, const double *T, double Ra, const double *avg, double Aexp, double refT,
                            double lm_jump, double vmin, double vmax, double *buoy, double *vis);
 __global__ void k_assemble_stokes(DevLevel L, const double *vis, const double *buoy, double4 *K, double2 *F,
-                                  double2 *Kdiag);
+                                  double2 *Kdiag, int withK);
+void upload_shape_tables_mg(const ShapeTables &s, cudaStream_t st);
+void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st);
+void *stokes_mg_kernel(int fp64);
 __global__ void k_bab(DevLevel L, const double2 *Kdiag, double *bab);
 __global__ void k_stress_elem(DevLevel L, const double *vis, const double2 *V, double *se);
 __global__ void k_elem_to_node(DevLevel L, const double *pe, double *pn);
@@ -26,7 +29,7 @@ __global__ void k_kmul(DevLevel L, const double4 *K, const double2 *x, double2 *
 __global__ void k_gmul(DevLevel L, const double *p, double2 *y);
 __global__ void k_gtmul(DevLevel L, const double2 *u, double *p);
 __global__ void k_tau(DevLevel L, const double2 *V, double accuracy, double *tau0, double *tau1,
-                      unsigned long long *mins);
+                      unsigned long long *mins, int safe);
 __global__ void k_assemble_heat(DevLevel L, const double2 *V, const double *tau0, const double *tau1, double Q,
                                 double *HK, double *HC, double *HF);
 __global__ void k_heat_dt(DevLevel L, const double2 *V, unsigned long long *mins);
@@ -75,6 +78,12 @@ struct mclg_ctx {
 	long long launches;
 	// scratch for the parity API
 	double *tmpA, *tmpB;
+	// converged solvers on uniform meshes (precision 1 and 2)
+	int coop_mg;
+	MGArgs<float> mgf;
+	MGArgs<double> mgd;
+	void *mg_ptr[192];
+	int mg_nptr;
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -227,6 +236,150 @@ static int coop_blocks(void *kernel, int num_sms, int work)
 	return nb < 1 ? 1 : nb;
 }
 
+// ---- converged solvers: hierarchy of the uniform mesh -------------------------
+template <class T>
+static cudaError_t mg_alloc(mclg_ctx *c, T **p, size_t n)
+{
+	if (c->mg_nptr >= (int)(sizeof c->mg_ptr / sizeof c->mg_ptr[0]))
+		return cudaErrorMemoryAllocation;
+	cudaError_t e = cudaMalloc((void **)p, (n + 1) * sizeof(T));
+	if (e == cudaSuccess) {
+		c->mg_ptr[c->mg_nptr++] = *p;
+		cudaMemsetAsync(*p, 0, (n + 1) * sizeof(T), c->st);
+	}
+	return e;
+}
+
+// Level l has N0 >> l elements per side; its node (cx, cz) is the fine node
+// (cx << l, cz << l), whose BC codes give the Dirichlet mask.
+template <class TI>
+static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
+{
+	typedef typename V2T<TI>::t VI;
+	const mclg_mesh &m = c->mesh;
+	const mclg_level &H = m.lev[c->fl];
+	const int N0 = m.max_elx[c->fl], n0 = N0 + 1;
+	int Nc = c->cfg.mg_coarse;
+	if (Nc < 2 || Nc > 8 || (Nc & (Nc - 1)) || Nc > N0) {
+		mclg_set_error("mg_coarse=%d: need a power of two in [2, min(8, %d)]", Nc, N0);
+		return MCLG_BAD_INPUT;
+	}
+	memset(&a, 0, sizeof a);
+	int nlev = 1;
+	while ((N0 >> (nlev - 1)) > Nc)
+		nlev++;
+	if (nlev > kMaxLev || nlev < 2) {
+		mclg_set_error("%d multigrid levels from %d to %d elements per side: need 2..%d", nlev, N0, Nc, kMaxLev);
+		return MCLG_BAD_INPUT;
+	}
+	a.H.nlev = nlev;
+	a.H.nblk = nlev;
+	for (int l = 0; l < nlev; l++)
+		if ((N0 >> l) <= c->cfg.mg_block_n) {   // small grids: one block beats grid barriers
+			a.H.nblk = l;
+			break;
+		}
+	std::vector<unsigned char> mk;
+	for (int l = 0; l < nlev; l++) {
+		MGLevel<TI> &L = a.H.lv[l];
+		L.N = N0 >> l;
+		L.n = L.N + 1;
+		const size_t nn = (size_t)L.n * L.n;
+		mk.assign(nn, 0);
+		for (int cx = 0; cx < L.n; cx++)
+			for (int cz = 0; cz < L.n; cz++) {
+				const size_t Af = (size_t)(cz << l) + (size_t)(cx << l) * n0;
+				mk[cz + (size_t)cx * L.n] = (unsigned char)((H.v_bc[Af] == 'V' ? 1 : 0) |
+				                                            (H.v_bc[(size_t)H.nno + Af] == 'V' ? 2 : 0));
+			}
+		unsigned char *dm;
+		CK(mg_alloc(c, &dm, nn));
+		CK(cudaMemcpyAsync(dm, mk.data(), nn, cudaMemcpyHostToDevice, c->st));
+		CK(cudaStreamSynchronize(c->st));
+		L.mask = dm;
+		CK(mg_alloc(c, &L.eta, nn));
+		CK(mg_alloc(c, &L.invD, nn));
+		CK(mg_alloc(c, &L.xa, nn));
+		CK(mg_alloc(c, &L.xb, nn));
+		CK(mg_alloc(c, &L.b, nn));
+		CK(mg_alloc(c, &L.r, nn));
+		if (l == 0)
+			a.mask0 = dm;
+	}
+	const int ncn = a.H.lv[nlev - 1].n;
+	a.H.cnd = 2 * ncn * ncn;
+	CK(mg_alloc(c, &a.H.cinv, (size_t)a.H.cnd * a.H.cnd));
+	CK(mg_alloc(c, &a.H.cwork, (size_t)a.H.cnd * 2 * a.H.cnd));
+	a.H.omega = (TI)c->cfg.mg_omega;
+	a.H.nu = c->cfg.mg_smooth < 1 ? 1 : c->cfg.mg_smooth;
+	a.H.eta_avg = c->cfg.mg_eta_avg;
+	const size_t nn0 = (size_t)n0 * n0, ne = (size_t)N0 * N0;
+	CK(mg_alloc(c, &a.H.px, nn0));
+	CK(mg_alloc(c, &a.H.pr, nn0));
+	CK(mg_alloc(c, &a.H.pz, nn0));
+	CK(mg_alloc(c, &a.H.pp, nn0));
+	CK(mg_alloc(c, &a.H.pq, nn0));
+	a.N0 = N0;
+	a.hx = 0.5 * m.dx[c->fl];
+	a.hz = 0.5 * m.dz[c->fl];
+	a.vis = c->vis;
+	a.vbcval = c->lb.vbcval;
+	a.F = c->F;
+	a.d = c->d;
+	a.p = c->p;
+	a.V = c->V;
+	CK(mg_alloc(c, &a.R, nn0));
+	CK(mg_alloc(c, &a.dd, nn0));
+	CK(mg_alloc(c, &a.u1, nn0));
+	CK(mg_alloc(c, &a.Kd, nn0));
+	CK(mg_alloc(c, &a.invD64, nn0));
+	CK(mg_alloc(c, &a.kdiag64, nn0));
+	double **ev[] = {&a.Rc, &a.r0, &a.r1, &a.r2, &a.z0, &a.z1, &a.s1, &a.s2, &a.Ahp, &a.dpv, &a.bab};
+	for (double **pp : ev)
+		CK(mg_alloc(c, pp, ne));
+	a.red.part = c->red_part;
+	a.sc = c->sc;
+	a.rtol = c->cfg.stokes_rtol;
+	a.outer_rtol = c->cfg.outer_rtol;
+	a.inner_rtol = c->cfg.inner_rtol;
+	a.max_refine = c->cfg.max_refine;
+	a.max_outer = c->cfg.max_outer;
+	a.max_inner = c->cfg.max_inner;
+	(void)sizeof(VI);
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+static int launch_stokes_mg(mclg_ctx *c)
+{
+	const mclg_config &f = c->cfg;
+	// warm_start: 0 = zero guess; 1 = previous (d, p); 2 = the reference's
+	// policy for zero_P=0 (initial_d_p, Solver.c:251-278): d zeroed, p kept
+	if (f.warm_start != 1)
+		CK(cudaMemsetAsync(c->d, 0, c->L.nno * sizeof(double2), c->st));
+	if (f.warm_start == 0)
+		CK(cudaMemsetAsync(c->p, 0, c->L.nel * sizeof(double), c->st));
+	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
+	if (f.precision == 2) {
+		void *args[] = {&c->mgd};
+		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(1), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
+	} else {
+		void *args[] = {&c->mgf};
+		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(0), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
+	}
+	c->launches++;
+	return MCLG_OK;
+}
+
+extern "C" {
+static int launch_uzawa(mclg_ctx *c);
+}
+
+static int launch_stokes(mclg_ctx *c)
+{
+	return c->cfg.precision == 0 ? launch_uzawa(c) : launch_stokes_mg(c);
+}
+
 extern "C" {
 
 const char *mclg_status_string(int s)
@@ -363,6 +516,23 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 	const int work = (int)(nn > ne ? nn : ne);
 	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(), c->num_sms, work);
 	c->coop_heat = coop_blocks(heat_cg_kernel_ptr(), c->num_sms, (int)nn);
+	if (cfg->precision != 0) {
+		if (!c->mesh.uniform) {
+			mclg_set_error("precision=mixed/fp64mg needs a uniform mesh (develop_mode=0); use precision=fp64");
+			mclg_destroy(c);
+			*out = NULL;
+			return MCLG_BAD_INPUT;
+		}
+		rc = cfg->precision == 2 ? mg_setup<double>(c, c->mgd) : mg_setup<float>(c, c->mgf);
+		if (rc != MCLG_OK) {
+			mclg_destroy(c);
+			*out = NULL;
+			return rc;
+		}
+		upload_shape_tables_mg(S, c->st);
+		upload_op_tables(S, c->mesh.dz[c->fl] / c->mesh.dx[c->fl], c->st);
+		c->coop_mg = coop_blocks(stokes_mg_kernel(cfg->precision == 2), c->num_sms, 1 << 30);
+	}
 	if (c->coop_uzawa < 1 || c->coop_heat < 1) {
 		mclg_set_error("cooperative occupancy query failed");
 		mclg_destroy(c);
@@ -393,6 +563,8 @@ void mclg_destroy(mclg_ctx *c)
 	for (int i = 0; i < 8; i++)
 		if (c->pe[i])
 			cudaFree(c->pe[i]);
+	for (int i = 0; i < c->mg_nptr; i++)
+		cudaFree(c->mg_ptr[i]);
 	if (c->sc_host)
 		cudaFreeHost(c->sc_host);
 	for (int i = 0; i < 6; i++)
@@ -466,9 +638,11 @@ int mclg_velocity_pressure_KGF_matrix(mclg_ctx *c)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	k_assemble_stokes<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->vis, c->buoy, c->K, c->F, c->Kdiag);
+	const int withK = c->cfg.precision == 0;
+	k_assemble_stokes<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->vis, c->buoy, c->K, c->F, c->Kdiag,
+	                                                               withK);
 	int rc = check_launch(c, "k_assemble_stokes");
-	if (rc)
+	if (rc || !withK)
 		return rc;
 	k_inv_diag2<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L.nno, c->Kdiag, c->idiag);
 	if ((rc = check_launch(c, "k_inv_diag2")))
@@ -571,13 +745,14 @@ static void fill_stats_stokes(mclg_ctx *c, mclg_step_stats *st)
 	st->res_momentum = s.res_m;
 	st->res_continuity = s.res_c;
 	st->status = status_from_bits(s.status);
+	st->refine_passes = s.refine_passes;
 }
 
 int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	int rc = launch_uzawa(c);
+	int rc = launch_stokes(c);
 	if (rc)
 		return rc;
 	if ((rc = launch_stress(c)))
@@ -593,7 +768,8 @@ static int launch_heat(mclg_ctx *c)
 	const mclg_config &f = c->cfg;
 	const DevLevel &L = c->L;
 	int rc;
-	k_tau<<<blocks_for(L.nel), kBlock, 0, c->st>>>(L, c->V, f.accuracy, c->tau0, c->tau1, c->mins);
+	k_tau<<<blocks_for(L.nel), kBlock, 0, c->st>>>(L, c->V, f.accuracy, c->tau0, c->tau1, c->mins,
+	                                                f.precision != 0);
 	if ((rc = check_launch(c, "k_tau")))
 		return rc;
 	k_assemble_heat<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->V, c->tau0, c->tau1, f.Q, c->HK, c->HC, c->HF);
@@ -686,7 +862,7 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 	if ((rc = mclg_velocity_pressure_KGF_matrix(c)))
 		return rc;
 	CK(cudaEventRecord(c->ev[4], c->st));
-	if ((rc = launch_uzawa(c)))
+	if ((rc = launch_stokes(c)))
 		return rc;
 	CK(cudaEventRecord(c->ev[5], c->st));
 	if ((rc = launch_stress(c)))

@@ -75,6 +75,7 @@ struct StepScalars {
 	double dv, dp;
 	double res_m, res_c, fnorm;
 	int uzawa_cycles, cg_cycles, heat_cycles, status;
+	int refine_passes;
 };
 
 // ---- deterministic grid-wide reductions -----------------------------------

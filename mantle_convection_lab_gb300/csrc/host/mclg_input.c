@@ -207,6 +207,14 @@ void mclg_config_defaults(mclg_config *c)
 	c->stokes_rtol = 1e-8;
 	c->mg_smooth = 2;
 	c->mg_omega = 0.6;
+	c->mg_coarse = 4;
+	c->outer_rtol = 1e-3;
+	c->inner_rtol = 1e-4;
+	c->max_refine = 20;
+	c->max_outer = 500;
+	c->max_inner = 200;
+	c->mg_eta_avg = 2;
+	c->mg_block_n = 8;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -282,13 +290,21 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_double(&pl, "ic_mode_amp", &c->ic_mode_amp, 0.005);
 	/* GB300 solver options */
 	get_string(&pl, "precision", buf, sizeof buf, "fp64");
-	c->precision = (strcmp(buf, "mixed") == 0) ? 1 : 0;
+	c->precision = (strcmp(buf, "mixed") == 0) ? 1 : (strcmp(buf, "fp64mg") == 0) ? 2 : 0;
 	get_double(&pl, "stokes_rtol", &c->stokes_rtol, 1e-8);
 	get_int(&pl, "warm_start", &c->warm_start, 0);
 	get_double(&pl, "vis_min", &c->vis_min, 0.0);
 	get_double(&pl, "vis_max", &c->vis_max, 0.0);
 	get_int(&pl, "mg_smooth", &c->mg_smooth, 2);
 	get_double(&pl, "mg_omega", &c->mg_omega, 0.6);
+	get_int(&pl, "mg_coarse", &c->mg_coarse, 4);
+	get_double(&pl, "outer_rtol", &c->outer_rtol, 1e-3);
+	get_double(&pl, "inner_rtol", &c->inner_rtol, 1e-4);
+	get_int(&pl, "max_refine", &c->max_refine, 20);
+	get_int(&pl, "max_outer", &c->max_outer, 500);
+	get_int(&pl, "max_inner", &c->max_inner, 200);
+	get_int(&pl, "mg_eta_avg", &c->mg_eta_avg, 2);
+	get_int(&pl, "mg_block_n", &c->mg_block_n, 8);
 	free(pl.e);
 	return MCLG_OK;
 }
