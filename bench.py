@@ -4,24 +4,31 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gb300|reference]
 
 A step is one pass of the reference's per-step sequence (Main.c:58-64):
-buoyancy, viscosity, K/F/G assembly, the Uzawa Stokes solve to the
-configured tolerance, stress, and the SUPG temperature update.  The inputs
-are the seeded synthetic .input workloads in mantle_convection_lab_gb300/configs.
+buoyancy, viscosity, K/F/G assembly, the Stokes solve, stress, and the SUPG
+temperature update, on seeded synthetic .input workloads
+(mantle_convection_lab_gb300/configs).
 
-One JSON line on rank 0:
-  value      steps/s over all ranks, device time (CUDA events on the engine's
-             stream), fields resident in HBM, L2 flushed between steps
-  e2e        steps/s through mclg_step_host: temperature copied in from pinned
-             host memory and T, V, P copied back every step
-  roofline   the persistent Stokes solver kernel: algorithmic bytes per launch
-             (per-iteration byte counts x measured iteration counts) / its
-             CUDA-event duration, against the measured HBM copy bandwidth
+Default workload -- configuration 3: 1024 x 1024 uniform Q1/P0 mesh, Ra=1e8,
+eta = exp(-ln(1e5) T) clipped to [1e-5, 1], every step solved to a true
+Stokes residual |[F - K d - G p; G^T d]|/|F| < 1e-8.
+  value      steps/s of the mixed-precision solver (FP32 multigrid-preconditioned
+             inner CG inside the FP64 Uzawa loop and FP64 iterative refinement),
+             warm-started from the previous step; device time (CUDA events on
+             the engine's stream), fields resident in HBM, working set larger
+             than L2 is not guaranteed so L2 is flushed (256 MB write) between steps
+  plain_fp64 the same solve with FP64 inner solves and the reference's start
+             (d = 0, p kept: initial_d_p, Solver.c:251-278)
+  e2e        steps/s through mclg_step_host: T copied in from pinned host memory
+             and T, V, P copied back every step
+  roofline   the persistent Stokes kernel: algorithmic bytes per launch (per-pass
+             byte counts x measured iteration counts) / its CUDA-event duration,
+             against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (a restatement of the reference's algorithm that
              reproduces it bit for bit) timed on this host's cores on a bounded sample
 
-Under torchrun every rank runs an independent replica (the single-model path
-does not shard; ensembles shard by model) and value is the sum over ranks.
---impl reference times the reference's CPU algorithm (the oracle) instead.
+Under torchrun every rank runs an independent replica (one model per GPU:
+the single-model path does not shard) and value is the sum over ranks.
+--impl reference times the reference's own CPU algorithm (the oracle).
 """
 import argparse
 import json
@@ -36,14 +43,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
+    "cfg3_mg_1024": {
+        "input": "mantle_convection_lab_gb300/configs/cfg3_mg_1024.input",
+        "kind": "converged",
+        "desc": "configuration 3: 1024x1024 uniform Q1/P0, Ra=1e8, eta=exp(-ln(1e5) T) in [1e-5,1], "
+                "tanh boundary layers + 8 seeded modes, free slip; true Stokes residual < 1e-8 every step",
+        "mesh": "1024x1024",
+    },
     "cfg1_plain_64": {
         "input": "mantle_convection_lab_gb300/configs/cfg1_plain_64.input",
+        "kind": "replica",
         "desc": "configuration 1: 64x64 uniform Q1/P0, Ra=1e5, isoviscous, free slip, FP64 Uzawa + "
                 "Jacobi-PCG (the reference's iteration), true Stokes residual < 1e-8",
         "mesh": "64x64",
     },
 }
-DEFAULT_WORKLOAD = "cfg1_plain_64"
+DEFAULT_WORKLOAD = "cfg3_mg_1024"
+METRIC = "time steps/s at Stokes residual 1e-8"
 
 
 def load_peaks():
@@ -80,21 +96,47 @@ class ClockSampler:
         self.fh.seek(0)
         rows = [r.split(",") for r in self.fh.read().strip().splitlines() if r.count(",") >= 8]
         os.unlink(self.fh.name)
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+        sm = [x for x in (num(r[1]) for r in rows) if x is not None]
+        mx = [x for x in (num(r[2]) for r in rows) if x is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
 
-def stokes_bytes(st, neq, nno, nel, w=8):
-    """Algorithmic bytes of one Stokes solve: per inner CG iteration w*(10 n_v + nn) + nn,
-    per Uzawa iteration w*(4 n_v + 8 ne), plus the prologue/epilogue (two residual passes)."""
-    cg = st.cg_cycles * (w * (10 * neq + nno) + nno)
-    uz = st.uzawa_cycles * w * (4 * neq + 8 * nel)
-    pro = 2 * (w * (10 * neq + nno) + nno)
-    return cg + uz + pro
+def replica_bytes(st, neq, nno, nel, w=8):
+    """FP64 replica: per inner CG iteration w*(10 n_v + nn) + nn, per Uzawa iteration
+    w*(4 n_v + 8 ne), plus the two residual passes around the solve."""
+    return (st.cg_cycles * (w * (10 * neq + nno) + nno) + st.uzawa_cycles * w * (4 * neq + 8 * nel)
+            + 2 * (w * (10 * neq + nno) + nno))
+
+
+def converged_bytes(st, N, w=4):
+    """Mixed solver, per launch.  Per inner MG-PCG iteration: the CG part
+    w*(10 n_v + nn) + nn, plus a V(2,2) cycle of 4 tile passes per level (read x,
+    b, D^-1 as 2w each, eta w, mask 1; write 2w: 9w+1 B/node) and the transfer
+    (restriction reads 9 fine residuals per coarse node, prolongation 4 coarse
+    values per fine node, cached: counted as 4w B per fine node).  Per Uzawa
+    iteration: FP64 G s, G^T u and the pressure-vector updates, 8*(4 n_v + 8 ne).
+    Per refinement pass: FP64 K d + G p residual, 8*(3 n_v + nn) + 8*3 ne."""
+    nn = (N + 1) ** 2
+    nv = 2 * nn
+    ne = N * N
+    vcyc, n = 0, N
+    while n >= 4:
+        m = (n + 1) ** 2
+        vcyc += 4 * (9 * w + 1) * m + 4 * w * m
+        n //= 2
+    inner = w * (10 * nv + nn) + nn + vcyc
+    outer = 8 * (4 * nv + 8 * ne)
+    refine = 8 * (3 * nv + nn) + 8 * 3 * ne
+    return st.cg_cycles * inner + st.uzawa_cycles * outer + max(st.refine_passes, 1) * refine
 
 
 def dist_env():
@@ -111,67 +153,111 @@ def init_dist(world, local_rank):
     return dist
 
 
-def reduce_max(dist, v):
+def reduce_op(dist, v, op):
     if dist is None:
         return v
     import torch
     t = torch.tensor([float(v)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=op(dist))
     return float(t.item())
 
 
-def reduce_sum(dist, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([float(v)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+def rmax(dist, v):
+    return reduce_op(dist, v, lambda d: d.ReduceOp.MAX)
 
 
-def cpu_sample(inp, steps):
-    """Time the CPU oracle for `steps` steady steps (after one setup step)."""
+def rsum(dist, v):
+    return reduce_op(dist, v, lambda d: d.ReduceOp.SUM)
+
+
+# ---- CPU oracle samples (the reference's algorithm) --------------------------
+def _oracle(inp, threads):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_port
-    o = oracle_port.Oracle(os.path.join(ROOT, inp), threads=1)
-    o.step()
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    return oracle_port.Oracle(os.path.join(ROOT, inp), threads=threads)
+
+
+def cpu_sample(wl, threads, steps=None):
+    """Returns (steps_per_s, cores, description).  Configuration 1 runs whole
+    steps.  At 1024^2 one reference step is thousands of CG solves (its Uzawa
+    loop runs to max_citcom_cycle x max_cg_cycle at this viscosity contrast), so
+    the sample times the assembly and 20 inner CG iterations on the real mesh
+    and scales to that per-step iteration budget."""
+    if wl["kind"] == "replica":
+        o = _oracle(wl["input"], 1)
         o.step()
-    dt = time.perf_counter() - t0
+        n = steps or 10
+        t0 = time.perf_counter()
+        for _ in range(n):
+            o.step()
+        el = time.perf_counter() - t0
+        o.close()
+        return n / el, 1, f"{n} steady steps of the reference algorithm on 1 core ({el:.1f} s)"
+    o = _oracle(wl["input"], threads)
+    t0 = time.perf_counter()
+    o.assemble()
+    t_asm = time.perf_counter() - t0
+    ncg = 20
+    t0 = time.perf_counter()
+    o.cg_sample(ncg)
+    t_cg = (time.perf_counter() - t0) / ncg
+    budget = o.cfg.max_citcom_cycle * o.cfg.max_cg_cycle
     o.close()
-    return steps / dt, dt
+    per_step = t_asm + budget * t_cg
+    return 1.0 / per_step, threads, (f"assembly ({t_asm:.2f} s) + {ncg} CG iterations ({1e3 * t_cg:.1f} ms each) "
+                                     f"on the 1024^2 mesh with {threads} threads, scaled to the reference's "
+                                     f"per-step budget of {budget} CG iterations (max_citcom_cycle x max_cg_cycle)")
 
 
 def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    steps = max(1, args.steps)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_port
-    o = oracle_port.Oracle(os.path.join(ROOT, wl["input"]), threads=1)
-    for _ in range(max(0, args.warmup)):
-        o.step()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        o.step()
-    el = time.perf_counter() - t0
-    v = steps / el
-    line = {"metric": "time steps/s at Stokes residual 1e-8", "impl": "reference", "value": v,
-            "unit": "steps/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .input)",
-            "config": {"workload": args.workload, "desc": wl["desc"]},
-            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                             "sample": f"{steps} steps of {args.workload} after {args.warmup} warm-up steps"},
+    threads = os.cpu_count() or 1
+    if wl["kind"] == "replica":
+        steps = max(1, args.steps)
+        o = _oracle(wl["input"], 1)
+        for _ in range(max(0, args.warmup)):
+            o.step()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step()
+        el = time.perf_counter() - t0
+        o.close()
+        v, cores, sample = steps / el, 1, f"{steps} steps after {args.warmup} warm-up steps, 1 core"
+    else:
+        v, cores, sample = cpu_sample(wl, threads)
+        steps = args.steps
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "steps/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .input)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"]},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
+# ---- GPU arm --------------------------------------------------------------------
+def timed_steps(model, steps, flush, torch):
+    acc = {"ms_total": 0.0, "ms_solver": 0.0, "launches": 0, "uz": 0, "cg": 0, "refine": 0, "res": 0.0,
+           "stats": []}
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = model.step()
+        acc["ms_total"] += st.ms_total
+        acc["ms_solver"] += st.solver_kernel_ms
+        acc["launches"] += st.kernel_launches
+        acc["uz"] += st.uzawa_cycles
+        acc["cg"] += st.cg_cycles
+        acc["refine"] += st.refine_passes
+        acc["res"] = max(acc["res"], st.res_momentum, st.res_continuity)
+        acc["stats"].append(st)
+    return acc
+
+
 def run_gpu(args, wl):
-    import numpy as np
     import torch
     from mantle_convection_lab_gb300 import Config, Model
 
@@ -185,33 +271,21 @@ def run_gpu(args, wl):
     for _ in range(max(args.warmup, 0)):
         model.step()
 
-    # device-timed region
     sampler = ClockSampler() if rank == 0 else None
     if sampler:
         sampler.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ms_total, ms_solver, launches, alg_bytes, uz, cgc, res = 0.0, 0.0, 0, 0, 0, 0, 0.0
     t_wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        st = model.step()
-        ms_total += st.ms_total
-        ms_solver += st.solver_kernel_ms
-        launches += st.kernel_launches
-        alg_bytes += stokes_bytes(st, model.neq, model.nno, model.nel)
-        uz += st.uzawa_cycles
-        cgc += st.cg_cycles
-        res = max(res, st.res_momentum, st.res_continuity)
+    acc = timed_steps(model, args.steps, flush, torch)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
     if dist:
         dist.barrier()
     clocks = sampler.stop() if sampler else None
-    t_max = reduce_max(dist, ms_total / 1e3)
-    value = reduce_sum(dist, args.steps) / t_max if world > 1 else args.steps / (ms_total / 1e3)
+    t_max = rmax(dist, acc["ms_total"] / 1e3)
+    value = rsum(dist, args.steps) / t_max
 
     # end-to-end through the host-buffer entry point
     nno, nel = model.nno, model.nel
@@ -226,40 +300,71 @@ def run_gpu(args, wl):
     for _ in range(args.steps):
         model.step_host(T_in, T_out, V_out, P_out)
         T_in[:] = T_out
-    e2e_el = reduce_max(dist, time.perf_counter() - t0)
-    e2e = reduce_sum(dist, args.steps) / e2e_el
+    e2e = rsum(dist, args.steps) / rmax(dist, time.perf_counter() - t0)
 
     peak, peak_kind = load_peaks()
-    achieved = (alg_bytes / args.steps) / (ms_solver / args.steps / 1e3) / 1e9 if ms_solver > 0 else 0.0
+    n_launch = max(len(acc["stats"]), 1)
+    if wl["kind"] == "converged":
+        alg = sum(converged_bytes(s, cfg_N(cfg)) for s in acc["stats"]) / n_launch
+        kname = "k_stokes_mg<float> (persistent mixed-precision Stokes solve)"
+        dtype = "f32 inner / f64 outer"
+    else:
+        alg = sum(replica_bytes(s, model.neq, nno, nel) for s in acc["stats"]) / n_launch
+        kname = "k_uzawa (persistent FP64 Uzawa/CG)"
+        dtype = "f64"
+    ms_launch = acc["ms_solver"] / n_launch
+    achieved = alg / (ms_launch / 1e3) / 1e9 if ms_launch > 0 else 0.0
     line = {
-        "metric": "time steps/s at Stokes residual 1e-8", "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": acc["ms_total"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype,
         "data": "synthetic (seeded .input, Philox initial temperature)",
         "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between steps",
-                   "uzawa_cycles_per_step": uz / args.steps, "cg_cycles_per_step": cgc / args.steps,
-                   "max_stokes_residual": res},
+                   "uzawa_cycles_per_step": acc["uz"] / args.steps, "inner_cg_per_step": acc["cg"] / args.steps,
+                   "refine_passes_per_step": acc["refine"] / args.steps, "max_stokes_residual": acc["res"]},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * nno,
                 "d2h_bytes_per_step": 8 * (3 * nno + nel)},
-        "gpu_launches": launches,
-        "roofline": {"kernel": "k_uzawa (persistent Stokes solver)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": None, "alg_bytes_per_launch": alg_bytes / args.steps,
-                     "ms_per_launch": ms_solver / args.steps},
+        "gpu_launches": acc["launches"],
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "alg_bytes_per_launch": alg, "ms_per_launch": ms_launch},
         "clocks": clocks,
         "wall_s_timed": wall,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, el = cpu_sample(wl["input"], args.cpu_steps)
-        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                "sample": f"{args.cpu_steps} steady steps of {args.workload} ({el:.1f} s)"}
     model.close()
+    del model
+    if wl["kind"] == "converged" and not args.no_plain:
+        pcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+        pcfg.precision = 2
+        pcfg.warm_start = 2
+        pm = Model(pcfg)
+        pm.initial_temperature()
+        for _ in range(max(args.warmup, 0)):
+            pm.step()
+        torch.cuda.synchronize()
+        pacc = timed_steps(pm, args.plain_steps, flush, torch)
+        pm.close()
+        pv = rsum(dist, args.plain_steps) / rmax(dist, pacc["ms_total"] / 1e3)
+        line["plain_fp64"] = {"value": pv, "unit": "steps/s", "steps": args.plain_steps,
+                              "ms_per_step": pacc["ms_total"] / args.plain_steps,
+                              "uzawa_cycles_per_step": pacc["uz"] / args.plain_steps,
+                              "inner_cg_per_step": pacc["cg"] / args.plain_steps,
+                              "max_stokes_residual": pacc["res"],
+                              "desc": "FP64 inner solves, d=0 and p kept each step (the reference's start)"}
+        line["speedup_vs_plain_fp64"] = value / pv
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_sample(wl, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def cfg_N(cfg):
+    return 1 << (cfg.level - 1)
 
 
 def main():
@@ -269,7 +374,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]

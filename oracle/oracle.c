@@ -435,28 +435,38 @@ static int conj_grad(orc *o, const double *b, double *x, double accu, int max_cy
 	}
 	delta_new = dot(o, r, dd, n);
 	delta0 = delta_new;
+	/* element-wise loops give the same result on any thread count; only the
+	 * dot products (dot) change their summation order with threads > 1 */
 	while (cycle < max_cycle && delta_new > accu * delta0) {
+		const int par = o->threads > 1 && n > 4096;
 		K_prod(o, dd, q);
 		alpha = delta_new / dot(o, dd, q, n);
+#pragma omp parallel for num_threads(o->threads) if (par)
 		for (i = 0; i < n; i++)
 			x[i] += alpha * dd[i];
 		constrain_v(o, x);
 		if (cycle % 50 == 0) {
 			K_prod(o, x, r);
+#pragma omp parallel for num_threads(o->threads) if (par)
 			for (i = 0; i < n; i++)
 				r[i] = b[i] - r[i];
-		} else
+		} else {
+#pragma omp parallel for num_threads(o->threads) if (par)
 			for (i = 0; i < n; i++)
 				r[i] -= alpha * q[i];
+		}
+#pragma omp parallel for num_threads(o->threads) if (par)
 		for (i = 0; i < n; i++)
 			s[i] = pc ? r[i] / o->Kdiag[i] : r[i];
 		delta_old = delta_new;
 		delta_new = dot(o, r, s, n);
 		beta = delta_new / delta_old;
+#pragma omp parallel for num_threads(o->threads) if (par)
 		for (i = 0; i < n; i++)
 			dd[i] = s[i] + beta * dd[i];
 		cycle++;
 		res = 0.0;
+#pragma omp parallel for reduction(max : res) num_threads(o->threads) if (par)
 		for (i = 0; i < n; i++)
 			if (fabs(alpha * r[i]) > res)
 				res = fabs(alpha * r[i]);

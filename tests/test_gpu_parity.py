@@ -64,8 +64,10 @@ def test_time_steps(case, steps, tol):
             assert rel(st.dt, g["series/dt"][s]) < tol
             assert rel(st.model_time, g["series/model_time"][s]) < tol
             for f, k in (("V0", "V0"), ("V1", "V1"), ("P", "p"), ("d", "d"), ("stress", "stress")):
-                assert rel(m.get(f), g[f"step{s:04d}/{k}"]) < tol, (case, s, f)
-            assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < tol, (case, s, "T")
+                e = rel(m.get(f), g[f"step{s:04d}/{k}"])
+                assert e < tol, (case, s, f, e)
+            e = rel(m.get("T"), g[f"heat{s:04d}/T"])
+            assert e < tol, (case, s, "T", e)
 
 
 def rel_nan(a, b):
