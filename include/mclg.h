@@ -146,6 +146,20 @@ int mclg_buoyancy_force(mclg_ctx *ctx);                    /* Buoyancy.c:3-22 */
 int mclg_viscosity(mclg_ctx *ctx);                         /* Viscosity.c:3-24 */
 int mclg_velocity_pressure_KGF_matrix(mclg_ctx *ctx);      /* Build_matrix.c:4-40 */
 int mclg_solve_velocity_pressure(mclg_ctx *ctx, mclg_step_stats *st); /* Solver.c:3-12 */
+/* No counterpart in the reference (its solver mallocs its work vectors on
+ * every call).  The same FP64 solve as mclg_solve_velocity_pressure (replica
+ * mode, precision=fp64) for callers that must not allocate device memory at
+ * solve time -- a host program that hands out all device memory up front, or
+ * a time loop that cannot take cudaMalloc's latency and implicit device
+ * synchronisation.  Its scratch is one device array built into the library,
+ * sized for meshes of at most MCLG_NOALLOC_MAX_NODES nodes and
+ * MCLG_NOALLOC_MAX_ELEMS elements (about 3.3 MB, held on every GPU that loads
+ * the library until exit); larger meshes get MCLG_BAD_INPUT.  All calls share
+ * the array: calls whose GPU work overlaps race.  The first call on a device
+ * looks the array's device address up, so make it before any stream capture. */
+#define MCLG_NOALLOC_MAX_NODES 16641
+#define MCLG_NOALLOC_MAX_ELEMS 16384
+int mclg_solve_velocity_pressure_noalloc(mclg_ctx *ctx, mclg_step_stats *st);
 int mclg_update_temperature(mclg_ctx *ctx, mclg_step_stats *st);      /* Update_temperature.c:3-133 */
 /* output(): Output.c:4-156 text files for the current G.timestep. */
 int mclg_output(mclg_ctx *ctx, const char *data_dir, int timestep);

@@ -113,6 +113,7 @@ def lib():
         "mclg_initial_temperature": (C.c_int, [vp]), "mclg_buoyancy_force": (C.c_int, [vp]),
         "mclg_viscosity": (C.c_int, [vp]), "mclg_velocity_pressure_KGF_matrix": (C.c_int, [vp]),
         "mclg_solve_velocity_pressure": (C.c_int, [vp, vp]), "mclg_update_temperature": (C.c_int, [vp, vp]),
+        "mclg_solve_velocity_pressure_noalloc": (C.c_int, [vp, vp]),
         "mclg_output": (C.c_int, [vp, C.c_char_p, C.c_int]), "mclg_step": (C.c_int, [vp, C.c_int, vp]),
         "mclg_step_host": (C.c_int, [vp, dp, dp, dp, dp, vp]),
         "mclg_get_field": (C.c_int, [vp, C.c_int, C.c_int, dp, sz]),
@@ -235,6 +236,13 @@ class Model:
     def solve_velocity_pressure(self):
         st = StepStats()
         _check(lib().mclg_solve_velocity_pressure(self._c, C.byref(st)), "solve_velocity_pressure")
+        return st
+
+    def solve_velocity_pressure_noalloc(self):
+        """The same solve with library-resident scratch: allocates no device memory."""
+        st = StepStats()
+        _check(lib().mclg_solve_velocity_pressure_noalloc(self._c, C.byref(st)),
+               "solve_velocity_pressure_noalloc")
         return st
 
     def update_temperature(self):

@@ -1181,3 +1181,142 @@ __global__ void k_inv_diag2(int n, const double2 *__restrict__ d, double2 *__res
 	inv[i] = make_double2(1.0 / v.x, 1.0 / v.y);
 }
 }  // namespace mclg
+
+// ---- Stokes solve without allocation -----------------------------------------
+// mclg_solve_velocity_pressure_noalloc: the FP64 Uzawa solve of
+// mclg_solve_velocity_pressure, with every scratch vector taken from one
+// file-scope device array instead of the context's own buffers.  It is for
+// callers whose device memory is handed out up front by their host program
+// (a memory planner that reserves the whole device at start-up, or a time
+// loop where the latency and device synchronisation of cudaMalloc are not
+// acceptable): the call itself allocates nothing.
+//
+// The array is sized for meshes of at most MCLG_NOALLOC_MAX_NODES nodes and
+// MCLG_NOALLOC_MAX_ELEMS elements; every GPU that loads this library holds it
+// until the process exits.  All calls share it and it keeps the last call's
+// contents, so two calls whose work overlaps on the GPU (different streams or
+// contexts at the same time) race on it; each call clears the scalars it
+// needs zeroed before it starts.  In host code the array's name is only a
+// host-side handle: its device address is looked up once per device with
+// cudaGetSymbolAddress on the first call made while that device is current,
+// so that first call should come before any stream capture.
+namespace {
+constexpr size_t kNoallocNodeVecs = 7;      // u1, Ah, r, s, dd, q, xt (double2 per node)
+constexpr size_t kNoallocElemVecs = 9;      // r0, r1, r2, z0, z1, s1, s2, Ahp, stress_e
+constexpr size_t kNoallocPartBytes = 2ull * kMaxCoopBlocks * kRedWidth * sizeof(double);
+constexpr size_t kNoallocBytes = kNoallocNodeVecs * MCLG_NOALLOC_MAX_NODES * sizeof(double2) +
+                                 kNoallocElemVecs * MCLG_NOALLOC_MAX_ELEMS * sizeof(double) + kNoallocPartBytes +
+                                 256 + sizeof(StepScalars);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+constexpr int kNoallocMaxDevices = 64;
+static unsigned char *g_noalloc_addr[kNoallocMaxDevices];
+}  // namespace
+
+extern "C" int mclg_solve_velocity_pressure_noalloc(mclg_ctx *c, mclg_step_stats *st)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	if (c->cfg.precision != 0) {
+		mclg_set_error("the allocation-free solve runs the FP64 replica (precision=fp64) only");
+		return MCLG_BAD_INPUT;
+	}
+	const size_t nn = c->L.nno, ne = c->L.nel;
+	if (nn > MCLG_NOALLOC_MAX_NODES || ne > MCLG_NOALLOC_MAX_ELEMS) {
+		mclg_set_error("mesh of %zu nodes / %zu elements exceeds the allocation-free limit of %d nodes / %d elements",
+		               nn, ne, MCLG_NOALLOC_MAX_NODES, MCLG_NOALLOC_MAX_ELEMS);
+		return MCLG_BAD_INPUT;
+	}
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	if (dev < 0 || dev >= kNoallocMaxDevices) {
+		mclg_set_error("device %d is beyond the allocation-free table", dev);
+		return MCLG_BAD_INPUT;
+	}
+	if (g_noalloc_addr[dev] == NULL) {
+		void *p = NULL;
+		CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+		g_noalloc_addr[dev] = (unsigned char *)p;
+	}
+	unsigned char *base = g_noalloc_addr[dev];
+	double2 *nv[kNoallocNodeVecs];
+	double *ev[kNoallocElemVecs];
+	for (size_t i = 0; i < kNoallocNodeVecs; i++)
+		nv[i] = (double2 *)(base + i * MCLG_NOALLOC_MAX_NODES * sizeof(double2));
+	unsigned char *ebase = base + kNoallocNodeVecs * MCLG_NOALLOC_MAX_NODES * sizeof(double2);
+	for (size_t i = 0; i < kNoallocElemVecs; i++)
+		ev[i] = (double *)(ebase + i * MCLG_NOALLOC_MAX_ELEMS * sizeof(double));
+	double *part = (double *)(ebase + kNoallocElemVecs * MCLG_NOALLOC_MAX_ELEMS * sizeof(double));
+	StepScalars *sc = (StepScalars *)((unsigned char *)part + kNoallocPartBytes + 256 -
+	                                  ((uintptr_t)((unsigned char *)part + kNoallocPartBytes) & 255u));
+
+	const mclg_config &f = c->cfg;
+	// initial_d_p (Solver.c:251-278), as in mclg_solve_velocity_pressure
+	CK(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
+	if (!(c->p_initialized && f.AMR == 0 && f.zero_P == 0))
+		CK(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
+	c->p_initialized = 1;
+	CK(cudaMemsetAsync(sc, 0, sizeof(StepScalars), c->st));
+	UzawaArgs a;
+	memset(&a, 0, sizeof a);
+	a.L = c->L;
+	a.K = c->K;
+	a.idiag = c->idiag;
+	a.F = c->F;
+	a.bab = c->bab;
+	a.d = c->d;
+	a.u1 = nv[0];
+	a.Ah = nv[1];
+	a.r = nv[2];
+	a.s = nv[3];
+	a.dd = nv[4];
+	a.q = nv[5];
+	a.xt = nv[6];
+	a.V = c->V;
+	a.p = c->p;
+	a.r0 = ev[0];
+	a.r1 = ev[1];
+	a.r2 = ev[2];
+	a.z0 = ev[3];
+	a.z1 = ev[4];
+	a.s1 = ev[5];
+	a.s2 = ev[6];
+	a.Ahp = ev[7];
+	a.red.part = part;
+	a.red.flip = 0;
+	a.sc = sc;
+	a.max_citcom = f.max_citcom_cycle;
+	a.max_cg = f.max_cg_cycle;
+	a.precond = f.cg_precondition;
+	a.check_v_only = f.check_v_only;
+	a.solver_jc = strcmp(f.solver, "jc") == 0;
+	a.auto_accuracy = f.auto_accuracy;
+	a.neq = c->mesh.lev[c->fl].neq;
+	a.citcom_accu = f.citcom_solver_accu;
+	a.accuracy = f.accuracy;
+	void *args[] = {&a};
+	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(), dim3(c->coop_uzawa), dim3(kBlock), args, 0, c->st));
+	c->launches++;
+	// compute_stress with the element stresses in the same array
+	k_stress_elem<<<blocks_for(ne), kBlock, 0, c->st>>>(c->L, c->vis, c->V, ev[8]);
+	int rc = check_launch(c, "k_stress_elem");
+	if (rc)
+		return rc;
+	k_elem_to_node<<<blocks_for(nn), kBlock, 0, c->st>>>(c->L, ev[8], c->stress);
+	if ((rc = check_launch(c, "k_elem_to_node")))
+		return rc;
+	StepScalars hs;
+	CK(cudaMemcpyAsync(&hs, sc, sizeof hs, cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	if (st) {
+		st->timestep = c->timestep;
+		st->uzawa_cycles = hs.uzawa_cycles;
+		st->cg_cycles = hs.cg_cycles;
+		st->dv = hs.dv;
+		st->dp = hs.dp;
+		st->res_momentum = hs.res_m;
+		st->res_continuity = hs.res_c;
+		st->status = status_from_bits(hs.status);
+		st->refine_passes = 0;
+	}
+	return MCLG_OK;
+}
