@@ -225,6 +225,11 @@ enum {
 int mclg_mesh_get_real(const mclg_mesh_handle *h, int which, int lev, double *out, size_t n);
 /* Initial_condition.c:3-136 on level lev (finest when lev < 0). */
 int mclg_mesh_initial_temperature(const mclg_mesh_handle *h, int lev, double *T, size_t n);
+/* Output.c:4-156 from host fields of the finest level (each nno long, G.node
+ * order): the files mclg_output writes, for fields the caller holds. */
+int mclg_mesh_write_output(const mclg_mesh_handle *h, const char *data_dir, int timestep,
+                           const double *T, const double *V0, const double *V1,
+                           const double *stress, const double *vis, size_t n);
 
 /* ---- single operators, for parity tests (finest level unless lev >= 0) -- */
 int mclg_stokes_matvec(mclg_ctx *ctx, int lev, const double *x, double *y);   /* K_prod_d, Solver.c:360-386 */

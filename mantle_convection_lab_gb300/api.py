@@ -123,6 +123,7 @@ def lib():
         "mclg_mesh_get": (C.c_int, [vp, C.c_int, C.c_int, ip, sz]),
         "mclg_mesh_get_real": (C.c_int, [vp, C.c_int, C.c_int, dp, sz]),
         "mclg_mesh_initial_temperature": (C.c_int, [vp, C.c_int, dp, sz]),
+        "mclg_mesh_write_output": (C.c_int, [vp, C.c_char_p, C.c_int, dp, dp, dp, dp, dp, sz]),
         "mclg_stokes_matvec": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_stokes_G": (C.c_int, [vp, C.c_int, dp, dp]),
         "mclg_stokes_GT": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_heat_matvec": (C.c_int, [vp, C.c_int, dp, dp]),
     }
@@ -193,6 +194,15 @@ class Mesh:
         out = np.zeros(n, np.float64)
         _check(lib().mclg_mesh_initial_temperature(self._h, lev, _dptr(out), n), "mesh_initial_temperature")
         return out
+
+    def write_output(self, data_dir, timestep, T, V0, V1, stress, vis):
+        """Output.c's text files for host fields of the finest level (G.node order)."""
+        f = [np.ascontiguousarray(a, np.float64) for a in (T, V0, V1, stress, vis)]
+        n = f[0].size
+        if any(a.size != n for a in f):
+            raise MclgError(BAD_INPUT, "write_output: fields differ in length")
+        _check(lib().mclg_mesh_write_output(self._h, data_dir.encode(), int(timestep), *map(_dptr, f), n),
+               "mesh_write_output")
 
 
 class Model:

@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 		coarse_build<TI>(H);
 	g.sync();
 
-	int refine = 0, outer_total = 0, inner_total = 0;
+	int refine = 0, outer_total = 0, inner_total = 0, capped = 0;
 	double res_m = 0.0, res_c = 0.0, fnorm = 1.0;
 	while (true) {
 		// -- FP64 residual R = [F - K d - G p ; G^T d]
@@ -612,8 +612,17 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 		res_m = sqrt(rs[0]) / fnorm;
 		res_c = sqrt(rs[1]) / fnorm;
 		const double res = sqrt(rs[0] + rs[1]) / fnorm;
-		if (!(res >= a.rtol) || refine >= a.max_refine || !isfinite(res))
+		if (!isfinite(res)) {
+			if (tid == 0)
+				atomicOr(status, 2);
 			break;
+		}
+		if (!(res >= a.rtol))
+			break;
+		if (refine >= a.max_refine) {
+			capped = 1;
+			break;
+		}
 		refine++;
 
 		// -- correction solve: Uzawa on [K G; G^T 0][dd; dp] = [R_m; -R_c]
@@ -724,7 +733,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 			a.p[e] += a.dpv[e];
 		g.sync();
 	}
-	if (refine >= a.max_refine && tid == 0)
+	if (capped && tid == 0)
 		atomicOr(status, 1);
 	// nodal velocity (v_to_nodes, Solver.c:1319-1343)
 	for (int A = tid; A < nn; A += nth) {

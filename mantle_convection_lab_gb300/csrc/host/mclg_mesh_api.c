@@ -174,3 +174,18 @@ int mclg_mesh_initial_temperature(const mclg_mesh_handle *h, int lev, double *T,
 	}
 	return mclg_host_initial_temperature(&h->mesh, &h->cfg, lev, T);
 }
+
+int mclg_mesh_write_output(const mclg_mesh_handle *h, const char *data_dir, int timestep,
+                           const double *T, const double *V0, const double *V1,
+                           const double *stress, const double *vis, size_t n)
+{
+	const mclg_level *L;
+	if (h == NULL || T == NULL || V0 == NULL || V1 == NULL || stress == NULL || vis == NULL)
+		return MCLG_BAD_INPUT;
+	L = &h->mesh.lev[h->mesh.max_level - 1];
+	if (n != (size_t)L->nno) {
+		mclg_set_error("output fields have %zu entries, the finest level has %d nodes", n, L->nno);
+		return MCLG_BAD_INPUT;
+	}
+	return mclg_write_output(data_dir ? data_dir : h->cfg.data_dir, timestep, L, T, V0, V1, stress, vis);
+}

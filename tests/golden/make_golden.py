@@ -105,6 +105,9 @@ CASES = {
 }
 
 
+TEXT_CASES = {"cfg1_l5"}   # cases whose Output.c text files are kept too
+
+
 def run_case(name, extra, keep_steps, keep_coarse):
     text = BASE + extra
     work = tempfile.mkdtemp(prefix="mclg_golden_")
@@ -115,10 +118,18 @@ def run_case(name, extra, keep_steps, keep_coarse):
         dump = os.path.join(work, "dump")
         os.makedirs(dump)
         env = dict(os.environ, MCLG_DUMP_DIR=dump)
+        if name in TEXT_CASES:
+            env["MCLG_REF_TEXT"] = "1"   # the harness also calls the reference's own output()
         proc = subprocess.run([REF_BIN, inp], cwd=work, env=env, capture_output=True, text=True)
         if proc.returncode != 0:
             raise RuntimeError(f"{name}: reference exited {proc.returncode}\n{proc.stderr[-2000:]}")
         out = {}
+        if name in TEXT_CASES:   # Output.c files, verbatim
+            for root, _, files in os.walk(os.path.join(work, "out")):
+                for f in files:
+                    rel_path = os.path.relpath(os.path.join(root, f), os.path.join(work, "out"))
+                    with open(os.path.join(root, f), "rb") as fh:
+                        out["text/" + rel_path] = np.frombuffer(fh.read(), np.uint8)
         uz = [int(m.group(1)) for m in re.finditer(r"^(\d+) dv = ", proc.stdout, re.M)]
         heat = [int(m.group(1)) for m in re.finditer(r"Temperature CG cycle = (\d+)", proc.stdout)]
         mesh = read_dump(os.path.join(dump, "mesh.dump"))

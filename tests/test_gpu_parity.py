@@ -46,14 +46,18 @@ def test_stokes_operators(case):
 
 
 # Cases whose Uzawa loop stops at max_citcom_cycle before converging.  Their
-# iterates depend on summation order: the CPU oracle with 4 threads moves
-# dev14_l7 by 1.7e-6 from the reference.  They are held to 1e-5 instead.
+# iterates depend on summation order: the CPU oracle with 16 threads moves
+# dev14_l7 by 3e-5 from the reference.  They are held to 1e-5 instead, and
+# dev14_l7, whose iterate moves by 1e-4 (V) and 8e-4 (P) when T moves by
+# 1e-13 (test_oracle_golden.py::test_capped_dev14_iterate_is_ill_conditioned),
+# to 2e-3.
 CAPPED_TOL = 1e-5
+ILL_TOL = 2e-3
 
 
 @pytest.mark.parametrize("case,steps,tol", [("cfg1_l5", 4, FIELD_TOL), ("vc_l6", 3, FIELD_TOL),
                                             ("hang11v_l6", 2, CAPPED_TOL), ("dev12_l7", 1, CAPPED_TOL),
-                                            ("dev13_l8", 1, CAPPED_TOL), ("dev14_l7", 1, CAPPED_TOL)])
+                                            ("dev13_l8", 1, CAPPED_TOL), ("dev14_l7", 1, ILL_TOL)])
 def test_time_steps(case, steps, tol):
     g = golden(case)
     with make(case) as m:
