@@ -11,11 +11,16 @@ temperature update, on seeded synthetic .input workloads
 Default workload -- configuration 3: 1024 x 1024 uniform Q1/P0 mesh, Ra=1e8,
 eta = exp(-ln(1e5) T) clipped to [1e-5, 1], every step solved to a true
 Stokes residual |[F - K d - G p; G^T d]|/|F| < 1e-8.
-  value      steps/s of the mixed-precision solver (FP32 multigrid-preconditioned
-             inner CG inside the FP64 Uzawa loop and FP64 iterative refinement),
-             warm-started from the previous step; device time (CUDA events on
-             the engine's stream), fields resident in HBM, working set larger
-             than L2 is not guaranteed so L2 is flushed (256 MB write) between steps
+  value      steps/s of the mixed-precision solver (FP64 iterative refinement
+             around MINRES on the full Stokes system, preconditioned by one FP32
+             multigrid V-cycle and the BAB pressure diagonal) with the learned
+             guess: each step starts from the linear
+             extrapolation of the last two solutions, corrected by the CNN
+             (mantle_convection_lab_gb300/weights) when that lowers the FP64
+             residual; device time (CUDA events on the engine's stream), fields
+             resident in HBM, working set larger than L2 is not guaranteed so
+             L2 is flushed (256 MB write) between steps
+  mixed_no_network  the same solver and warm start without the network
   plain_fp64 the same solve with FP64 inner solves and the reference's start
              (d = 0, p kept: initial_d_p, Solver.c:251-278)
   e2e        steps/s through mclg_step_host: T copied in from pinned host memory
@@ -59,6 +64,8 @@ WORKLOADS = {
     },
 }
 DEFAULT_WORKLOAD = "cfg3_mg_1024"
+GUESS_NET = os.path.join(ROOT, "mantle_convection_lab_gb300", "weights", "guess_cfg3.bin")
+GUESS_GRID = 128
 METRIC = "time steps/s at Stokes residual 1e-8"
 
 
@@ -117,13 +124,17 @@ def replica_bytes(st, neq, nno, nel, w=8):
             + 2 * (w * (10 * neq + nno) + nno))
 
 
-def converged_bytes(st, N, w=4):
-    """Mixed solver, per launch.  Per inner MG-PCG iteration: the CG part
-    w*(10 n_v + nn) + nn, plus a V(2,2) cycle of 4 tile passes per level (read x,
+def converged_bytes(st, N, method=0, w=4):
+    """Mixed solver, per launch.  V(2,2) cycle: 4 tile passes per level (read x,
     b, D^-1 as 2w each, eta w, mask 1; write 2w: 9w+1 B/node) and the transfer
     (restriction reads 9 fine residuals per coarse node, prolongation 4 coarse
-    values per fine node, cached: counted as 4w B per fine node).  Per Uzawa
-    iteration: FP64 G s, G^T u and the pressure-vector updates, 8*(4 n_v + 8 ne).
+    values per fine node, cached: counted as 4w B per fine node).
+    Uzawa (method 0), per inner MG-PCG iteration: the CG part w*(10 n_v + nn) +
+    nn plus a V-cycle; per Uzawa iteration: FP64 G s, G^T u and the pressure
+    updates, 8*(4 n_v + 8 ne).
+    MINRES (method 1), per iteration: a V-cycle, the TI operator (5w+1 B/node),
+    and the FP64 Lanczos, direction and solution updates with G and G^T:
+    (225 + 10w) B per node and 136 B per element.
     Per refinement pass: FP64 K d + G p residual, 8*(3 n_v + nn) + 8*3 ne."""
     nn = (N + 1) ** 2
     nv = 2 * nn
@@ -133,9 +144,13 @@ def converged_bytes(st, N, w=4):
         m = (n + 1) ** 2
         vcyc += 4 * (9 * w + 1) * m + 4 * w * m
         n //= 2
+    refine = 8 * (3 * nv + nn) + 8 * 3 * ne
+    if method == 1:
+        it = vcyc + (5 * w + 1) * nn + (225 + 10 * w) * nn + 136 * ne
+        extra_vcycles = max(st.cg_cycles - st.uzawa_cycles, 0)
+        return st.uzawa_cycles * it + extra_vcycles * (vcyc + 24 * nn) + max(st.refine_passes, 1) * refine
     inner = w * (10 * nv + nn) + nn + vcyc
     outer = 8 * (4 * nv + 8 * ne)
-    refine = 8 * (3 * nv + nn) + 8 * 3 * ne
     return st.cg_cycles * inner + st.uzawa_cycles * outer + max(st.refine_passes, 1) * refine
 
 
@@ -263,6 +278,17 @@ def timed_steps(model, steps, flush, torch):
     return acc
 
 
+def attach_guess(model, wl, args):
+    """The learned initial guess (converged workloads with trained weights)."""
+    from mantle_convection_lab_gb300 import Cnn
+    from mantle_convection_lab_gb300.api import GUESS_LEARNED
+    if wl["kind"] != "converged" or args.no_learned or not os.path.exists(GUESS_NET):
+        return None
+    net = Cnn.load(GUESS_NET)
+    model.guess_set(GUESS_LEARNED, GUESS_GRID, net)
+    return net
+
+
 def run_gpu(args, wl):
     import torch
     from mantle_convection_lab_gb300 import Config, Model
@@ -273,6 +299,7 @@ def run_gpu(args, wl):
     cfg = Config.from_input(os.path.join(ROOT, wl["input"]))
     model = Model(cfg)
     model.initial_temperature()
+    net = attach_guess(model, wl, args)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
     for _ in range(max(args.warmup, 0)):
         model.step()
@@ -310,7 +337,7 @@ def run_gpu(args, wl):
     peak, peak_kind = load_peaks()
     n_launch = max(len(acc["stats"]), 1)
     if wl["kind"] == "converged":
-        alg = sum(converged_bytes(s, cfg_N(cfg)) for s in acc["stats"]) / n_launch
+        alg = sum(converged_bytes(s, cfg_N(cfg), cfg.stokes_method) for s in acc["stats"]) / n_launch
         kname = "k_stokes_mg<float> (persistent mixed-precision Stokes solve)"
         dtype = "f32 inner / f64 outer"
     else:
@@ -326,7 +353,9 @@ def run_gpu(args, wl):
         "data": "synthetic (seeded .input, Philox initial temperature)",
         "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between steps",
-                   "uzawa_cycles_per_step": acc["uz"] / args.steps, "inner_cg_per_step": acc["cg"] / args.steps,
+                   "outer_iterations_per_step": acc["uz"] / args.steps, "vcycles_or_inner_cg_per_step": acc["cg"] / args.steps,
+                   "correction_solve": ["Uzawa + inner MG-PCG", "MINRES, block-diagonal preconditioner"][cfg.stokes_method]
+                   if wl["kind"] == "converged" else "Uzawa + Jacobi-PCG (reference iteration)",
                    "refine_passes_per_step": acc["refine"] / args.steps, "max_stokes_residual": acc["res"]},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 8 * nno,
                 "d2h_bytes_per_step": 8 * (3 * nno + nel)},
@@ -337,12 +366,38 @@ def run_gpu(args, wl):
         "clocks": clocks,
         "wall_s_timed": wall,
     }
+    if net is not None:
+        line["learned_guess"] = {
+            "network": os.path.relpath(GUESS_NET, ROOT), "params": net.nparam, "grid": GUESS_GRID,
+            "steps_network_kept": sum(1 for s in acc["stats"] if s.guess_used == 1),
+            "steps_judged": sum(1 for s in acc["stats"] if s.guess_used >= 0),
+            "ms_guess_per_step": sum(s.ms_guess for s in acc["stats"]) / args.steps,
+            "desc": "CNN correction of the extrapolated guess, kept only when its FP64 residual is smaller"}
     model.close()
     del model
+    if net is not None and not args.no_plain:
+        # the same solver without the network
+        mcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+        mm = Model(mcfg)
+        mm.initial_temperature()
+        for _ in range(max(args.warmup, 0)):
+            mm.step()
+        torch.cuda.synchronize()
+        macc = timed_steps(mm, args.steps, flush, torch)
+        mm.close()
+        mv = job_throughput(dist, args.steps, macc["ms_total"] / 1e3)
+        line["mixed_no_network"] = {"value": mv, "unit": "steps/s", "steps": args.steps,
+                                    "ms_per_step": macc["ms_total"] / args.steps,
+                                    "uzawa_cycles_per_step": macc["uz"] / args.steps,
+                                    "inner_cg_per_step": macc["cg"] / args.steps,
+                                    "max_stokes_residual": macc["res"]}
     if wl["kind"] == "converged" and not args.no_plain:
         pcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
         pcfg.precision = 2
         pcfg.warm_start = 2
+        pcfg.stokes_method = 0       # Uzawa outer loop with inner MG-PCG, as the reference iterates
+        pcfg.outer_rtol = 1e-2
+        pcfg.inner_rtol = 1e-2
         pm = Model(pcfg)
         pm.initial_temperature()
         for _ in range(max(args.warmup, 0)):
@@ -356,7 +411,8 @@ def run_gpu(args, wl):
                               "uzawa_cycles_per_step": pacc["uz"] / args.plain_steps,
                               "inner_cg_per_step": pacc["cg"] / args.plain_steps,
                               "max_stokes_residual": pacc["res"],
-                              "desc": "FP64 inner solves, d=0 and p kept each step (the reference's start)"}
+                              "desc": "the reference's Uzawa outer loop with FP64 multigrid-preconditioned inner CG, "
+                                      "d=0 and p kept each step (the reference's start)"}
         line["speedup_vs_plain_fp64"] = value / pv
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample = cpu_sample(wl, os.cpu_count() or 1)
@@ -382,6 +438,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -91,7 +91,8 @@ typedef struct mclg_config {
 	                                FP64 Uzawa loop and FP64 iterative refinement (uniform meshes);
 	                            2 "fp64mg": the same converged solver with FP64 inner solves */
 	double stokes_rtol;      /* converged solvers: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
-	int warm_start;          /* converged solvers: start from the previous step's (d,p) */
+	int warm_start;          /* converged solvers: 0 zero, 1 the previous step's (d,p), 2 d=0 and p kept
+	                            (the reference's start), 3 linear extrapolation of the last two steps */
 	double vis_min, vis_max; /* viscosity clip, applied when vis_max > 0 */
 	int mg_smooth;           /* damped-Jacobi sweeps per V-cycle side (2) */
 	double mg_omega;         /* Jacobi damping (0.6) */
@@ -101,6 +102,9 @@ typedef struct mclg_config {
 	int max_refine, max_outer, max_inner;  /* caps (20, 500, 200) */
 	int mg_eta_avg;          /* coarse viscosity: 0 injection, 1 full-weighted mean, 2 log-mean (2) */
 	int mg_block_n;          /* grids of at most this many elements per side run in one block (8) */
+	int guess_smooth;        /* learned guess: binomial filter passes on the network's output (2) */
+	int stokes_method;       /* converged solvers' correction solve: 0 Uzawa with inner MG-PCG (the
+	                            reference's outer loop), 1 MINRES with a block-diagonal preconditioner (0) */
 } mclg_config;
 
 typedef struct mclg_step_stats {
@@ -118,6 +122,9 @@ typedef struct mclg_step_stats {
 	double solver_kernel_ms; /* device time of the Stokes solver kernel(s) of this step (CUDA events) */
 	long long solver_kernel_launches;
 	int refine_passes;       /* converged solvers: FP64 refinement passes (0 for the replica) */
+	int guess_used;          /* learned guess: 1 network, 0 previous solution, -1 not judged this step */
+	double res_guess_learned, res_guess_prev;   /* relative FP64 residuals of the two candidate guesses */
+	double ms_guess;         /* device time of the network and its feature kernels this step */
 } mclg_step_stats;
 
 typedef struct mclg_ctx mclg_ctx;
@@ -237,6 +244,49 @@ int mclg_stokes_G(mclg_ctx *ctx, int lev, const double *p, double *y);        /*
 int mclg_stokes_GT(mclg_ctx *ctx, int lev, const double *x, double *p);       /* GT_prod_d, Solver.c:645-666 */
 enum { MCLG_HEAT_K = 0, MCLG_HEAT_C = 1 };
 int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /* K_prod_d_heat, Update_temperature.c:935-962 */
+
+/* ---- learned initial guess (no reference counterpart) -------------------
+ * A fully convolutional network of `depth` 3x3 convolution layers (ReLU
+ * between them, `width` channels) with BF16 weights and FP32 accumulation,
+ * trained on the device by the library's own forward, backward and Adam
+ * kernels.  Parameters are one flat FP32 array, layer by layer:
+ * W[cout][cin][3][3] then b[cout].  Tensors are [batch][channel][h][w]. */
+typedef struct mclg_cnn mclg_cnn;
+int mclg_cnn_create(mclg_cnn **net, int cin, int width, int depth, int cout, unsigned long long seed);
+void mclg_cnn_destroy(mclg_cnn *net);
+size_t mclg_cnn_num_params(const mclg_cnn *net);
+int mclg_cnn_shape(const mclg_cnn *net, int *cin, int *width, int *depth, int *cout);
+int mclg_cnn_get_params(const mclg_cnn *net, float *out, size_t n);
+int mclg_cnn_set_params(mclg_cnn *net, const float *in, size_t n);   /* also resets the Adam moments */
+int mclg_cnn_forward(mclg_cnn *net, const float *x, int batch, int h, int w, float *y);
+/* Mean squared error against target and its gradient (flat parameter layout). */
+int mclg_cnn_gradient(mclg_cnn *net, const float *x, const float *target, int batch, int h, int w,
+                      double *loss, float *grad, size_t n);
+int mclg_cnn_adam_step(mclg_cnn *net, const float *grad, size_t n, float lr);   /* beta 0.9/0.999, eps 1e-8 */
+/* Adam on the mean squared error over nsamples (x, target) pairs held on the
+ * device; `iters` steps of `batch` samples drawn with a Philox stream. */
+int mclg_cnn_train(mclg_cnn *net, const float *x, const float *target, int nsamples, int h, int w, int batch,
+                   int iters, float lr, unsigned long long seed, float *loss_trace);
+int mclg_cnn_save(const mclg_cnn *net, const char *path);
+int mclg_cnn_load(mclg_cnn **net, const char *path);
+
+/* The guess on a context (converged solvers, warm_start=1 or 3).  Features
+ * live on the (grid+1)^2 node grid of a uniform mesh coarsened to `grid`
+ * elements per side: T, 0.2 log10 eta, the last solution (u, w scaled by its
+ * RMS speed, nodal p by its RMS) and the last change between solutions (scaled
+ * by its own RMS).  The network predicts, in units of the last change, the
+ * correction to the warm_start guess (the last solution, or its linear
+ * extrapolation), prolonged bilinearly to the mesh.  The solver keeps
+ * whichever of the corrected and the plain warm_start guess has the smaller
+ * FP64 residual, and switches the network off for 16 steps after it fails to
+ * save iterations on 3 steps in a row.  MCLG_GUESS_RECORD computes features
+ * and targets without a network (training data, see mclg_guess_sample). */
+enum { MCLG_GUESS_OFF = 0, MCLG_GUESS_RECORD = 1, MCLG_GUESS_LEARNED = 2,
+       MCLG_GUESS_FORCED = 3 /* the network's guess on every step, never judged (for measurement) */ };
+int mclg_guess_set(mclg_ctx *ctx, int mode, int grid, mclg_cnn *net);
+/* Features x[8][grid+1][grid+1] and target y[3][grid+1][grid+1] of the last
+ * solve; MCLG_BAD_INPUT when that solve had fewer than two solutions before it. */
+int mclg_guess_sample(mclg_ctx *ctx, float *x, size_t nx, float *y, size_t ny);
 
 #ifdef __cplusplus
 }

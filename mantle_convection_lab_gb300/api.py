@@ -62,7 +62,8 @@ class Config(C.Structure):
         ("vis_max", C.c_double), ("mg_smooth", C.c_int), ("mg_omega", C.c_double),
         ("mg_coarse", C.c_int), ("outer_rtol", C.c_double), ("inner_rtol", C.c_double),
         ("max_refine", C.c_int), ("max_outer", C.c_int), ("max_inner", C.c_int),
-        ("mg_eta_avg", C.c_int), ("mg_block_n", C.c_int),
+        ("mg_eta_avg", C.c_int), ("mg_block_n", C.c_int), ("guess_smooth", C.c_int),
+        ("stokes_method", C.c_int),
     ]
 
     @classmethod
@@ -87,6 +88,8 @@ class StepStats(C.Structure):
         ("ms_stokes", C.c_double), ("ms_heat", C.c_double), ("ms_total", C.c_double),
         ("kernel_launches", C.c_longlong), ("solver_kernel_ms", C.c_double),
         ("solver_kernel_launches", C.c_longlong), ("refine_passes", C.c_int),
+        ("guess_used", C.c_int), ("res_guess_learned", C.c_double), ("res_guess_prev", C.c_double),
+        ("ms_guess", C.c_double),
     ]
 
     def as_dict(self):
@@ -105,6 +108,7 @@ def lib():
         raise MclgError(BAD_INPUT, f"{LIB_PATH} is missing: run __graft_entry__.build() first")
     L = C.CDLL(LIB_PATH)
     vp, ip, dp, sz = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_size_t
+    fp = C.POINTER(C.c_float)
     sig = {
         "mclg_config_defaults": (None, [vp]), "mclg_config_from_input": (C.c_int, [C.c_char_p, vp]),
         "mclg_config_sizeof": (sz, []), "mclg_step_stats_sizeof": (sz, []),
@@ -126,6 +130,18 @@ def lib():
         "mclg_mesh_write_output": (C.c_int, [vp, C.c_char_p, C.c_int, dp, dp, dp, dp, dp, sz]),
         "mclg_stokes_matvec": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_stokes_G": (C.c_int, [vp, C.c_int, dp, dp]),
         "mclg_stokes_GT": (C.c_int, [vp, C.c_int, dp, dp]), "mclg_heat_matvec": (C.c_int, [vp, C.c_int, dp, dp]),
+        "mclg_cnn_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong]),
+        "mclg_cnn_destroy": (None, [vp]), "mclg_cnn_num_params": (sz, [vp]),
+        "mclg_cnn_shape": (C.c_int, [vp, ip, ip, ip, ip]),
+        "mclg_cnn_get_params": (C.c_int, [vp, fp, sz]), "mclg_cnn_set_params": (C.c_int, [vp, fp, sz]),
+        "mclg_cnn_forward": (C.c_int, [vp, fp, C.c_int, C.c_int, C.c_int, fp]),
+        "mclg_cnn_gradient": (C.c_int, [vp, fp, fp, C.c_int, C.c_int, C.c_int, dp, fp, sz]),
+        "mclg_cnn_adam_step": (C.c_int, [vp, fp, sz, C.c_float]),
+        "mclg_cnn_train": (C.c_int, [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                     C.c_ulonglong, fp]),
+        "mclg_cnn_save": (C.c_int, [vp, C.c_char_p]), "mclg_cnn_load": (C.c_int, [C.POINTER(vp), C.c_char_p]),
+        "mclg_guess_set": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "mclg_guess_sample": (C.c_int, [vp, fp, sz, fp, sz]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -150,6 +166,86 @@ def _dptr(a):
 
 def _iptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+GUESS_OFF, GUESS_RECORD, GUESS_LEARNED, GUESS_FORCED = 0, 1, 2, 3
+GUESS_CIN, GUESS_COUT = 8, 3
+
+
+class Cnn:
+    """The learned-guess network (mclg_cnn_*): 3x3 convolutions, BF16 weights,
+    FP32 accumulation, trained on the device by the library's own kernels."""
+
+    def __init__(self, cin=GUESS_CIN, width=32, depth=6, cout=GUESS_COUT, seed=0, _handle=None):
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            _check(lib().mclg_cnn_create(C.byref(self._h), cin, width, depth, cout, seed), "cnn_create")
+        a = [C.c_int() for _ in range(4)]
+        _check(lib().mclg_cnn_shape(self._h, *[C.byref(x) for x in a]), "cnn_shape")
+        self.cin, self.width, self.depth, self.cout = (x.value for x in a)
+        self.nparam = int(lib().mclg_cnn_num_params(self._h))
+
+    @classmethod
+    def load(cls, path):
+        h = C.c_void_p()
+        _check(lib().mclg_cnn_load(C.byref(h), os.fsencode(path)), "cnn_load")
+        return cls(_handle=h)
+
+    def save(self, path):
+        _check(lib().mclg_cnn_save(self._h, os.fsencode(path)), "cnn_save")
+
+    def close(self):
+        if self._h:
+            lib().mclg_cnn_destroy(self._h)
+            self._h = C.c_void_p()
+
+    __del__ = close
+
+    def params(self):
+        out = np.zeros(self.nparam, np.float32)
+        _check(lib().mclg_cnn_get_params(self._h, _fptr(out), out.size), "cnn_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib().mclg_cnn_set_params(self._h, _fptr(p), p.size), "cnn_set_params")
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        b, c, h, w = x.shape
+        y = np.zeros((b, self.cout, h, w), np.float32)
+        _check(lib().mclg_cnn_forward(self._h, _fptr(x), b, h, w, _fptr(y)), "cnn_forward")
+        return y
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        b, c, h, w = x.shape
+        g = np.zeros(self.nparam, np.float32)
+        loss = C.c_double()
+        _check(lib().mclg_cnn_gradient(self._h, _fptr(x), _fptr(t), b, h, w, C.byref(loss), _fptr(g), g.size),
+               "cnn_gradient")
+        return loss.value, g
+
+    def adam_step(self, g, lr):
+        g = np.ascontiguousarray(g, np.float32)
+        _check(lib().mclg_cnn_adam_step(self._h, _fptr(g), g.size, lr), "cnn_adam_step")
+
+    def train(self, x, t, batch=16, iters=100, lr=1e-3, seed=0):
+        """Adam on the mean squared error; returns the loss of every iteration."""
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        n, c, h, w = x.shape
+        trace = np.zeros(max(iters, 1), np.float32)
+        _check(lib().mclg_cnn_train(self._h, _fptr(x), _fptr(t), n, h, w, batch, iters, lr, seed, _fptr(trace)),
+               "cnn_train")
+        return trace[:iters]
 
 
 class Mesh:
@@ -323,6 +419,21 @@ class Model:
         p = np.zeros(self.nel)
         _check(lib().mclg_stokes_GT(self._c, -1, _dptr(x), _dptr(p)), "stokes_GT")
         return p
+
+    def guess_set(self, mode, grid=128, net=None):
+        """Learned initial guess: GUESS_OFF, GUESS_RECORD (features and targets
+        only) or GUESS_LEARNED (needs `net`)."""
+        self._guess_net = net   # keep the network alive while the context uses it
+        self._guess_grid = grid
+        _check(lib().mclg_guess_set(self._c, mode, grid, net._h if net is not None else None), "guess_set")
+
+    def guess_sample(self):
+        """(features [8, g+1, g+1], target [3, g+1, g+1]) of the last solve."""
+        n = self._guess_grid + 1
+        x = np.zeros((GUESS_CIN, n, n), np.float32)
+        y = np.zeros((GUESS_COUT, n, n), np.float32)
+        _check(lib().mclg_guess_sample(self._c, _fptr(x), x.size, _fptr(y), y.size), "guess_sample")
+        return x, y
 
     def heat_matvec(self, which, x):
         x = np.ascontiguousarray(x, np.float64)

@@ -472,8 +472,8 @@ __device__ __forceinline__ void g_entries(double hx, double hz, int a, double &g
 }
 
 // y = G s at every node (masked); s in Morton order.
-__device__ void gmul64(int N0, const unsigned char *mask, double hx, double hz, const double *s, double2 *y,
-                       int tid, int nth)
+__device__ void gmul64(int N0, const unsigned char *mask, const GTab &gt, const double *s, double2 *y, int tid,
+                       int nth)
 {
 	const int n = N0 + 1;
 	for (int A = tid; A < n * n; A += nth) {
@@ -485,8 +485,7 @@ __device__ void gmul64(int N0, const unsigned char *mask, double hx, double hz, 
 			const int ex = eox[q], ez = eoz[q];
 			if (ex < 0 || ex >= N0 || ez < 0 || ez >= N0)
 				continue;
-			double g0, g1;
-			g_entries(hx, hz, ea[q], g0, g1);
+			const double g0 = gt.g0[ea[q]], g1 = gt.g1[ea[q]];
 			const double se = s[morton(ex, ez)];
 			s0 += g0 * se;
 			s1 += g1 * se;
@@ -497,7 +496,7 @@ __device__ void gmul64(int N0, const unsigned char *mask, double hx, double hz, 
 }
 
 // (G^T u)_e at element (ex, ez), free dofs in ascending equation order.
-__device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask, double hx, double hz,
+__device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask, const GTab &gt,
                                                const double2 *u, int ex, int ez)
 {
 	const int n = N0 + 1;
@@ -506,8 +505,7 @@ __device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask
 #pragma unroll
 	for (int c = 0; c < 4; c++) {
 		const int a = kSortedCorner[c];
-		double g0, g1;
-		g_entries(hx, hz, a, g0, g1);
+		const double g0 = gt.g0[a], g1 = gt.g1[a];
 		const double2 ua = u[cn[a]];
 		const unsigned m = mask[cn[a]];
 		if (!(m & 1u))
@@ -518,9 +516,225 @@ __device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask
 	return s;
 }
 
+// FP64 residual R = [F - K d - G p ; G^T d] into a.R, a.Rc; rs = {|R_m|^2, |R_c|^2, |F|^2}
+// summed over the grid (every block holds the same values on return).
+template <class TI>
+__device__ void stokes_residual(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
+                                const double2 *d, const double *p, double (&rs)[3])
+{
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	const GTab &gt = a.gt;
+	tile_pass<double, double2>(sm, true, N0, a.mask0, a.vis, d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0, nullptr);
+	gmul64(N0, a.mask0, gt, p, a.R, tid, nth);
+	g.sync();
+	rs[0] = rs[1] = rs[2] = 0.0;
+	for (int A = tid; A < nn; A += nth) {
+		const double2 f = a.F[A], kd = a.Kd[A], gp = a.R[A];
+		const double2 r = make_double2(f.x - kd.x - gp.x, f.y - kd.y - gp.y);
+		a.R[A] = r;
+		rs[0] += r.x * r.x + r.y * r.y;
+		rs[2] += f.x * f.x + f.y * f.y;
+	}
+	for (int e = tid; e < ne; e += nth) {
+		const int ex = e / N0, ez = e - ex * N0;
+		const double c = gtmul64_elem(N0, a.mask0, gt, d, ex, ez);
+		a.Rc[morton(ex, ez)] = c;
+		rs[1] += c * c;
+	}
+	grid_reduce<3>(g, red, rs, 0u);
+}
+
+// (G^T u)_e for a TI velocity field (free dofs only).
+template <class V>
+__device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask, const GTab &gt, const V *u, int ex,
+                                               int ez)
+{
+	const int n = N0 + 1;
+	const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
+	double s = 0.0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		const double g0 = gt.g0[a], g1 = gt.g1[a];
+		const V ua = u[cn[a]];
+		const unsigned m = mask[cn[a]];
+		if (!(m & 1u))
+			s += g0 * (double)ua.x;
+		if (!(m & 2u))
+			s += g1 * (double)ua.y;
+	}
+	return s;
+}
+
+// z = M^-1 v for M = diag(one V-cycle of K, BAB): the velocity part goes
+// through the TI hierarchy (z_u stays in TI), the pressure part is divided by
+// BAB.  Returns <z, v> over the grid.
+template <class TI>
+__device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
+                                const double2 *vu, const double *vp, typename V2T<TI>::t *zu, double *zp)
+{
+	typedef typename V2T<TI>::t VI;
+	const MGHier<TI> &H = a.H;
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	VI *bI = H.lv[0].b;
+	for (int A = tid; A < nn; A += nth) {
+		const double2 v = vu[A];
+		VI w;
+		w.x = (TI)v.x;
+		w.y = (TI)v.y;
+		bI[A] = w;
+	}
+	g.sync();
+	vcycle<TI>(g, sm, H, bI, zu);
+	double dot[1] = {0.0};
+	for (int A = tid; A < nn; A += nth) {
+		const VI z = zu[A];
+		const double2 v = vu[A];
+		dot[0] += (double)z.x * v.x + (double)z.y * v.y;
+	}
+	for (int e = tid; e < ne; e += nth) {
+		const double z = vp[e] / a.bab[e];
+		zp[e] = z;
+		dot[0] += z * vp[e];
+	}
+	grid_reduce<1>(g, red, dot, 0u);
+	return dot[0];
+}
+
+// Correction solve by preconditioned MINRES (the Lanczos-based algorithm of
+// Elman, Silvester and Wathen, "Finite Elements and Fast Iterative Solvers",
+// Alg. 4.1) on [K G; G^T 0][x_u; x_p] = [R_m; -R_c] from a zero start, with
+// the block-diagonal SPD preconditioner diag(V-cycle, BAB).  K is applied in
+// TI by the tiled operator, G and G^T in FP64; Lanczos and direction vectors
+// are FP64 and x_u, x_p accumulate in a.dd, a.dpv.  The FP64 refinement
+// around this solve restores full accuracy.  Stops when the M^-1-norm of the
+// residual has dropped by rtol.  Returns the iterations.
+template <class TI>
+__device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
+                                 double rtol, int maxit, int *status)
+{
+	typedef typename V2T<TI>::t VI;
+	const MGHier<TI> &H = a.H;
+	const MGLevel<TI> &L0 = H.lv[0];
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	double2 *vu[2] = {a.mv[0], a.mv[1]}, *wu[2] = {a.mw[0], a.mw[1]};
+	double *vp[2] = {a.mvp[0], a.mvp[1]}, *zp[2] = {a.mzp[0], a.mzp[1]}, *wp[2] = {a.mwp[0], a.mwp[1]};
+	VI *zu[2] = {H.pz, H.pp}, *kz = H.pq;   // inner-CG vectors, free while MINRES runs
+	const GTab &gt = a.gt;
+	const double2 zero2 = make_double2(0.0, 0.0);
+	for (int A = tid; A < nn; A += nth) {
+		vu[0][A] = a.R[A];
+		vu[1][A] = zero2;
+		wu[0][A] = zero2;
+		wu[1][A] = zero2;
+		a.dd[A] = zero2;
+	}
+	for (int e = tid; e < ne; e += nth) {
+		vp[0][e] = -a.Rc[e];
+		vp[1][e] = 0.0;
+		wp[0][e] = 0.0;
+		wp[1][e] = 0.0;
+		a.dpv[e] = 0.0;
+	}
+	g.sync();
+	double gam2 = block_precond(a, sm, g, red, vu[0], vp[0], zu[0], zp[0]);
+	if (!(gam2 > 0.0))
+		return 0;
+	double gam = sqrt(gam2), gam_prev = 1.0;
+	const double eta0 = gam;
+	double eta = gam, c_prev = 1.0, c_cur = 1.0, s_prev = 0.0, s_cur = 0.0;
+	int cv = 0, cw = 0, it = 0;   // index cv: z(j), v(j); 1-cv: v(j-1).  cw: w(j); 1-cw: w(j-1)
+	while (it < maxit) {
+		// A z(j), unscaled (z~ = z / gam): K z_u + G z_p, and G^T z_u per element
+		tile_pass<TI, VI>(sm, true, L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
+		gmul64(N0, a.mask0, gt, zp[cv], a.u1, tid, nth);
+		g.sync();
+		double dl[1] = {0.0};
+		for (int A = tid; A < nn; A += nth) {
+			const VI k = kz[A], z = zu[cv][A];
+			const double2 q = a.u1[A];
+			const double2 az = make_double2((double)k.x + q.x, (double)k.y + q.y);
+			a.Kd[A] = az;
+			dl[0] += az.x * (double)z.x + az.y * (double)z.y;
+		}
+		for (int e = tid; e < ne; e += nth) {
+			const int ex = e / N0, ez = e - ex * N0;
+			const int me = morton(ex, ez);
+			const double t = gtmul_elem_t(N0, a.mask0, gt, zu[cv], ex, ez);
+			a.Ahp[me] = t;
+			dl[0] += t * zp[cv][me];
+		}
+		grid_reduce<1>(g, red, dl, 0u);
+		const double delta = dl[0] / (gam * gam);
+		// v(j+1) = A z~ - (delta/gam) v(j) - (gam/gam_prev) v(j-1), into v(j-1)'s buffer
+		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
+		for (int A = tid; A < nn; A += nth) {
+			const double2 az = a.Kd[A], v = vu[cv][A], vo = vu[1 - cv][A];
+			vu[1 - cv][A] = make_double2(az.x * ig - dg * v.x - gg * vo.x, az.y * ig - dg * v.y - gg * vo.y);
+		}
+		for (int e = tid; e < ne; e += nth)
+			vp[1 - cv][e] = a.Ahp[e] * ig - dg * vp[cv][e] - gg * vp[1 - cv][e];
+		g.sync();
+		const double gn2 = block_precond(a, sm, g, red, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv]);
+		const double gam_next = sqrt(fmax(gn2, 0.0));
+		// Givens rotations
+		const double a0 = c_cur * delta - c_prev * s_cur * gam;
+		const double a1 = sqrt(a0 * a0 + gam_next * gam_next);
+		const double a2 = s_cur * delta + c_prev * c_cur * gam;
+		const double a3 = s_prev * gam;
+		if (!(a1 > 0.0) || !isfinite(a1)) {
+			if (!isfinite(a1) && tid == 0)
+				atomicOr(status, 2);
+			break;
+		}
+		const double c_next = a0 / a1, s_next = gam_next / a1;
+		// w(j+1) = (z~(j) - a3 w(j-1) - a2 w(j)) / a1 into w(j-1)'s buffer; x += c_next eta w(j+1)
+		const double ia1 = 1.0 / a1, step = c_next * eta;
+		for (int A = tid; A < nn; A += nth) {
+			const VI z = zu[cv][A];
+			const double2 wo = wu[1 - cw][A], w = wu[cw][A];
+			const double2 wn = make_double2(((double)z.x * ig - a3 * wo.x - a2 * w.x) * ia1,
+			                                ((double)z.y * ig - a3 * wo.y - a2 * w.y) * ia1);
+			wu[1 - cw][A] = wn;
+			double2 x = a.dd[A];
+			x.x += step * wn.x;
+			x.y += step * wn.y;
+			a.dd[A] = x;
+		}
+		for (int e = tid; e < ne; e += nth) {
+			const double wn = (zp[cv][e] * ig - a3 * wp[1 - cw][e] - a2 * wp[cw][e]) * ia1;
+			wp[1 - cw][e] = wn;
+			a.dpv[e] += step * wn;
+		}
+		eta = -s_next * eta;
+		it++;
+		cv = 1 - cv;
+		cw = 1 - cw;
+		gam_prev = gam;
+		gam = gam_next;
+		c_prev = c_cur;
+		c_cur = c_next;
+		s_prev = s_cur;
+		s_cur = s_next;
+		if (!isfinite(eta)) {
+			if (tid == 0)
+				atomicOr(status, 2);
+			break;
+		}
+		if (!(fabs(eta) > rtol * eta0) || !(gam > 0.0))
+			break;
+		g.sync();
+	}
+	g.sync();
+	return it;
+}
+
 // ---- the persistent kernel ----------------------------------------------------
 template <class TI>
-__global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
+__global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 {
 	typedef typename V2T<TI>::t VI;
 	cg::grid_group g = cg::this_grid();
@@ -530,6 +744,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	int *status = &a.sc->status;
+	const GTab &gt = a.gt;
 
 	// -- per-step setup: viscosity on every level, inverse diagonals, BAB, coarse inverse
 	for (int A = tid; A < nn; A += nth)
@@ -587,27 +802,32 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 
 	int refine = 0, outer_total = 0, inner_total = 0, capped = 0;
 	double res_m = 0.0, res_c = 0.0, fnorm = 1.0;
+	if (a.d_alt != nullptr) {
+		// Two candidate guesses: (d, p) from the network and (d_alt, p_alt),
+		// the previous step's solution.  Keep the one with the smaller FP64
+		// residual; a non-finite network guess always loses.
+		double rl[3], rp[3];
+		stokes_residual(a, sm, g, red, a.d, a.p, rl);
+		stokes_residual(a, sm, g, red, a.d_alt, a.p_alt, rp);
+		const double el = rl[0] + rl[1], ep = rp[0] + rp[1];
+		const bool learned = isfinite(el) && (a.guess_force || el < ep);
+		if (!learned) {
+			for (int A = tid; A < nn; A += nth)
+				a.d[A] = a.d_alt[A];
+			for (int e = tid; e < ne; e += nth)
+				a.p[e] = a.p_alt[e];
+		}
+		if (tid == 0) {
+			a.sc->guess_used = learned ? 1 : 0;
+			a.sc->res_learned = sqrt(el / rl[2]);
+			a.sc->res_prev = sqrt(ep / rp[2]);
+		}
+		g.sync();
+	}
 	while (true) {
 		// -- FP64 residual R = [F - K d - G p ; G^T d]
-		tile_pass<double, double2>(sm, true, N0, a.mask0, a.vis, a.d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0,
-		                           nullptr);
-		gmul64(N0, a.mask0, a.hx, a.hz, a.p, a.R, tid, nth);
-		g.sync();
-		double rs[3] = {0.0, 0.0, 0.0};
-		for (int A = tid; A < nn; A += nth) {
-			const double2 f = a.F[A], kd = a.Kd[A], gp = a.R[A];
-			const double2 r = make_double2(f.x - kd.x - gp.x, f.y - kd.y - gp.y);
-			a.R[A] = r;
-			rs[0] += r.x * r.x + r.y * r.y;
-			rs[2] += f.x * f.x + f.y * f.y;
-		}
-		for (int e = tid; e < ne; e += nth) {
-			const int ex = e / N0, ez = e - ex * N0;
-			const double c = gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.d, ex, ez);
-			a.Rc[morton(ex, ez)] = c;
-			rs[1] += c * c;
-		}
-		grid_reduce<3>(g, red, rs, 0u);
+		double rs[3];
+		stokes_residual(a, sm, g, red, a.d, a.p, rs);
 		fnorm = sqrt(rs[2]);
 		res_m = sqrt(rs[0]) / fnorm;
 		res_c = sqrt(rs[1]) / fnorm;
@@ -624,6 +844,28 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 			break;
 		}
 		refine++;
+
+		if (a.method == 1) {
+			// -- correction solve: MINRES on [K G; G^T 0][dd; dp] = [R_m; -R_c].
+			// Far from the target (res > 1e4 rtol) a pass reduces by 1e-2,
+			// where MINRES converges fastest; close to it, by what is left to
+			// reach rtol (with a factor 2 margin), but not below outer_rtol.
+			const double prt = res > 1e4 * a.rtol ? 1e-2 : fmax(a.outer_rtol, 0.5 * a.rtol / res);
+			const int it = minres_correction<TI>(a, sm, g, red, prt, a.max_outer, status);
+			outer_total += it;
+			inner_total += it + 1;
+			for (int A = tid; A < nn; A += nth) {
+				const double2 c = a.dd[A];
+				double2 v = a.d[A];
+				v.x += c.x;
+				v.y += c.y;
+				a.d[A] = v;
+			}
+			for (int e = tid; e < ne; e += nth)
+				a.p[e] += a.dpv[e];
+			g.sync();
+			continue;
+		}
 
 		// -- correction solve: Uzawa on [K G; G^T 0][dd; dp] = [R_m; -R_c]
 		VI *bI = H.lv[0].b, *xI = H.px;   // level-0 buffers double as CG input/output here
@@ -646,7 +888,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 		for (int e = tid; e < ne; e += nth) {
 			const int ex = e / N0, ez = e - ex * N0;
 			const int me = morton(ex, ez);
-			const double v = a.Rc[me] + gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.dd, ex, ez);
+			const double v = a.Rc[me] + gtmul64_elem(N0, a.mask0, gt, a.dd, ex, ez);
 			r1[me] = v;
 			a.dpv[me] = 0.0;
 			c0[0] += v * v;
@@ -669,7 +911,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 			for (int e = tid; e < ne; e += nth)
 				s2[e] = cycle == 0 ? z1[e] : z1[e] + delta * s1[e];
 			g.sync();
-			gmul64(N0, a.mask0, a.hx, a.hz, s2, a.u1, tid, nth);
+			gmul64(N0, a.mask0, gt, s2, a.u1, tid, nth);
 			for (int A = tid; A < nn; A += nth) {
 				const double2 v = a.u1[A];
 				VI w;
@@ -688,7 +930,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_mg(MGArgs<TI> a)
 			for (int e = tid; e < ne; e += nth) {
 				const int ex = e / N0, ez = e - ex * N0;
 				const int me = morton(ex, ez);
-				const double t = gtmul64_elem(N0, a.mask0, a.hx, a.hz, a.u1, ex, ez);
+				const double t = gtmul64_elem(N0, a.mask0, gt, a.u1, ex, ez);
 				a.Ahp[me] = t;
 				sa[0] += s2[me] * t;
 			}

@@ -35,12 +35,19 @@ struct MGHier {
 	typename V2T<T>::t *px, *pr, *pz, *pp, *pq;
 };
 
+// G coefficients (Build_matrix.c get_element_G) of the 4 corners of an
+// element of the uniform mesh, filled on the host.
+struct GTab {
+	double g0[4], g1[4];
+};
+
 // The converged Stokes solve of one time step (FP64 state, TI inner solves).
 template <class TI>
 struct MGArgs {
 	MGHier<TI> H;
 	int N0;                      // fine elements per side
 	double hx, hz;               // fine element half-widths (dx_dxi, dz_deta)
+	GTab gt;                     // G coefficients for those half-widths
 	const double *vis;           // [nno] viscosity (FP64, G.node order == x-major)
 	const unsigned char *mask0;  // fine-level Dirichlet mask
 	const double *vbcval;        // [2*nno] BC values (for the nodal velocity)
@@ -50,6 +57,12 @@ struct MGArgs {
 	double2 *V;                  // [nno] nodal velocity out (v_to_nodes)
 	double2 *R, *dd, *u1, *Kd, *invD64, *kdiag64;   // FP64 node vectors
 	double *Rc, *r0, *r1, *r2, *z0, *z1, *s1, *s2, *Ahp, *dpv, *bab;  // FP64 element vectors
+	int method;                  // correction solve: 0 Uzawa with inner MG-PCG, 1 MINRES (block-diagonal preconditioner)
+	double2 *mv[2], *mw[2];      // MINRES Lanczos and direction vectors, velocity part (z_u lives in TI)
+	double *mvp[2], *mzp[2], *mwp[2]; // Lanczos, preconditioned and direction vectors, pressure part (Morton)
+	const double2 *d_alt;        // second candidate guess (previous solution) or null
+	const double *p_alt;
+	int guess_force;             // keep (d, p) without judging it against (d_alt, p_alt)
 	GridRed red;
 	StepScalars *sc;
 	double rtol, outer_rtol, inner_rtol;

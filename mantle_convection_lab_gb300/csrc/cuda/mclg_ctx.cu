@@ -6,6 +6,7 @@
 #include <string.h>
 #include <vector>
 #include "k_mg.cuh"
+#include "cnn.cuh"
 #include "../host/mclg_host.h"
 
 namespace mclg {
@@ -55,7 +56,7 @@ struct mclg_ctx {
 	mclg_mesh mesh;
 	int fl;                       // finest level index
 	cudaStream_t st;
-	cudaEvent_t ev[6];
+	cudaEvent_t ev[7];
 	int num_sms;
 	int coop_uzawa, coop_heat;    // cooperative grid sizes
 	DevLevelBuf lb;
@@ -84,6 +85,17 @@ struct mclg_ctx {
 	MGArgs<double> mgd;
 	void *mg_ptr[192];
 	int mg_nptr;
+	// learned initial guess (converged solvers, warm_start=1)
+	mclg_cnn *gnet;
+	int gmode, gs, gnc;           // mode, coarsening factor, coarse elements per side
+	int ghist;                    // solutions seen since the guess was switched on
+	int gsample, gtimed;          // a sample from the last solve exists; ev[6] was recorded
+	double2 *d_h1, *d_h2, *d_cand;   // last two solutions, second candidate guess
+	double *p_h1, *p_h2, *p_cand, *gscale;
+	float *gX, *gYt, *gYs;        // features, target and filter scratch on the coarse node grid
+	CnnWork gw;
+	int goff, gbad;               // steps left with the network off; consecutive steps it did not pay
+	int git_prev;                 // inner iterations of the last step solved from the last solution (-1: none)
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -260,6 +272,10 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	const mclg_level &H = m.lev[c->fl];
 	const int N0 = m.max_elx[c->fl], n0 = N0 + 1;
 	int Nc = c->cfg.mg_coarse;
+	if (c->cfg.stokes_method != 0 && c->cfg.stokes_method != 1) {
+		mclg_set_error("stokes_method=%d: 0 (Uzawa) or 1 (MINRES)", c->cfg.stokes_method);
+		return MCLG_BAD_INPUT;
+	}
 	if (Nc < 2 || Nc > 8 || (Nc & (Nc - 1)) || Nc > N0) {
 		mclg_set_error("mg_coarse=%d: need a power of two in [2, min(8, %d)]", Nc, N0);
 		return MCLG_BAD_INPUT;
@@ -322,6 +338,20 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	a.N0 = N0;
 	a.hx = 0.5 * m.dx[c->fl];
 	a.hz = 0.5 * m.dz[c->fl];
+	{
+		// element_g (mclg_dev.cuh) for the uniform mesh: g0 = -sum dN/dxi * hz, g1 = -sum dN/deta * hx
+		ShapeTables S;
+		shape_tables(S);
+		for (int k = 0; k < 4; k++) {
+			double g0 = 0.0, g1 = 0.0;
+			for (int gs = 0; gs < 4; gs++) {
+				g0 -= S.dNdxi[k][gs] * a.hz;
+				g1 -= S.dNdeta[k][gs] * a.hx;
+			}
+			a.gt.g0[k] = g0;
+			a.gt.g1[k] = g1;
+		}
+	}
 	a.vis = c->vis;
 	a.vbcval = c->lb.vbcval;
 	a.F = c->F;
@@ -337,6 +367,16 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	double **ev[] = {&a.Rc, &a.r0, &a.r1, &a.r2, &a.z0, &a.z1, &a.s1, &a.s2, &a.Ahp, &a.dpv, &a.bab};
 	for (double **pp : ev)
 		CK(mg_alloc(c, pp, ne));
+	a.method = c->cfg.stokes_method;
+	if (a.method == 1) {
+		for (int k = 0; k < 2; k++) {
+			CK(mg_alloc(c, &a.mv[k], nn0));
+			CK(mg_alloc(c, &a.mw[k], nn0));
+			CK(mg_alloc(c, &a.mvp[k], ne));
+			CK(mg_alloc(c, &a.mzp[k], ne));
+			CK(mg_alloc(c, &a.mwp[k], ne));
+		}
+	}
 	a.red.part = c->red_part;
 	a.sc = c->sc;
 	a.rtol = c->cfg.stokes_rtol;
@@ -350,16 +390,87 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	return MCLG_OK;
 }
 
+// History buffers of the converged solvers: the last two solutions (for
+// warm_start=3 and the learned guess) and a second candidate guess.
+static int alloc_history(mclg_ctx *c)
+{
+	if (c->d_h1 != NULL)
+		return MCLG_OK;
+	const size_t nn = (size_t)c->L.nno, ne = (size_t)c->L.nel;
+	CK(dalloc(&c->d_h1, nn));
+	CK(dalloc(&c->d_h2, nn));
+	CK(dalloc(&c->d_cand, nn));
+	CK(dalloc(&c->p_h1, ne));
+	CK(dalloc(&c->p_h2, ne));
+	CK(dalloc(&c->p_cand, ne));
+	CK(dalloc(&c->gscale, 4));
+	c->ghist = 0;
+	return MCLG_OK;
+}
+
 static int launch_stokes_mg(mclg_ctx *c)
 {
 	const mclg_config &f = c->cfg;
 	// warm_start: 0 = zero guess; 1 = previous (d, p); 2 = the reference's
-	// policy for zero_P=0 (initial_d_p, Solver.c:251-278): d zeroed, p kept
-	if (f.warm_start != 1)
+	// policy for zero_P=0 (initial_d_p, Solver.c:251-278): d zeroed, p kept;
+	// 3 = linear extrapolation in time of the last two solutions (previous
+	// solution until two exist)
+	if (f.warm_start != 1 && f.warm_start != 3)
 		CK(cudaMemsetAsync(c->d, 0, c->L.nno * sizeof(double2), c->st));
 	if (f.warm_start == 0)
 		CK(cudaMemsetAsync(c->p, 0, c->L.nel * sizeof(double), c->st));
 	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
+	CK(cudaMemsetAsync(&c->sc->guess_used, 0xff, sizeof(int), c->st));   // -1: not judged
+	const int N0 = c->mgf.N0 ? c->mgf.N0 : c->mgd.N0;
+	const unsigned char *mask0 = c->mgf.N0 ? c->mgf.mask0 : c->mgd.mask0;
+	const size_t nn = (size_t)c->L.nno, ne = (size_t)c->L.nel;
+	const bool track = c->d_h1 != NULL;
+	const bool hist2 = track && c->ghist >= 2;
+	const bool extrap = hist2 && f.warm_start == 3;
+	const bool net_on = hist2 && (c->gmode == MCLG_GUESS_LEARNED || c->gmode == MCLG_GUESS_FORCED) &&
+	                    c->gnet != NULL && c->goff == 0;
+	const bool feat = hist2 && (c->gmode == MCLG_GUESS_RECORD || net_on);
+	const double2 *d_alt = nullptr;
+	const double *p_alt = nullptr;
+	c->gtimed = 0;
+	c->gsample = 0;
+	if (track) {
+		// features from (T, eta, last two solutions) before d is overwritten
+		if (feat)
+			guess_features(c->st, N0, c->gs, c->T, c->vis, c->d, c->p, c->d_h2, c->p_h2, c->gX, c->gscale);
+		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+		if (extrap) {
+			guess_extrapolate(c->st, (int)nn, (int)ne, mask0, c->d_h1, c->p_h1, c->d_h2, c->p_h2, c->d, c->p);
+			c->launches++;
+		}
+		if (net_on) {
+			// the network's change on top of that base guess; the kernel
+			// keeps whichever of the two has the smaller FP64 residual
+			CK(cudaMemcpyAsync(c->d_cand, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+			CK(cudaMemcpyAsync(c->p_cand, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+			int rc = cnn_forward_dev(c->gnet, c->gw, c->gX, c->st);
+			if (rc)
+				return rc;
+			float *Y = const_cast<float *>(cnn_output(c->gnet, c->gw));
+			guess_smooth(c->st, c->gnc + 1, f.guess_smooth, Y, c->gYs);
+			guess_apply(c->st, N0, c->gs, Y, c->gscale, mask0, c->d_cand, c->p_cand, c->d, c->p);
+			c->launches += 2 * (f.guess_smooth > 0 ? f.guess_smooth : 0);
+			d_alt = c->d_cand;
+			p_alt = c->p_cand;
+			c->launches += 1 + cnn_layers(c->gnet);
+		}
+		if (feat)
+			c->launches += 2;
+		CK(cudaGetLastError());
+		CK(cudaEventRecord(c->ev[6], c->st));
+		c->gtimed = 1;
+	}
+	c->mgf.d_alt = d_alt;
+	c->mgf.p_alt = p_alt;
+	c->mgd.d_alt = d_alt;
+	c->mgd.p_alt = p_alt;
+	c->mgf.guess_force = c->mgd.guess_force = c->gmode == MCLG_GUESS_FORCED;
 	if (f.precision == 2) {
 		void *args[] = {&c->mgd};
 		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(1), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
@@ -368,7 +479,48 @@ static int launch_stokes_mg(mclg_ctx *c)
 		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(0), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
 	}
 	c->launches++;
+	if (track) {
+		if (feat) {
+			// target: the converged solution minus the base guess (extrapolation or the last solution)
+			guess_target(c->st, N0, c->gs, c->d, c->p, c->d_h1, c->p_h1, extrap ? c->d_h2 : nullptr,
+			             extrap ? c->p_h2 : nullptr, c->gscale, c->gYt);
+			c->gsample = 1;
+			c->launches++;
+		}
+		CK(cudaGetLastError());
+		double2 *t2 = c->d_h2;
+		c->d_h2 = c->d_h1;
+		c->d_h1 = t2;
+		double *t1 = c->p_h2;
+		c->p_h2 = c->p_h1;
+		c->p_h1 = t1;
+		c->ghist++;
+	}
 	return MCLG_OK;
+}
+
+// Switch the network off for 16 steps after 3 consecutive steps on which its
+// guess won the residual test but took more inner iterations than the last
+// step solved from the previous solution.
+static void guess_bookkeeping(mclg_ctx *c)
+{
+	if (c->gmode != MCLG_GUESS_LEARNED || c->cfg.precision == 0)
+		return;   // MCLG_GUESS_FORCED never switches the network off
+	const StepScalars &s = *c->sc_host;
+	if (s.guess_used == 1) {
+		if (c->git_prev >= 0 && s.cg_cycles > c->git_prev)
+			c->gbad++;
+		else
+			c->gbad = 0;
+		if (c->gbad >= 3) {
+			c->goff = 16;
+			c->gbad = 0;
+		}
+	} else {
+		c->git_prev = s.cg_cycles;
+		if (c->goff > 0)
+			c->goff--;
+	}
 }
 
 extern "C" {
@@ -441,8 +593,9 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 		}                                          \
 	} while (0)
 	CKD(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-	for (int i = 0; i < 6; i++)
+	for (int i = 0; i < 7; i++)
 		CKD(cudaEventCreate(&c->ev[i]));
+	c->git_prev = -1;
 	int dev = 0;
 	CKD(cudaGetDevice(&dev));
 	CKD(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -532,6 +685,11 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 		upload_shape_tables_mg(S, c->st);
 		upload_op_tables(S, c->mesh.dz[c->fl] / c->mesh.dx[c->fl], c->st);
 		c->coop_mg = coop_blocks(stokes_mg_kernel(cfg->precision == 2), c->num_sms, 1 << 30);
+		if (cfg->warm_start == 3 && (rc = alloc_history(c)) != MCLG_OK) {
+			mclg_destroy(c);
+			*out = NULL;
+			return rc;
+		}
 	}
 	if (c->coop_uzawa < 1 || c->coop_heat < 1) {
 		mclg_set_error("cooperative occupancy query failed");
@@ -567,9 +725,14 @@ void mclg_destroy(mclg_ctx *c)
 		cudaFree(c->mg_ptr[i]);
 	if (c->sc_host)
 		cudaFreeHost(c->sc_host);
-	for (int i = 0; i < 6; i++)
+	for (int i = 0; i < 7; i++)
 		if (c->ev[i])
 			cudaEventDestroy(c->ev[i]);
+	void *gptrs[] = {c->d_h1, c->d_h2, c->d_cand, c->p_h1, c->p_h2, c->p_cand, c->gscale, c->gX, c->gYt, c->gYs};
+	for (void *q : gptrs)
+		if (q)
+			cudaFree(q);
+	cnn_work_free(c->gw);
 	if (c->st)
 		cudaStreamDestroy(c->st);
 	mclg_mesh_free(&c->mesh);
@@ -746,6 +909,9 @@ static void fill_stats_stokes(mclg_ctx *c, mclg_step_stats *st)
 	st->res_continuity = s.res_c;
 	st->status = status_from_bits(s.status);
 	st->refine_passes = s.refine_passes;
+	st->guess_used = c->cfg.precision != 0 ? s.guess_used : -1;
+	st->res_guess_learned = st->guess_used >= 0 ? s.res_learned : 0.0;
+	st->res_guess_prev = st->guess_used >= 0 ? s.res_prev : 0.0;
 }
 
 int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
@@ -759,6 +925,7 @@ int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
 		return rc;
 	if ((rc = read_scalars(c)))
 		return rc;
+	guess_bookkeeping(c);
 	fill_stats_stokes(c, st);
 	return MCLG_OK;
 }
@@ -878,6 +1045,7 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 	CK(cudaEventRecord(c->ev[3], c->st));
 	if ((rc = read_scalars(c)))
 		return rc;
+	guess_bookkeeping(c);
 	fill_stats_stokes(c, st);
 	const StepScalars &s = *c->sc_host;
 	st->heat_cg_cycles = s.heat_cycles;
@@ -890,8 +1058,13 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 	st->ms_heat = ms;
 	cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
 	st->ms_total = ms;
-	cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+	cudaEventElapsedTime(&ms, c->gtimed ? c->ev[6] : c->ev[4], c->ev[5]);
 	st->solver_kernel_ms = ms;
+	st->ms_guess = 0.0;
+	if (c->gtimed) {
+		cudaEventElapsedTime(&ms, c->ev[4], c->ev[6]);
+		st->ms_guess = ms;
+	}
 	st->solver_kernel_launches = 1;
 	st->kernel_launches = c->launches - l0;
 	c->timestep++;
@@ -1317,6 +1490,85 @@ extern "C" int mclg_solve_velocity_pressure_noalloc(mclg_ctx *c, mclg_step_stats
 		st->res_continuity = hs.res_c;
 		st->status = status_from_bits(hs.status);
 		st->refine_passes = 0;
+		st->guess_used = -1;
 	}
+	return MCLG_OK;
+}
+
+// ---- learned initial guess --------------------------------------------------------
+extern "C" int mclg_guess_set(mclg_ctx *c, int mode, int grid, mclg_cnn *net)
+{
+	if (c == NULL || mode < MCLG_GUESS_OFF || mode > MCLG_GUESS_FORCED)
+		return MCLG_BAD_INPUT;
+	if (mode == MCLG_GUESS_OFF) {
+		c->gmode = MCLG_GUESS_OFF;
+		c->gnet = NULL;
+		c->gsample = 0;
+		return MCLG_OK;
+	}
+	if (c->cfg.precision == 0 || (c->cfg.warm_start != 1 && c->cfg.warm_start != 3)) {
+		mclg_set_error("the learned guess needs a converged solver (precision=mixed/fp64mg) with warm_start=1 or 3");
+		return MCLG_BAD_INPUT;
+	}
+	const int N0 = c->mgf.N0 ? c->mgf.N0 : c->mgd.N0;
+	if (grid < 2 || grid > N0 || N0 % grid != 0) {
+		mclg_set_error("guess grid %d: need 2 <= grid <= %d dividing %d", grid, N0, N0);
+		return MCLG_BAD_INPUT;
+	}
+	if (mode == MCLG_GUESS_LEARNED || mode == MCLG_GUESS_FORCED) {
+		int cin = 0, cout = 0;
+		if (net == NULL || cnn_channels(net, &cin, &cout) != MCLG_OK || cin != kGuessCin || cout != kGuessCout) {
+			mclg_set_error("the learned guess needs a network with %d input and %d output channels", kGuessCin,
+			               kGuessCout);
+			return MCLG_BAD_INPUT;
+		}
+	}
+	const size_t plane = (size_t)(grid + 1) * (grid + 1);
+	int rc = alloc_history(c);
+	if (rc)
+		return rc;
+	if (c->gX == NULL || c->gnc != grid) {
+		if (c->gX)
+			cudaFree(c->gX);
+		if (c->gYt)
+			cudaFree(c->gYt);
+		if (c->gYs)
+			cudaFree(c->gYs);
+		c->gX = c->gYt = c->gYs = NULL;
+		CK(dalloc(&c->gX, (size_t)kGuessCin * plane));
+		CK(dalloc(&c->gYt, (size_t)kGuessCout * plane));
+		CK(dalloc(&c->gYs, (size_t)kGuessCout * plane));
+	}
+	if (mode == MCLG_GUESS_LEARNED || mode == MCLG_GUESS_FORCED) {
+		rc = cnn_work_ensure(net, c->gw, 1, grid + 1, grid + 1);
+		if (rc)
+			return rc;
+	}
+	c->gmode = mode;
+	c->gnet = (mode == MCLG_GUESS_LEARNED || mode == MCLG_GUESS_FORCED) ? net : NULL;
+	c->gs = N0 / grid;
+	c->gnc = grid;
+	c->goff = c->gbad = 0;
+	c->git_prev = -1;
+	return MCLG_OK;
+}
+
+extern "C" int mclg_guess_sample(mclg_ctx *c, float *x, size_t nx, float *y, size_t ny)
+{
+	if (c == NULL || x == NULL || y == NULL)
+		return MCLG_BAD_INPUT;
+	const size_t plane = (size_t)(c->gnc + 1) * (c->gnc + 1);
+	if (c->gmode == MCLG_GUESS_OFF || !c->gsample) {
+		mclg_set_error("no guess sample: the last solve did not follow two earlier solves with the guess on");
+		return MCLG_BAD_INPUT;
+	}
+	if (nx != kGuessCin * plane || ny != kGuessCout * plane) {
+		mclg_set_error("sample buffers have %zu and %zu entries, need %zu and %zu", nx, ny, kGuessCin * plane,
+		               kGuessCout * plane);
+		return MCLG_BAD_INPUT;
+	}
+	CK(cudaMemcpyAsync(x, c->gX, nx * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(y, c->gYt, ny * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
 	return MCLG_OK;
 }

@@ -215,6 +215,8 @@ void mclg_config_defaults(mclg_config *c)
 	c->max_inner = 200;
 	c->mg_eta_avg = 2;
 	c->mg_block_n = 8;
+	c->guess_smooth = 2;
+	c->stokes_method = 0;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -305,6 +307,8 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_int(&pl, "max_inner", &c->max_inner, 200);
 	get_int(&pl, "mg_eta_avg", &c->mg_eta_avg, 2);
 	get_int(&pl, "mg_block_n", &c->mg_block_n, 8);
+	get_int(&pl, "guess_smooth", &c->guess_smooth, 2);
+	get_int(&pl, "stokes_method", &c->stokes_method, 0);
 	free(pl.e);
 	return MCLG_OK;
 }

@@ -181,3 +181,15 @@ def test_output_rejects_wrong_lengths(tmp_path):
     with pytest.raises(MclgError) as e:
         m.write_output(str(tmp_path), 0, z, z, z, z, z)
     assert e.value.status == api.BAD_INPUT
+
+
+def test_cnn_create_without_device_reports_no_device():
+    L = api.lib()
+    h = C.c_void_p()
+    rc = L.mclg_cnn_create(C.byref(h), 8, 32, 6, 3, 0)
+    if rc == api.OK:
+        L.mclg_cnn_destroy(h)
+        pytest.skip("a CUDA device is visible")
+    assert rc == api.NO_DEVICE
+    assert L.mclg_cnn_create(C.byref(h), 8, 32, 1, 3, 0) == api.BAD_INPUT   # depth < 2
+    assert L.mclg_cnn_load(C.byref(h), b"/nonexistent/net.bin") == api.IO_ERROR
