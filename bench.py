@@ -63,6 +63,15 @@ WORKLOADS = {
         "mesh": "64x64",
     },
 }
+WORKLOADS["cfg4_ensemble_256"] = {
+    "input": "mantle_convection_lab_gb300/configs/cfg3_mg_1024.input",
+    "kind": "ensemble",
+    "desc": "configuration 4: 256 independent models, elements per side from {32,64,128,256}, Ra log-uniform "
+            "[1e5,1e7], viscosity contrast log-uniform [1,1e4], seeded perturbations, uniform meshes; mixed "
+            "precision, every model to Stokes residual < 1e-8 every step; one batched solver launch per step",
+    "mesh": "256 models, 32^2..256^2",
+}
+ENSEMBLE_METRIC = "aggregate model-steps/s at Stokes residual 1e-8"
 DEFAULT_WORKLOAD = "cfg3_mg_1024"
 GUESS_NET = os.path.join(ROOT, "mantle_convection_lab_gb300", "weights", "guess_cfg3.bin")
 GUESS_GRID = 128
@@ -230,11 +239,47 @@ def cpu_sample(wl, threads, steps=None):
                                      f"per-step budget of {budget} CG iterations (max_citcom_cycle x max_cg_cycle)")
 
 
+def ensemble_cpu_sample():
+    """The reference's algorithm on one 32x32 member (1 core, a few steps),
+    extrapolated to the whole 256-member mix with a per-step cost growing as
+    (N/32)^3 (Jacobi-PCG iterations grow like N, work per iteration like N^2)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_port
+    from mantle_convection_lab_gb300 import ensemble
+    params = ensemble.draw(256, 4)
+    small = next(p for p in params if p[0] == 32)
+    cfg = ensemble.member_config(*small)
+    cfg.precision = 0
+    cfg.warm_start = 0
+    cfg.max_citcom_cycle, cfg.max_cg_cycle, cfg.accuracy, cfg.citcom_solver_accu = 2000, 2000, 1e-8, 1e-8
+    o = oracle_port.Oracle(cfg, threads=1)
+    o.step()
+    n = 3
+    t0 = time.perf_counter()
+    for _ in range(n):
+        o.step()
+    t32 = (time.perf_counter() - t0) / n
+    o.close()
+    total = sum(t32 * (p[0] / 32) ** 3 for p in params)
+    return 256 / total, 1, (f"{n} steps of a 32x32 member on 1 core ({1e3 * t32:.0f} ms/step), extrapolated to the "
+                            f"256-member mix as (N/32)^3 per member")
+
+
 def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
+    if wl["kind"] == "ensemble":
+        v, cores, sample = ensemble_cpu_sample()
+        line = {"metric": ENSEMBLE_METRIC, "impl": "reference", "value": v, "unit": "model-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 256e3 / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded members)",
+                "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"]},
+                "cpu_baseline": {"value": v, "unit": "model-steps/s", "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": "model-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
     if wl["kind"] == "replica":
         steps = max(1, args.steps)
         o = _oracle(wl["input"], 1)
@@ -289,9 +334,81 @@ def attach_guess(model, wl, args):
     return net
 
 
+def run_ensemble(args, wl):
+    import torch
+    from mantle_convection_lab_gb300 import ensemble
+
+    rank, world, local_rank = dist_env()
+    dist = init_dist(world, local_rank)
+    torch.cuda.set_device(local_rank)
+    e = ensemble.make(256, seed=4)
+    n = e.n
+    for _ in range(max(args.warmup, 0)):
+        e.step()
+    sampler = ClockSampler() if rank == 0 else None
+    if sampler:
+        sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms, ms_solver, launches, res, inner = 0.0, 0.0, 0, 0.0, 0
+    grids = []
+    for _ in range(args.steps):
+        st = e.step()
+        ms += st[0].ms_total
+        ms_solver += st[0].solver_kernel_ms
+        launches += st[0].kernel_launches
+        res = max(res, max(max(s.res_momentum, s.res_continuity) for s in st))
+        inner += sum(s.cg_cycles for s in st)
+        assert all(s.status == 0 for s in st), [s.status for s in st]
+        grids.append(e.grid_used)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop() if sampler else None
+    value = job_throughput(dist, n * args.steps, ms / 1e3)
+    # end to end: the same steps with every member's temperature read back to the host
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        e.step()
+        for m in e.members:
+            d2h += 8 * m.get("T").size
+    e2e = job_throughput(dist, n * args.steps, time.perf_counter() - t0)
+    sizes = [p[0] for p in ensemble.draw(256, 4)]
+    # algorithmic bytes of the batched solver launch: the per-model MINRES model, summed
+    line = {
+        "metric": ENSEMBLE_METRIC, "value": value, "unit": "model-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic (seeded members)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
+                   "members_by_size": {str(k): sizes.count(k) for k in ensemble.SIZES},
+                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (256 models)",
+                   "solver_ms_per_step": ms_solver / args.steps, "batch_grid": grids,
+                   "inner_per_model_step": inner / (n * args.steps), "max_stokes_residual": res},
+        "e2e": {"value": e2e, "unit": "model-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h // max(args.steps, 1)},
+        "gpu_launches": launches,
+        "roofline": None,
+        "clocks": clocks,
+    }
+    e.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = ensemble_cpu_sample()
+        line["cpu_baseline"] = {"value": v, "unit": "model-steps/s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_gpu(args, wl):
     import torch
     from mantle_convection_lab_gb300 import Config, Model
+
+    if wl["kind"] == "ensemble":
+        return run_ensemble(args, wl)
 
     rank, world, local_rank = dist_env()
     dist = init_dist(world, local_rank)

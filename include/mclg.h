@@ -245,6 +245,29 @@ int mclg_stokes_GT(mclg_ctx *ctx, int lev, const double *x, double *p);       /*
 enum { MCLG_HEAT_K = 0, MCLG_HEAT_C = 1 };
 int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /* K_prod_d_heat, Update_temperature.c:935-962 */
 
+/* ---- batched ensembles (no reference counterpart) ------------------------
+ * n independent models, each built from its own configuration (converged
+ * solvers on uniform meshes, all with the same precision and element aspect
+ * ratio), stepped together on one stream: per step the members' element
+ * kernels, ONE launch of the batched converged solver (each thread block
+ * solves one model; blocks take models from a queue ordered largest first),
+ * then the members' stress and heat kernels.  The batch launch's grid (1 or
+ * 2 blocks per SM) is chosen by timing both on the first two steps that start
+ * from an extrapolated guess.  Results per member equal those of the member
+ * stepped alone up to summation order (the batched solve reduces within a
+ * block instead of over the grid). */
+typedef struct mclg_ensemble mclg_ensemble;
+int mclg_ensemble_create(mclg_ensemble **e, const mclg_config *cfgs, int n);
+void mclg_ensemble_destroy(mclg_ensemble *e);
+int mclg_ensemble_size(const mclg_ensemble *e);
+/* Member i as a context (fields, mesh, single operators); owned by the ensemble. */
+int mclg_ensemble_member(mclg_ensemble *e, int i, mclg_ctx **ctx);
+int mclg_ensemble_initial_temperature(mclg_ensemble *e);
+/* One time step of every member; stats (optional) has n entries, grid_used
+ * (optional) receives the blocks of this step's batched launch.  ms_total and
+ * solver_kernel_ms are the whole batch's. */
+int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *stats, int *grid_used);
+
 /* ---- learned initial guess (no reference counterpart) -------------------
  * A fully convolutional network of `depth` 3x3 convolution layers (ReLU
  * between them, `width` channels) with BF16 weights and FP32 accumulation,

@@ -141,6 +141,10 @@ def lib():
                                      C.c_ulonglong, fp]),
         "mclg_cnn_save": (C.c_int, [vp, C.c_char_p]), "mclg_cnn_load": (C.c_int, [C.POINTER(vp), C.c_char_p]),
         "mclg_guess_set": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
+        "mclg_ensemble_size": (C.c_int, [vp]), "mclg_ensemble_member": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+        "mclg_ensemble_initial_temperature": (C.c_int, [vp]),
+        "mclg_ensemble_step": (C.c_int, [vp, vp, ip]),
         "mclg_guess_sample": (C.c_int, [vp, fp, sz, fp, sz]),
     }
     for name, (res, args) in sig.items():
@@ -304,18 +308,22 @@ class Mesh:
 class Model:
     """One device-resident model; method names follow the reference's calls."""
 
-    def __init__(self, config):
+    def __init__(self, config, _handle=None):
         self.config = config
         self._c = C.c_void_p()
-        _check(lib().mclg_create(C.byref(self._c), C.byref(config)), "create")
+        self._owned = _handle is None
+        if _handle is None:
+            _check(lib().mclg_create(C.byref(self._c), C.byref(config)), "create")
+        else:
+            self._c = _handle
         s = self.mesh("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
         self.timestep = 0
 
     def close(self):
-        if self._c:
+        if self._c and self._owned:
             lib().mclg_destroy(self._c)
-            self._c = C.c_void_p()
+        self._c = C.c_void_p()
 
     __del__ = close
 
@@ -440,3 +448,49 @@ class Model:
         y = np.zeros(self.heat_neq)
         _check(lib().mclg_heat_matvec(self._c, {"K": 0, "C": 1}[which], _dptr(x), _dptr(y)), "heat_matvec")
         return y
+
+
+class Ensemble:
+    """Independent models stepped together: one batched solver launch per step
+    (mclg_ensemble_*).  Members are converged-solver models on uniform meshes."""
+
+    def __init__(self, configs):
+        arr = (Config * len(configs))(*configs)
+        self._e = C.c_void_p()
+        _check(lib().mclg_ensemble_create(C.byref(self._e), arr, len(configs)), "ensemble_create")
+        self.n = len(configs)
+        self.members = []
+        for i in range(self.n):
+            h = C.c_void_p()
+            _check(lib().mclg_ensemble_member(self._e, i, C.byref(h)), "ensemble_member")
+            self.members.append(Model(configs[i], _handle=h))
+        self.grid_used = 0
+
+    def close(self):
+        if self._e:
+            for m in self.members:
+                m.close()
+            lib().mclg_ensemble_destroy(self._e)
+            self._e = C.c_void_p()
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def initial_temperature(self):
+        _check(lib().mclg_ensemble_initial_temperature(self._e), "ensemble_initial_temperature")
+        for m in self.members:
+            m.timestep = 0
+
+    def step(self):
+        stats = (StepStats * self.n)()
+        g = C.c_int()
+        _check(lib().mclg_ensemble_step(self._e, stats, C.byref(g)), "ensemble_step")
+        self.grid_used = g.value
+        for m in self.members:
+            m.timestep += 1
+        return list(stats)

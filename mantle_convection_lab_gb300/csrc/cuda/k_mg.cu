@@ -62,11 +62,38 @@ void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st)
 	cudaMemcpyToSymbolAsync(cTf, &f, sizeof f, 0, cudaMemcpyHostToDevice, st);
 }
 
+// ---- where a solve runs ---------------------------------------------------------
+// grid: one model on the whole cooperative grid (grid barriers and
+// deterministic grid reductions); otherwise one model inside one thread block
+// of a batch (block barriers and reductions, every level block-local).
+struct Sync {
+	cg::grid_group *g;
+	GridRed red;
+	bool grid;
+	int tid, nth;
+	__device__ void sync()
+	{
+		if (grid)
+			g->sync();
+		else
+			__syncthreads();
+	}
+	template <int NV>
+	__device__ void reduce(double (&v)[NV])
+	{
+		if (grid)
+			grid_reduce<NV>(*g, red, v, 0u);
+		else
+			block_reduce<NV>(v, 0u);
+	}
+	__device__ bool leader() const { return !grid || blockIdx.x == 0; }
+};
+
 // ---- small helpers ----------------------------------------------------------
-__device__ __forceinline__ void barrier(cg::grid_group &g, bool grid)
+__device__ __forceinline__ void barrier(Sync &sy, bool grid)
 {
 	if (grid)
-		g.sync();
+		sy.g->sync();
 	else
 		__syncthreads();
 }
@@ -208,7 +235,7 @@ __device__ void jacobi_first(bool grid, int n, const V *b, const V *invD, V *x, 
 // Assemble the coarsest operator densely (FP64), put identity rows on the
 // Dirichlet dofs and invert it by Gauss-Jordan; block 0 only.
 template <class T>
-__device__ void coarse_build(MGHier<T> &H)
+__device__ void coarse_build(const MGHier<T> &H)
 {
 	const MGLevel<T> &L = H.lv[H.nlev - 1];
 	const OpTab<double> &O = tab<double>();
@@ -301,7 +328,7 @@ __device__ void coarse_solve(const MGHier<T> &H, V *x)
 // the same buffer bookkeeping so that all of them know where each level's
 // result lies; only the active blocks do the work.
 template <class T>
-__device__ void level_down(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, int l,
+__device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
                            const typename V2T<T>::t *rhs0, bool grid, bool active, typename V2T<T>::t **xcur)
 {
 	typedef typename V2T<T>::t V;
@@ -311,18 +338,18 @@ __device__ void level_down(cg::grid_group &g, unsigned char *sm, const MGHier<T>
 	if (H.nu == 1) {
 		if (active) {
 			jacobi_first<T, V>(grid, L.n, b, L.invD, x, H.omega);
-			barrier(g, grid);
+			barrier(sy, grid);
 		}
 	} else {
 		// sweep 1 (from zero) fused into sweep 2
 		if (active) {
 			tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr, XS_ZERO);
-			barrier(g, grid);
+			barrier(sy, grid);
 		}
 		for (int s = 2; s < H.nu; s++) {
 			if (active) {
 				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, xt, PASS_SMOOTH, H.omega, nullptr);
-				barrier(g, grid);
+				barrier(sy, grid);
 			}
 			V *tmp = x;
 			x = xt;
@@ -331,15 +358,15 @@ __device__ void level_down(cg::grid_group &g, unsigned char *sm, const MGHier<T>
 	}
 	if (active) {
 		tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
-		barrier(g, grid);
+		barrier(sy, grid);
 		restrict_res<T, V>(grid, L, H.lv[l + 1]);
-		barrier(g, grid);
+		barrier(sy, grid);
 	}
 	xcur[l] = x;
 }
 
 template <class T>
-__device__ void level_up(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, int l,
+__device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
                          const typename V2T<T>::t *rhs0, typename V2T<T>::t *out0, bool grid, bool active,
                          typename V2T<T>::t **xcur)
 {
@@ -358,7 +385,7 @@ __device__ void level_up(cg::grid_group &g, unsigned char *sm, const MGHier<T> &
 				                XS_PROLONG, xcur[l + 1], C.n);
 			else
 				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr);
-			barrier(g, grid);
+			barrier(sy, grid);
 		}
 		xt = x;
 		x = dst;
@@ -367,37 +394,38 @@ __device__ void level_up(cg::grid_group &g, unsigned char *sm, const MGHier<T> &
 }
 
 template <class T>
-__device__ void vcycle(cg::grid_group &g, unsigned char *sm, const MGHier<T> &H, const typename V2T<T>::t *rhs0,
+__device__ void vcycle(Sync &sy, unsigned char *sm, const MGHier<T> &H, const typename V2T<T>::t *rhs0,
                        typename V2T<T>::t *out0)
 {
 	typedef typename V2T<T>::t V;
 	V *xcur[kMaxLev];
 	const int lc = H.nlev - 1;
-	const int nb = H.nblk < lc ? H.nblk : lc;   // first block-local level; the coarsest always is
-	const bool b0 = blockIdx.x == 0;
+	// first block-local level (the coarsest always is; in a batch all are)
+	const int nb = sy.grid ? (H.nblk < lc ? H.nblk : lc) : 0;
+	const bool b0 = sy.leader();
 	for (int l = 0; l < lc; l++)
-		level_down<T>(g, sm, H, l, rhs0, l < nb, l < nb || b0, xcur);
+		level_down<T>(sy, sm, H, l, rhs0, l < nb, l < nb || b0, xcur);
 	if (b0)
 		coarse_solve<T, V>(H, H.lv[lc].xa);
 	xcur[lc] = H.lv[lc].xa;
 	for (int l = lc - 1; l >= 0; l--) {
 		if (l == nb - 1)
-			g.sync();   // block 0's coarse-level results become visible to every block
-		level_up<T>(g, sm, H, l, rhs0, out0, l < nb, l < nb || b0, xcur);
+			sy.sync();   // block 0's coarse-level results become visible to every block
+		level_up<T>(sy, sm, H, l, rhs0, out0, l < nb, l < nb || b0, xcur);
 	}
 	if (nb == 0)
-		g.sync();
+		sy.sync();
 }
 
 // ---- inner solve: CG preconditioned by one V-cycle, all in T -----------------
 template <class T>
-__device__ int pcg_inner(cg::grid_group &g, unsigned char *sm, GridRed &red, const MGHier<T> &H,
-                         const typename V2T<T>::t *b, typename V2T<T>::t *x, double rtol, int maxit)
+__device__ int pcg_inner(Sync &sy, unsigned char *sm, const MGHier<T> &H, const typename V2T<T>::t *b,
+                         typename V2T<T>::t *x, double rtol, int maxit)
 {
 	typedef typename V2T<T>::t V;
 	const MGLevel<T> &L = H.lv[0];
 	const int nn = L.n * L.n;
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int tid = sy.tid, nth = sy.nth;
 	V *r = H.pr, *z = H.pz, *p = H.pp, *q = H.pq;
 	double bb[1] = {0.0};
 	for (int A = tid; A < nn; A += nth) {
@@ -409,23 +437,23 @@ __device__ int pcg_inner(cg::grid_group &g, unsigned char *sm, GridRed &red, con
 		x[A] = zero;
 		bb[0] += (double)bv.x * bv.x + (double)bv.y * bv.y;
 	}
-	grid_reduce<1>(g, red, bb, 0u);
+	sy.reduce<1>(bb);
 	if (!(bb[0] > 0.0))
 		return 0;
-	vcycle<T>(g, sm, H, r, z);
+	vcycle<T>(sy, sm, H, r, z);
 	double rz[1] = {0.0};
 	for (int A = tid; A < nn; A += nth) {
 		const V rv = r[A], zv = z[A];
 		rz[0] += (double)rv.x * zv.x + (double)rv.y * zv.y;
 		p[A] = zv;
 	}
-	grid_reduce<1>(g, red, rz, 0u);
+	sy.reduce<1>(rz);
 	double rho = rz[0];
 	int it = 0;
 	while (it < maxit) {
 		double pq[1];
-		tile_pass<T, V>(sm, true, L.N, L.mask, L.eta, p, nullptr, nullptr, q, PASS_MATVEC, T(0), pq);
-		grid_reduce<1>(g, red, pq, 0u);
+		tile_pass<T, V>(sm, sy.grid, L.N, L.mask, L.eta, p, nullptr, nullptr, q, PASS_MATVEC, T(0), pq);
+		sy.reduce<1>(pq);
 		const double alpha = rho / pq[0];
 		double rr[1] = {0.0};
 		for (int A = tid; A < nn; A += nth) {
@@ -439,17 +467,17 @@ __device__ int pcg_inner(cg::grid_group &g, unsigned char *sm, GridRed &red, con
 			r[A] = rv;
 			rr[0] += (double)rv.x * rv.x + (double)rv.y * rv.y;
 		}
-		grid_reduce<1>(g, red, rr, 0u);
+		sy.reduce<1>(rr);
 		it++;
 		if (!(rr[0] > rtol * rtol * bb[0]) || !isfinite(alpha))
 			break;
-		vcycle<T>(g, sm, H, r, z);
+		vcycle<T>(sy, sm, H, r, z);
 		double rz2[1] = {0.0};
 		for (int A = tid; A < nn; A += nth) {
 			const V rv = r[A], zv = z[A];
 			rz2[0] += (double)rv.x * zv.x + (double)rv.y * zv.y;
 		}
-		grid_reduce<1>(g, red, rz2, 0u);
+		sy.reduce<1>(rz2);
 		const double beta = rz2[0] / rho;
 		rho = rz2[0];
 		for (int A = tid; A < nn; A += nth) {
@@ -459,9 +487,9 @@ __device__ int pcg_inner(cg::grid_group &g, unsigned char *sm, GridRed &red, con
 			pv.y = zv.y + (T)beta * pv.y;
 			p[A] = pv;
 		}
-		g.sync();
+		sy.sync();
 	}
-	g.sync();
+	sy.sync();
 	return it;
 }
 
@@ -519,15 +547,15 @@ __device__ __forceinline__ double gtmul64_elem(int N0, const unsigned char *mask
 // FP64 residual R = [F - K d - G p ; G^T d] into a.R, a.Rc; rs = {|R_m|^2, |R_c|^2, |F|^2}
 // summed over the grid (every block holds the same values on return).
 template <class TI>
-__device__ void stokes_residual(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
-                                const double2 *d, const double *p, double (&rs)[3])
+__device__ void stokes_residual(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, const double2 *d, const double *p,
+                                double (&rs)[3])
 {
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	const GTab &gt = a.gt;
-	tile_pass<double, double2>(sm, true, N0, a.mask0, a.vis, d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0, nullptr);
+	tile_pass<double, double2>(sm, sy.grid, N0, a.mask0, a.vis, d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0, nullptr);
 	gmul64(N0, a.mask0, gt, p, a.R, tid, nth);
-	g.sync();
+	sy.sync();
 	rs[0] = rs[1] = rs[2] = 0.0;
 	for (int A = tid; A < nn; A += nth) {
 		const double2 f = a.F[A], kd = a.Kd[A], gp = a.R[A];
@@ -542,7 +570,7 @@ __device__ void stokes_residual(const MGArgs<TI> &a, unsigned char *sm, cg::grid
 		a.Rc[morton(ex, ez)] = c;
 		rs[1] += c * c;
 	}
-	grid_reduce<3>(g, red, rs, 0u);
+	sy.reduce<3>(rs);
 }
 
 // (G^T u)_e for a TI velocity field (free dofs only).
@@ -571,12 +599,12 @@ __device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask
 // through the TI hierarchy (z_u stays in TI), the pressure part is divided by
 // BAB.  Returns <z, v> over the grid.
 template <class TI>
-__device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
-                                const double2 *vu, const double *vp, typename V2T<TI>::t *zu, double *zp)
+__device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, const double2 *vu, const double *vp,
+                                typename V2T<TI>::t *zu, double *zp)
 {
 	typedef typename V2T<TI>::t VI;
 	const MGHier<TI> &H = a.H;
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	VI *bI = H.lv[0].b;
 	for (int A = tid; A < nn; A += nth) {
@@ -586,8 +614,8 @@ __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, cg::grid
 		w.y = (TI)v.y;
 		bI[A] = w;
 	}
-	g.sync();
-	vcycle<TI>(g, sm, H, bI, zu);
+	sy.sync();
+	vcycle<TI>(sy, sm, H, bI, zu);
 	double dot[1] = {0.0};
 	for (int A = tid; A < nn; A += nth) {
 		const VI z = zu[A];
@@ -599,7 +627,7 @@ __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, cg::grid
 		zp[e] = z;
 		dot[0] += z * vp[e];
 	}
-	grid_reduce<1>(g, red, dot, 0u);
+	sy.reduce<1>(dot);
 	return dot[0];
 }
 
@@ -612,13 +640,13 @@ __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, cg::grid
 // around this solve restores full accuracy.  Stops when the M^-1-norm of the
 // residual has dropped by rtol.  Returns the iterations.
 template <class TI>
-__device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::grid_group &g, GridRed &red,
-                                 double rtol, int maxit, int *status)
+__device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, double rtol, int maxit,
+                                 int *status)
 {
 	typedef typename V2T<TI>::t VI;
 	const MGHier<TI> &H = a.H;
 	const MGLevel<TI> &L0 = H.lv[0];
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	double2 *vu[2] = {a.mv[0], a.mv[1]}, *wu[2] = {a.mw[0], a.mw[1]};
 	double *vp[2] = {a.mvp[0], a.mvp[1]}, *zp[2] = {a.mzp[0], a.mzp[1]}, *wp[2] = {a.mwp[0], a.mwp[1]};
@@ -639,8 +667,8 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::gri
 		wp[1][e] = 0.0;
 		a.dpv[e] = 0.0;
 	}
-	g.sync();
-	double gam2 = block_precond(a, sm, g, red, vu[0], vp[0], zu[0], zp[0]);
+	sy.sync();
+	double gam2 = block_precond(a, sm, sy, vu[0], vp[0], zu[0], zp[0]);
 	if (!(gam2 > 0.0))
 		return 0;
 	double gam = sqrt(gam2), gam_prev = 1.0;
@@ -649,9 +677,9 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::gri
 	int cv = 0, cw = 0, it = 0;   // index cv: z(j), v(j); 1-cv: v(j-1).  cw: w(j); 1-cw: w(j-1)
 	while (it < maxit) {
 		// A z(j), unscaled (z~ = z / gam): K z_u + G z_p, and G^T z_u per element
-		tile_pass<TI, VI>(sm, true, L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
+		tile_pass<TI, VI>(sm, sy.grid, L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
 		gmul64(N0, a.mask0, gt, zp[cv], a.u1, tid, nth);
-		g.sync();
+		sy.sync();
 		double dl[1] = {0.0};
 		for (int A = tid; A < nn; A += nth) {
 			const VI k = kz[A], z = zu[cv][A];
@@ -667,7 +695,7 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::gri
 			a.Ahp[me] = t;
 			dl[0] += t * zp[cv][me];
 		}
-		grid_reduce<1>(g, red, dl, 0u);
+		sy.reduce<1>(dl);
 		const double delta = dl[0] / (gam * gam);
 		// v(j+1) = A z~ - (delta/gam) v(j) - (gam/gam_prev) v(j-1), into v(j-1)'s buffer
 		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
@@ -677,8 +705,8 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::gri
 		}
 		for (int e = tid; e < ne; e += nth)
 			vp[1 - cv][e] = a.Ahp[e] * ig - dg * vp[cv][e] - gg * vp[1 - cv][e];
-		g.sync();
-		const double gn2 = block_precond(a, sm, g, red, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv]);
+		sy.sync();
+		const double gn2 = block_precond(a, sm, sy, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv]);
 		const double gam_next = sqrt(fmax(gn2, 0.0));
 		// Givens rotations
 		const double a0 = c_cur * delta - c_prev * s_cur * gam;
@@ -726,22 +754,22 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, cg::gri
 		}
 		if (!(fabs(eta) > rtol * eta0) || !(gam > 0.0))
 			break;
-		g.sync();
+		sy.sync();
 	}
-	g.sync();
+	sy.sync();
 	return it;
 }
 
-// ---- the persistent kernel ----------------------------------------------------
+// ---- one converged Stokes solve ----------------------------------------------------
+// The whole solve of one time step: per-step setup of the hierarchy, FP64
+// refinement, correction solves.  Runs on the cooperative grid (one model) or
+// inside one block (one model of a batch), as `sy` says.
 template <class TI>
-__global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
+__device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 {
 	typedef typename V2T<TI>::t VI;
-	cg::grid_group g = cg::this_grid();
-	__shared__ __align__(16) unsigned char sm[kSmemBytes];
-	GridRed red = a.red;
-	MGHier<TI> &H = a.H;
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const MGHier<TI> &H = a.H;
+	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	int *status = &a.sc->status;
 	const GTab &gt = a.gt;
@@ -749,7 +777,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 	// -- per-step setup: viscosity on every level, inverse diagonals, BAB, coarse inverse
 	for (int A = tid; A < nn; A += nth)
 		H.lv[0].eta[A] = (TI)a.vis[A];
-	g.sync();
+	sy.sync();
 	for (int l = 1; l < H.nlev; l++) {
 		const MGLevel<TI> &C = H.lv[l], &F = H.lv[l - 1];
 		for (int A = tid; A < C.n * C.n; A += nth) {
@@ -772,12 +800,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 				C.eta[A] = (TI)(H.eta_avg == 2 ? exp(s) : s);
 			}
 		}
-		g.sync();
+		sy.sync();
 	}
 	for (int l = 0; l < H.nlev; l++)
-		level_invdiag<TI, VI>(true, H.lv[l].N, H.lv[l].mask, H.lv[l].eta, H.lv[l].invD, nullptr);
-	level_invdiag<double, double2>(true, N0, a.mask0, a.vis, a.invD64, a.kdiag64);
-	g.sync();
+		level_invdiag<TI, VI>(sy.grid, H.lv[l].N, H.lv[l].mask, H.lv[l].eta, H.lv[l].invD, nullptr);
+	level_invdiag<double, double2>(sy.grid, N0, a.mask0, a.vis, a.invD64, a.kdiag64);
+	sy.sync();
 	for (int e = tid; e < ne; e += nth) {
 		const int ex = e / N0, ez = e - ex * N0;
 		const int cn[4] = {ez + ex * n0, ez + 1 + ex * n0, ez + 1 + (ex + 1) * n0, ez + (ex + 1) * n0};
@@ -796,9 +824,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 		}
 		a.bab[morton(ex, ez)] = s;
 	}
-	if (blockIdx.x == 0)
+	if (sy.leader())
 		coarse_build<TI>(H);
-	g.sync();
+	sy.sync();
 
 	int refine = 0, outer_total = 0, inner_total = 0, capped = 0;
 	double res_m = 0.0, res_c = 0.0, fnorm = 1.0;
@@ -807,8 +835,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 		// the previous step's solution.  Keep the one with the smaller FP64
 		// residual; a non-finite network guess always loses.
 		double rl[3], rp[3];
-		stokes_residual(a, sm, g, red, a.d, a.p, rl);
-		stokes_residual(a, sm, g, red, a.d_alt, a.p_alt, rp);
+		stokes_residual(a, sm, sy, a.d, a.p, rl);
+		stokes_residual(a, sm, sy, a.d_alt, a.p_alt, rp);
 		const double el = rl[0] + rl[1], ep = rp[0] + rp[1];
 		const bool learned = isfinite(el) && (a.guess_force || el < ep);
 		if (!learned) {
@@ -822,12 +850,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 			a.sc->res_learned = sqrt(el / rl[2]);
 			a.sc->res_prev = sqrt(ep / rp[2]);
 		}
-		g.sync();
+		sy.sync();
 	}
 	while (true) {
 		// -- FP64 residual R = [F - K d - G p ; G^T d]
 		double rs[3];
-		stokes_residual(a, sm, g, red, a.d, a.p, rs);
+		stokes_residual(a, sm, sy, a.d, a.p, rs);
 		fnorm = sqrt(rs[2]);
 		res_m = sqrt(rs[0]) / fnorm;
 		res_c = sqrt(rs[1]) / fnorm;
@@ -851,7 +879,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 			// where MINRES converges fastest; close to it, by what is left to
 			// reach rtol (with a factor 2 margin), but not below outer_rtol.
 			const double prt = res > 1e4 * a.rtol ? 1e-2 : fmax(a.outer_rtol, 0.5 * a.rtol / res);
-			const int it = minres_correction<TI>(a, sm, g, red, prt, a.max_outer, status);
+			const int it = minres_correction<TI>(a, sm, sy, prt, a.max_outer, status);
 			outer_total += it;
 			inner_total += it + 1;
 			for (int A = tid; A < nn; A += nth) {
@@ -863,7 +891,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 			}
 			for (int e = tid; e < ne; e += nth)
 				a.p[e] += a.dpv[e];
-			g.sync();
+			sy.sync();
 			continue;
 		}
 
@@ -876,13 +904,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 			v.y = (TI)r.y;
 			bI[A] = v;
 		}
-		g.sync();
-		inner_total += pcg_inner<TI>(g, sm, red, H, bI, xI, a.inner_rtol, a.max_inner);
+		sy.sync();
+		inner_total += pcg_inner<TI>(sy, sm, H, bI, xI, a.inner_rtol, a.max_inner);
 		for (int A = tid; A < nn; A += nth) {
 			const VI v = xI[A];
 			a.dd[A] = make_double2((double)v.x, (double)v.y);
 		}
-		g.sync();
+		sy.sync();
 		double *r0 = a.r0, *r1 = a.r1, *r2 = a.r2, *z0 = a.z0, *z1 = a.z1, *s1 = a.s1, *s2 = a.s2;
 		double c0[1] = {0.0};
 		for (int e = tid; e < ne; e += nth) {
@@ -893,7 +921,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 			a.dpv[me] = 0.0;
 			c0[0] += v * v;
 		}
-		grid_reduce<1>(g, red, c0, 0u);
+		sy.reduce<1>(c0);
 		const double rnorm0 = sqrt(c0[0]);
 		double rnorm = rnorm0;
 		int cycle = 0;
@@ -906,11 +934,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 				if (cycle > 0)
 					rz[1] += r0[e] * z0[e];
 			}
-			grid_reduce<2>(g, red, rz, 0u);
+			sy.reduce<2>(rz);
 			const double delta = cycle == 0 ? 0.0 : rz[0] / rz[1];
 			for (int e = tid; e < ne; e += nth)
 				s2[e] = cycle == 0 ? z1[e] : z1[e] + delta * s1[e];
-			g.sync();
+			sy.sync();
 			gmul64(N0, a.mask0, gt, s2, a.u1, tid, nth);
 			for (int A = tid; A < nn; A += nth) {
 				const double2 v = a.u1[A];
@@ -919,13 +947,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 				w.y = (TI)v.y;
 				bI[A] = w;
 			}
-			g.sync();
-			inner_total += pcg_inner<TI>(g, sm, red, H, bI, xI, a.inner_rtol, a.max_inner);
+			sy.sync();
+			inner_total += pcg_inner<TI>(sy, sm, H, bI, xI, a.inner_rtol, a.max_inner);
 			for (int A = tid; A < nn; A += nth) {
 				const VI v = xI[A];
 				a.u1[A] = make_double2((double)v.x, (double)v.y);
 			}
-			g.sync();
+			sy.sync();
 			double sa[1] = {0.0};
 			for (int e = tid; e < ne; e += nth) {
 				const int ex = e / N0, ez = e - ex * N0;
@@ -934,7 +962,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 				a.Ahp[me] = t;
 				sa[0] += s2[me] * t;
 			}
-			grid_reduce<1>(g, red, sa, 0u);
+			sy.reduce<1>(sa);
 			const double alpha = rz[0] / sa[0];
 			double rr[1] = {0.0};
 			for (int e = tid; e < ne; e += nth) {
@@ -950,7 +978,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 				v.y -= alpha * u.y;
 				a.dd[A] = v;
 			}
-			grid_reduce<1>(g, red, rr, 0u);
+			sy.reduce<1>(rr);
 			rnorm = sqrt(rr[0]);
 			cycle++;
 			double *sh = s1; s1 = s2; s2 = sh;
@@ -973,7 +1001,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 		}
 		for (int e = tid; e < ne; e += nth)
 			a.p[e] += a.dpv[e];
-		g.sync();
+		sy.sync();
 	}
 	if (capped && tid == 0)
 		atomicOr(status, 1);
@@ -994,6 +1022,53 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 	}
 }
 
+// One model on the whole cooperative grid.
+template <class TI>
+__global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
+{
+	__shared__ __align__(16) unsigned char sm[kSmemBytes];
+	cg::grid_group g = cg::this_grid();
+	Sync sy;
+	sy.g = &g;
+	sy.red = a.red;
+	sy.grid = true;
+	sy.tid = blockIdx.x * blockDim.x + threadIdx.x;
+	sy.nth = gridDim.x * blockDim.x;
+	stokes_solve<TI>(a, sm, sy);
+}
+
+// A batch of independent models: every block takes the next model from the
+// queue (ordered largest first by the host) and solves it alone, with block
+// barriers only, so the launch is an ordinary one and blocks never wait on
+// each other.
+template <class TI>
+__global__ void __launch_bounds__(kBlock, 2) k_stokes_mg_batch(const MGArgs<TI> *models, int nmodels, int *queue)
+{
+	__shared__ __align__(16) unsigned char sm[kSmemBytes];
+	__shared__ int next;
+	for (;;) {
+		if (threadIdx.x == 0)
+			next = atomicAdd(queue, 1);
+		__syncthreads();
+		const int m = next;
+		__syncthreads();
+		if (m >= nmodels)
+			break;
+		Sync sy;
+		sy.g = nullptr;
+		sy.red = models[m].red;
+		sy.grid = false;
+		sy.tid = threadIdx.x;
+		sy.nth = blockDim.x;
+		stokes_solve<TI>(models[m], sm, sy);
+		__syncthreads();
+	}
+}
+
 void *stokes_mg_kernel(int fp64) { return fp64 ? (void *)k_stokes_mg<double> : (void *)k_stokes_mg<float>; }
+void *stokes_mg_batch_kernel(int fp64)
+{
+	return fp64 ? (void *)k_stokes_mg_batch<double> : (void *)k_stokes_mg_batch<float>;
+}
 
 }  // namespace mclg

@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <vector>
 #include "k_mg.cuh"
 #include "cnn.cuh"
@@ -23,6 +24,7 @@ __global__ void k_assemble_stokes(DevLevel L, const double *vis, const double *b
 void upload_shape_tables_mg(const ShapeTables &s, cudaStream_t st);
 void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st);
 void *stokes_mg_kernel(int fp64);
+void *stokes_mg_batch_kernel(int fp64);
 __global__ void k_bab(DevLevel L, const double2 *Kdiag, double *bab);
 __global__ void k_stress_elem(DevLevel L, const double *vis, const double2 *V, double *se);
 __global__ void k_elem_to_node(DevLevel L, const double *pe, double *pn);
@@ -95,6 +97,8 @@ struct mclg_ctx {
 	float *gX, *gYt, *gYs;        // features, target and filter scratch on the coarse node grid
 	CnnWork gw;
 	int goff, gbad;               // steps left with the network off; consecutive steps it did not pay
+	bool g_extrap, g_feat;        // this step's solve started from extrapolation / computed features
+	bool st_borrowed;             // the stream belongs to an ensemble
 	int git_prev;                 // inner iterations of the last step solved from the last solution (-1: none)
 };
 
@@ -408,7 +412,11 @@ static int alloc_history(mclg_ctx *c)
 	return MCLG_OK;
 }
 
-static int launch_stokes_mg(mclg_ctx *c)
+// The converged solve of one step in three parts, so that a batch can run the
+// parts of many models around one launch of the batched kernel:
+// stokes_mg_prepare (warm start, learned guess), the solver kernel,
+// stokes_mg_finish (guess targets, history).
+static int stokes_mg_prepare(mclg_ctx *c)
 {
 	const mclg_config &f = c->cfg;
 	// warm_start: 0 = zero guess; 1 = previous (d, p); 2 = the reference's
@@ -471,14 +479,15 @@ static int launch_stokes_mg(mclg_ctx *c)
 	c->mgd.d_alt = d_alt;
 	c->mgd.p_alt = p_alt;
 	c->mgf.guess_force = c->mgd.guess_force = c->gmode == MCLG_GUESS_FORCED;
-	if (f.precision == 2) {
-		void *args[] = {&c->mgd};
-		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(1), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
-	} else {
-		void *args[] = {&c->mgf};
-		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(0), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
-	}
-	c->launches++;
+	c->g_extrap = extrap;
+	c->g_feat = feat;
+	return MCLG_OK;
+}
+
+static int stokes_mg_finish(mclg_ctx *c)
+{
+	const int N0 = c->mgf.N0 ? c->mgf.N0 : c->mgd.N0;
+	const bool track = c->d_h1 != NULL, extrap = c->g_extrap, feat = c->g_feat;
 	if (track) {
 		if (feat) {
 			// target: the converged solution minus the base guess (extrapolation or the last solution)
@@ -497,6 +506,22 @@ static int launch_stokes_mg(mclg_ctx *c)
 		c->ghist++;
 	}
 	return MCLG_OK;
+}
+
+static int launch_stokes_mg(mclg_ctx *c)
+{
+	int rc = stokes_mg_prepare(c);
+	if (rc)
+		return rc;
+	if (c->cfg.precision == 2) {
+		void *args[] = {&c->mgd};
+		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(1), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
+	} else {
+		void *args[] = {&c->mgf};
+		CK(cudaLaunchCooperativeKernel(stokes_mg_kernel(0), dim3(c->coop_mg), dim3(kBlock), args, 0, c->st));
+	}
+	c->launches++;
+	return stokes_mg_finish(c);
 }
 
 // Switch the network off for 16 steps after 3 consecutive steps on which its
@@ -733,7 +758,7 @@ void mclg_destroy(mclg_ctx *c)
 		if (q)
 			cudaFree(q);
 	cnn_work_free(c->gw);
-	if (c->st)
+	if (c->st && !c->st_borrowed)
 		cudaStreamDestroy(c->st);
 	mclg_mesh_free(&c->mesh);
 	free(c);
@@ -1572,3 +1597,229 @@ extern "C" int mclg_guess_sample(mclg_ctx *c, float *x, size_t nx, float *y, siz
 	CK(cudaStreamSynchronize(c->st));
 	return MCLG_OK;
 }
+
+// ---- batched ensembles ------------------------------------------------------------
+// Many independent models stepped together.  Every member is an ordinary
+// context (own mesh, fields, hierarchy) on the ensemble's one stream; each
+// step runs the members' element kernels, then ONE launch of the batched
+// converged solver for all members (a block per model, taken from a queue
+// ordered by decreasing mesh size), then the members' stress and heat kernels.
+struct mclg_ensemble {
+	int n;
+	mclg_ctx **m;          // members, caller's order
+	int *order;            // queue order: decreasing elements per side
+	cudaStream_t st;
+	cudaEvent_t ev[4];
+	void *dargs;           // device MGArgs<TI>[n], queue order
+	int *queue;            // device work counter
+	int fp64;
+	int grid;              // blocks of the batched launch (chosen by the autotuner)
+	int cand[2];           // autotuner candidates: 1 and 2 blocks per SM
+	float cand_ms[2];
+	long long steps;
+};
+
+extern "C" {
+
+void mclg_ensemble_destroy(mclg_ensemble *e)
+{
+	if (e == NULL)
+		return;
+	if (e->st)
+		cudaStreamSynchronize(e->st);
+	for (int i = 0; i < e->n; i++)
+		if (e->m && e->m[i])
+			mclg_destroy(e->m[i]);
+	free(e->m);
+	free(e->order);
+	if (e->dargs)
+		cudaFree(e->dargs);
+	if (e->queue)
+		cudaFree(e->queue);
+	for (int i = 0; i < 4; i++)
+		if (e->ev[i])
+			cudaEventDestroy(e->ev[i]);
+	if (e->st)
+		cudaStreamDestroy(e->st);
+	free(e);
+}
+
+int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
+{
+	if (out == NULL || cfgs == NULL || n < 1)
+		return MCLG_BAD_INPUT;
+	*out = NULL;
+	for (int i = 0; i < n; i++)
+		if (cfgs[i].precision == 0 || cfgs[i].precision != cfgs[0].precision) {
+			mclg_set_error("ensemble member %d: every member needs the same converged solver (precision=mixed or "
+			               "fp64mg)", i);
+			return MCLG_BAD_INPUT;
+		}
+	mclg_ensemble *e = (mclg_ensemble *)calloc(1, sizeof(mclg_ensemble));
+	if (e == NULL)
+		return MCLG_BAD_INPUT;
+	e->n = n;
+	e->fp64 = cfgs[0].precision == 2;
+	e->m = (mclg_ctx **)calloc((size_t)n, sizeof(mclg_ctx *));
+	e->order = (int *)calloc((size_t)n, sizeof(int));
+#define CKE(call)                                  \
+	do {                                           \
+		cudaError_t e_ = (call);                   \
+		if (e_ != cudaSuccess) {                   \
+			int r_ = cuda_fail(e_, #call);         \
+			mclg_ensemble_destroy(e);              \
+			return r_;                             \
+		}                                          \
+	} while (0)
+	if (e->m == NULL || e->order == NULL) {
+		mclg_ensemble_destroy(e);
+		return MCLG_BAD_INPUT;
+	}
+	for (int i = 0; i < n; i++) {
+		int rc = mclg_create(&e->m[i], &cfgs[i]);
+		if (rc != MCLG_OK) {
+			mclg_ensemble_destroy(e);
+			return rc;
+		}
+	}
+	CKE(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+	for (int i = 0; i < 4; i++)
+		CKE(cudaEventCreate(&e->ev[i]));
+	// one stream for all members; the solver's element tables are shared
+	// constants, so every member must have the same element aspect ratio
+	const double r0 = e->m[0]->mesh.dz[e->m[0]->fl] / e->m[0]->mesh.dx[e->m[0]->fl];
+	for (int i = 0; i < n; i++) {
+		mclg_ctx *c = e->m[i];
+		const double r = c->mesh.dz[c->fl] / c->mesh.dx[c->fl];
+		if (fabs(r - r0) > 1e-12 * r0) {
+			mclg_set_error("ensemble member %d: element aspect ratio %g differs from member 0's %g", i, r, r0);
+			mclg_ensemble_destroy(e);
+			return MCLG_BAD_INPUT;
+		}
+		CKE(cudaStreamSynchronize(c->st));
+		CKE(cudaStreamDestroy(c->st));
+		c->st = e->st;
+		c->st_borrowed = true;
+	}
+	for (int i = 0; i < n; i++)
+		e->order[i] = i;
+	auto N0 = [&](int i) { return e->fp64 ? e->m[i]->mgd.N0 : e->m[i]->mgf.N0; };
+	std::stable_sort(e->order, e->order + n, [&](int a, int b) { return N0(a) > N0(b); });
+	const size_t asz = e->fp64 ? sizeof(MGArgs<double>) : sizeof(MGArgs<float>);
+	std::vector<unsigned char> h(asz * (size_t)n);
+	for (int k = 0; k < n; k++) {
+		mclg_ctx *c = e->m[e->order[k]];
+		if (e->fp64)
+			memcpy(&h[asz * k], &c->mgd, asz);
+		else
+			memcpy(&h[asz * k], &c->mgf, asz);
+	}
+	CKE(cudaMalloc(&e->dargs, asz * (size_t)n));
+	CKE(cudaMemcpyAsync(e->dargs, h.data(), asz * (size_t)n, cudaMemcpyHostToDevice, e->st));
+	CKE(cudaMalloc((void **)&e->queue, sizeof(int)));
+	const int sms = e->m[0]->num_sms;
+	e->cand[0] = sms < n ? sms : n;
+	e->cand[1] = 2 * sms < n ? 2 * sms : n;
+	e->grid = e->cand[1];
+	CKE(cudaStreamSynchronize(e->st));
+#undef CKE
+	*out = e;
+	return MCLG_OK;
+}
+
+int mclg_ensemble_size(const mclg_ensemble *e)
+{
+	return e ? e->n : 0;
+}
+
+int mclg_ensemble_member(mclg_ensemble *e, int i, mclg_ctx **ctx)
+{
+	if (e == NULL || ctx == NULL || i < 0 || i >= e->n)
+		return MCLG_BAD_INPUT;
+	*ctx = e->m[i];
+	return MCLG_OK;
+}
+
+int mclg_ensemble_initial_temperature(mclg_ensemble *e)
+{
+	if (e == NULL)
+		return MCLG_BAD_INPUT;
+	for (int i = 0; i < e->n; i++) {
+		int rc = mclg_initial_temperature(e->m[i]);
+		if (rc)
+			return rc;
+	}
+	return MCLG_OK;
+}
+
+int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
+{
+	if (e == NULL)
+		return MCLG_BAD_INPUT;
+	int rc;
+	long long l0 = 0;
+	for (int i = 0; i < e->n; i++)
+		l0 += e->m[i]->launches;
+	CK(cudaEventRecord(e->ev[0], e->st));
+	for (int i = 0; i < e->n; i++) {
+		mclg_ctx *c = e->m[i];
+		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
+			return rc;
+	}
+	// autotuner: the first two steps with an extrapolated start time one
+	// candidate grid each; later steps use the faster
+	int tune = -1;
+	if (e->steps == 2 || e->steps == 3)
+		tune = (int)(e->steps - 2);
+	const int grid = tune >= 0 ? e->cand[tune] : e->grid;
+	CK(cudaEventRecord(e->ev[1], e->st));
+	CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
+	void *kargs[] = {&e->dargs, &e->n, &e->queue};
+	CK(cudaLaunchKernel(stokes_mg_batch_kernel(e->fp64), dim3(grid), dim3(kBlock), kargs, 0, e->st));
+	CK(cudaEventRecord(e->ev[2], e->st));
+	for (int i = 0; i < e->n; i++) {
+		mclg_ctx *c = e->m[i];
+		if ((rc = stokes_mg_finish(c)) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
+			return rc;
+		CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, e->st));
+	}
+	CK(cudaEventRecord(e->ev[3], e->st));
+	CK(cudaStreamSynchronize(e->st));
+	float ms_total = 0.f, ms_solver = 0.f;
+	cudaEventElapsedTime(&ms_total, e->ev[0], e->ev[3]);
+	cudaEventElapsedTime(&ms_solver, e->ev[1], e->ev[2]);
+	if (tune >= 0) {
+		e->cand_ms[tune] = ms_solver;
+		if (tune == 1)
+			e->grid = e->cand_ms[0] <= e->cand_ms[1] ? e->cand[0] : e->cand[1];
+	}
+	long long l1 = 0;
+	for (int i = 0; i < e->n; i++)
+		l1 += e->m[i]->launches;
+	for (int i = 0; i < e->n; i++) {
+		mclg_ctx *c = e->m[i];
+		if (st) {
+			mclg_step_stats *s = &st[i];
+			memset(s, 0, sizeof *s);
+			fill_stats_stokes(c, s);
+			const StepScalars &h = *c->sc_host;
+			s->heat_cg_cycles = h.heat_cycles;
+			s->dt = h.dt;
+			s->model_time = h.model_time;
+			const int s2 = status_from_bits(h.status);
+			if (s2 != MCLG_OK && s->status == MCLG_OK)
+				s->status = s2;
+			s->ms_total = ms_total;
+			s->solver_kernel_ms = ms_solver;
+			s->solver_kernel_launches = 1;
+			s->kernel_launches = (l1 - l0) + 1;
+		}
+		c->timestep++;
+	}
+	if (grid_used)
+		*grid_used = grid;
+	e->steps++;
+	return MCLG_OK;
+}
+
+}  // extern "C"
