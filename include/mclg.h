@@ -251,11 +251,12 @@ int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /*
  * ratio), stepped together on one stream: per step the members' element
  * kernels, ONE launch of the batched converged solver (each thread block
  * solves one model; blocks take models from a queue ordered largest first),
- * then the members' stress and heat kernels.  The batch launch's grid (1 or
- * 2 blocks per SM) is chosen by timing both on the first two steps that start
- * from an extrapolated guess.  Results per member equal those of the member
- * stepped alone up to summation order (the batched solve reduces within a
- * block instead of over the grid). */
+ * then the members' stress and heat kernels.  In the batch launch a model is
+ * solved by a thread-block cluster (cluster barriers, reductions through
+ * distributed shared memory); the cluster size (1, 2, 4, 8 or, where the
+ * device allows it, 16 blocks) is chosen by an autotuner that times each on
+ * one of steps 2..6 and keeps the cheapest per inner iteration.  Results per member equal those of the member
+ * stepped alone up to summation order. */
 typedef struct mclg_ensemble mclg_ensemble;
 int mclg_ensemble_create(mclg_ensemble **e, const mclg_config *cfgs, int n);
 void mclg_ensemble_destroy(mclg_ensemble *e);
@@ -265,8 +266,9 @@ int mclg_ensemble_member(mclg_ensemble *e, int i, mclg_ctx **ctx);
 int mclg_ensemble_initial_temperature(mclg_ensemble *e);
 /* One time step of every member; stats (optional) has n entries, grid_used
  * (optional) receives the blocks of this step's batched launch.  ms_total and
- * solver_kernel_ms are the whole batch's. */
-int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *stats, int *grid_used);
+ * solver_kernel_ms are the whole batch's.  cluster_used (optional) receives
+ * the cluster size of this step's batched launch. */
+int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *stats, int *cluster_used);
 
 /* ---- learned initial guess (no reference counterpart) -------------------
  * A fully convolutional network of `depth` 3x3 convolution layers (ReLU

@@ -464,7 +464,7 @@ class Ensemble:
             h = C.c_void_p()
             _check(lib().mclg_ensemble_member(self._e, i, C.byref(h)), "ensemble_member")
             self.members.append(Model(configs[i], _handle=h))
-        self.grid_used = 0
+        self.cluster_used = 0
 
     def close(self):
         if self._e:
@@ -490,7 +490,7 @@ class Ensemble:
         stats = (StepStats * self.n)()
         g = C.c_int()
         _check(lib().mclg_ensemble_step(self._e, stats, C.byref(g)), "ensemble_step")
-        self.grid_used = g.value
+        self.cluster_used = g.value
         for m in self.members:
             m.timestep += 1
         return list(stats)

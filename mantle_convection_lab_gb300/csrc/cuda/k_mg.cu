@@ -63,50 +63,78 @@ void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st)
 }
 
 // ---- where a solve runs ---------------------------------------------------------
-// grid: one model on the whole cooperative grid (grid barriers and
-// deterministic grid reductions); otherwise one model inside one thread block
-// of a batch (block barriers and reductions, every level block-local).
+// The team of blocks that solves one model:
+//   SYNC_GRID     the whole cooperative grid (grid barriers, deterministic
+//                 grid reductions through global memory);
+//   SYNC_CLUSTER  one thread-block cluster of a batch (cluster barriers,
+//                 reductions over the blocks' shared memory, read through
+//                 distributed shared memory in rank order);
+//   SYNC_BLOCK    one block of a batch (block barriers and reductions).
+enum { SYNC_GRID = 0, SYNC_CLUSTER = 1, SYNC_BLOCK = 2 };
+
 struct Sync {
+	int mode;
 	cg::grid_group *g;
 	GridRed red;
-	bool grid;
+	double *cpart;               // SYNC_CLUSTER: this block's [2][kRedWidth] partials (shared memory)
+	int cflip;
+	int rank, size;              // this block in the team
 	int tid, nth;
 	__device__ void sync()
 	{
-		if (grid)
+		if (mode == SYNC_GRID)
 			g->sync();
+		else if (mode == SYNC_CLUSTER)
+			cg::this_cluster().sync();
 		else
 			__syncthreads();
 	}
 	template <int NV>
 	__device__ void reduce(double (&v)[NV])
 	{
-		if (grid)
+		if (mode == SYNC_GRID) {
 			grid_reduce<NV>(*g, red, v, 0u);
-		else
+		} else if (mode == SYNC_CLUSTER) {
 			block_reduce<NV>(v, 0u);
+			double *mine = cpart + cflip * kRedWidth;
+			if (threadIdx.x == 0)
+				for (int k = 0; k < NV; k++)
+					mine[k] = v[k];
+			cg::cluster_group cl = cg::this_cluster();
+			cl.sync();
+			double acc[NV];
+			for (int k = 0; k < NV; k++)
+				acc[k] = 0.0;
+			for (int r = 0; r < size; r++) {
+				const double *other = cl.map_shared_rank(mine, r);
+				for (int k = 0; k < NV; k++)
+					acc[k] += other[k];
+			}
+			for (int k = 0; k < NV; k++)
+				v[k] = acc[k];
+			cflip ^= 1;   // the next reduction writes the other buffer (see GridRed)
+		} else {
+			block_reduce<NV>(v, 0u);
+		}
 	}
-	__device__ bool leader() const { return !grid || blockIdx.x == 0; }
+	__device__ bool leader() const { return rank == 0; }
+	// the blocks of a pass: the team for team-wide levels, this block alone otherwise
+	__device__ Part part(bool wide) const { return wide ? Part{rank, size} : Part{0, 1}; }
 };
 
 // ---- small helpers ----------------------------------------------------------
 __device__ __forceinline__ void barrier(Sync &sy, bool grid)
 {
 	if (grid)
-		sy.g->sync();
+		sy.sync();
 	else
 		__syncthreads();
 }
 
-__device__ __forceinline__ void span(bool grid, int &start, int &stride)
+__device__ __forceinline__ void span(Part pt, int &start, int &stride)
 {
-	if (grid) {
-		start = blockIdx.x * blockDim.x + threadIdx.x;
-		stride = gridDim.x * blockDim.x;
-	} else {
-		start = threadIdx.x;
-		stride = blockDim.x;
-	}
+	start = pt.rank * blockDim.x + threadIdx.x;
+	stride = pt.size * blockDim.x;
 }
 
 __device__ __forceinline__ unsigned spread_bits(unsigned v)
@@ -131,12 +159,12 @@ __device__ __forceinline__ int morton(int ex, int ez)
 
 // Inverse diagonal of the level operator (the element diagonals summed).
 template <class T, class V>
-__device__ void level_invdiag(bool grid, int N, const unsigned char *mask, const T *eta, V *invD, double2 *kdiag64)
+__device__ void level_invdiag(Part pt, int N, const unsigned char *mask, const T *eta, V *invD, double2 *kdiag64)
 {
 	const OpTab<T> &O = tab<T>();
 	const int n = N + 1;
 	int i0, st;
-	span(grid, i0, st);
+	span(pt, i0, st);
 	for (int A = i0; A < n * n; A += st) {
 		const int ix = A / n, iz = A - ix * n;
 		T du = 0, dw = 0;
@@ -170,10 +198,10 @@ __device__ void level_invdiag(bool grid, int N, const unsigned char *mask, const
 
 // b_c = P^T r_f over the coarse nodes (full weighting 1, 1/2, 1/4).
 template <class T, class V>
-__device__ void restrict_res(bool grid, const MGLevel<T> &F, const MGLevel<T> &C)
+__device__ void restrict_res(Part pt, const MGLevel<T> &F, const MGLevel<T> &C)
 {
 	int i0, st;
-	span(grid, i0, st);
+	span(pt, i0, st);
 	for (int A = i0; A < C.n * C.n; A += st) {
 		const int cx = A / C.n, cz = A - cx * C.n;
 		T su = 0, sw = 0;
@@ -199,10 +227,10 @@ __device__ void restrict_res(bool grid, const MGLevel<T> &F, const MGLevel<T> &C
 
 // out = x_f + P x_c (bilinear).
 template <class T, class V>
-__device__ void prolong_add(bool grid, const MGLevel<T> &F, const V *xf, V *out, const MGLevel<T> &C, const V *xc)
+__device__ void prolong_add(Part pt, const MGLevel<T> &F, const V *xf, V *out, const MGLevel<T> &C, const V *xc)
 {
 	int i0, st;
-	span(grid, i0, st);
+	span(pt, i0, st);
 	for (int A = i0; A < F.n * F.n; A += st) {
 		const int fx = A / F.n, fz = A - fx * F.n;
 		const int x0 = fx >> 1, z0 = fz >> 1, x1 = (fx + 1) >> 1, z1 = (fz + 1) >> 1;
@@ -218,10 +246,10 @@ __device__ void prolong_add(bool grid, const MGLevel<T> &F, const V *xf, V *out,
 
 // x = omega D^-1 b (first smoothing sweep from a zero guess).
 template <class T, class V>
-__device__ void jacobi_first(bool grid, int n, const V *b, const V *invD, V *x, T omega)
+__device__ void jacobi_first(Part pt, int n, const V *b, const V *invD, V *x, T omega)
 {
 	int i0, st;
-	span(grid, i0, st);
+	span(pt, i0, st);
 	for (int A = i0; A < n * n; A += st) {
 		const V bv = b[A], dv = invD[A];
 		V o;
@@ -337,18 +365,18 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 	V *x = L.xa, *xt = L.xb;
 	if (H.nu == 1) {
 		if (active) {
-			jacobi_first<T, V>(grid, L.n, b, L.invD, x, H.omega);
+			jacobi_first<T, V>(sy.part(grid), L.n, b, L.invD, x, H.omega);
 			barrier(sy, grid);
 		}
 	} else {
 		// sweep 1 (from zero) fused into sweep 2
 		if (active) {
-			tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr, XS_ZERO);
+			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr, XS_ZERO);
 			barrier(sy, grid);
 		}
 		for (int s = 2; s < H.nu; s++) {
 			if (active) {
-				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, xt, PASS_SMOOTH, H.omega, nullptr);
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, xt, PASS_SMOOTH, H.omega, nullptr);
 				barrier(sy, grid);
 			}
 			V *tmp = x;
@@ -357,9 +385,9 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 		}
 	}
 	if (active) {
-		tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
+		tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
 		barrier(sy, grid);
-		restrict_res<T, V>(grid, L, H.lv[l + 1]);
+		restrict_res<T, V>(sy.part(grid), L, H.lv[l + 1]);
 		barrier(sy, grid);
 	}
 	xcur[l] = x;
@@ -381,10 +409,10 @@ __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
 		V *dst = (l == 0 && s == H.nu - 1) ? out0 : xt;
 		if (active) {
 			if (s == 0)
-				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr,
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr,
 				                XS_PROLONG, xcur[l + 1], C.n);
 			else
-				tile_pass<T, V>(sm, grid, L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr);
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr);
 			barrier(sy, grid);
 		}
 		xt = x;
@@ -401,7 +429,7 @@ __device__ void vcycle(Sync &sy, unsigned char *sm, const MGHier<T> &H, const ty
 	V *xcur[kMaxLev];
 	const int lc = H.nlev - 1;
 	// first block-local level (the coarsest always is; in a batch all are)
-	const int nb = sy.grid ? (H.nblk < lc ? H.nblk : lc) : 0;
+	const int nb = sy.size > 1 ? (H.nblk < lc ? H.nblk : lc) : 0;
 	const bool b0 = sy.leader();
 	for (int l = 0; l < lc; l++)
 		level_down<T>(sy, sm, H, l, rhs0, l < nb, l < nb || b0, xcur);
@@ -452,7 +480,7 @@ __device__ int pcg_inner(Sync &sy, unsigned char *sm, const MGHier<T> &H, const 
 	int it = 0;
 	while (it < maxit) {
 		double pq[1];
-		tile_pass<T, V>(sm, sy.grid, L.N, L.mask, L.eta, p, nullptr, nullptr, q, PASS_MATVEC, T(0), pq);
+		tile_pass<T, V>(sm, sy.part(true), L.N, L.mask, L.eta, p, nullptr, nullptr, q, PASS_MATVEC, T(0), pq);
 		sy.reduce<1>(pq);
 		const double alpha = rho / pq[0];
 		double rr[1] = {0.0};
@@ -553,7 +581,7 @@ __device__ void stokes_residual(const MGArgs<TI> &a, unsigned char *sm, Sync &sy
 	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	const GTab &gt = a.gt;
-	tile_pass<double, double2>(sm, sy.grid, N0, a.mask0, a.vis, d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0, nullptr);
+	tile_pass<double, double2>(sm, sy.part(true), N0, a.mask0, a.vis, d, nullptr, nullptr, a.Kd, PASS_MATVEC, 0.0, nullptr);
 	gmul64(N0, a.mask0, gt, p, a.R, tid, nth);
 	sy.sync();
 	rs[0] = rs[1] = rs[2] = 0.0;
@@ -677,7 +705,7 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 	int cv = 0, cw = 0, it = 0;   // index cv: z(j), v(j); 1-cv: v(j-1).  cw: w(j); 1-cw: w(j-1)
 	while (it < maxit) {
 		// A z(j), unscaled (z~ = z / gam): K z_u + G z_p, and G^T z_u per element
-		tile_pass<TI, VI>(sm, sy.grid, L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
+		tile_pass<TI, VI>(sm, sy.part(true), L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
 		gmul64(N0, a.mask0, gt, zp[cv], a.u1, tid, nth);
 		sy.sync();
 		double dl[1] = {0.0};
@@ -803,8 +831,8 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 		sy.sync();
 	}
 	for (int l = 0; l < H.nlev; l++)
-		level_invdiag<TI, VI>(sy.grid, H.lv[l].N, H.lv[l].mask, H.lv[l].eta, H.lv[l].invD, nullptr);
-	level_invdiag<double, double2>(sy.grid, N0, a.mask0, a.vis, a.invD64, a.kdiag64);
+		level_invdiag<TI, VI>(sy.part(true), H.lv[l].N, H.lv[l].mask, H.lv[l].eta, H.lv[l].invD, nullptr);
+	level_invdiag<double, double2>(sy.part(true), N0, a.mask0, a.vis, a.invD64, a.kdiag64);
 	sy.sync();
 	for (int e = tid; e < ne; e += nth) {
 		const int ex = e / N0, ez = e - ex * N0;
@@ -1029,39 +1057,73 @@ __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg(MGArgs<TI> a)
 	__shared__ __align__(16) unsigned char sm[kSmemBytes];
 	cg::grid_group g = cg::this_grid();
 	Sync sy;
+	sy.mode = SYNC_GRID;
 	sy.g = &g;
 	sy.red = a.red;
-	sy.grid = true;
+	sy.cpart = nullptr;
+	sy.cflip = 0;
+	sy.rank = blockIdx.x;
+	sy.size = gridDim.x;
 	sy.tid = blockIdx.x * blockDim.x + threadIdx.x;
 	sy.nth = gridDim.x * blockDim.x;
 	stokes_solve<TI>(a, sm, sy);
 }
 
-// A batch of independent models: every block takes the next model from the
-// queue (ordered largest first by the host) and solves it alone, with block
-// barriers only, so the launch is an ordinary one and blocks never wait on
-// each other.
+// A batch of independent models.  Launched with clusters of `cs` blocks
+// (cs = 1: plain blocks); each cluster takes the next model from the queue
+// (ordered largest first by the host) and solves it alone with cluster
+// barriers, so the launch is an ordinary one and clusters never wait on each
+// other.  The cluster's rank-0 block draws from the queue and every block
+// reads the draw from its shared memory; all blocks of a cluster leave the
+// loop on the same draw.
 template <class TI>
 __global__ void __launch_bounds__(kBlock, 2) k_stokes_mg_batch(const MGArgs<TI> *models, int nmodels, int *queue)
 {
 	__shared__ __align__(16) unsigned char sm[kSmemBytes];
 	__shared__ int next;
+	__shared__ double cpart[2 * kRedWidth];
+	cg::cluster_group cl = cg::this_cluster();
+	const int cs = (int)cl.num_blocks(), rank = (int)cl.block_rank();
 	for (;;) {
-		if (threadIdx.x == 0)
+		if (rank == 0 && threadIdx.x == 0)
 			next = atomicAdd(queue, 1);
-		__syncthreads();
-		const int m = next;
-		__syncthreads();
-		if (m >= nmodels)
-			break;
-		Sync sy;
-		sy.g = nullptr;
-		sy.red = models[m].red;
-		sy.grid = false;
-		sy.tid = threadIdx.x;
-		sy.nth = blockDim.x;
-		stokes_solve<TI>(models[m], sm, sy);
-		__syncthreads();
+		if (cs > 1) {
+			cl.sync();
+			const int m = *cl.map_shared_rank(&next, 0);
+			cl.sync();   // every block has read the draw before the next one
+			if (m >= nmodels)
+				break;
+			Sync sy;
+			sy.mode = SYNC_CLUSTER;
+			sy.g = nullptr;
+			sy.red = models[m].red;
+			sy.cpart = cpart;
+			sy.cflip = 0;
+			sy.rank = rank;
+			sy.size = cs;
+			sy.tid = rank * blockDim.x + threadIdx.x;
+			sy.nth = cs * blockDim.x;
+			stokes_solve<TI>(models[m], sm, sy);
+			cl.sync();   // no block starts the next model (or leaves) while another reads its partials
+		} else {
+			__syncthreads();
+			const int m = next;
+			__syncthreads();
+			if (m >= nmodels)
+				break;
+			Sync sy;
+			sy.mode = SYNC_BLOCK;
+			sy.g = nullptr;
+			sy.red = models[m].red;
+			sy.cpart = nullptr;
+			sy.cflip = 0;
+			sy.rank = 0;
+			sy.size = 1;
+			sy.tid = threadIdx.x;
+			sy.nth = blockDim.x;
+			stokes_solve<TI>(models[m], sm, sy);
+			__syncthreads();
+		}
 	}
 }
 

@@ -6,6 +6,12 @@ namespace mclg {
 
 constexpr int kMaxLev = 14;
 
+// The blocks that share a pass over a level: block `rank` of `size` (the
+// whole grid, a thread-block cluster, or one block alone).
+struct Part {
+	int rank, size;
+};
+
 template <class T> struct V2T;
 template <> struct V2T<float> { typedef float2 t; };
 template <> struct V2T<double> { typedef double2 t; };

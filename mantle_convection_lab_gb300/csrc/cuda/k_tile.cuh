@@ -65,7 +65,7 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 //   SMOOTH: out = x + omega D^-1 (b - A x)
 // x at Dirichlet dofs is read as 0 and out is 0 there.
 template <class T, class V>
-__device__ __noinline__ void tile_pass(unsigned char *smraw, bool grid, int N, const unsigned char *__restrict__ mask,
+__device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, const unsigned char *__restrict__ mask,
                                        const T *__restrict__ eta, const V *__restrict__ x,
                                        const V *__restrict__ b, const V *__restrict__ invD, V *__restrict__ out,
                                        int mode, T omega, double *dot, int xs = XS_PLAIN,
@@ -79,7 +79,7 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, bool grid, int N, c
 	const OpTab<T> &O = tab<T>();
 	const int n = N + 1;
 	const int tz_tiles = (n + TZN - 1) / TZN, tx_tiles = (n + TX - 1) / TX, ntiles = tz_tiles * tx_tiles;
-	const int t0 = grid ? blockIdx.x : 0, ts = grid ? gridDim.x : 1;
+	const int t0 = pt.rank, ts = pt.size;
 	const int lz = threadIdx.x & 31, lx0 = threadIdx.x >> 5;
 	double dacc = 0.0;
 	T pu[PSLOTS], pw[PSLOTS], pe[PSLOTS];

@@ -1613,11 +1613,60 @@ struct mclg_ensemble {
 	void *dargs;           // device MGArgs<TI>[n], queue order
 	int *queue;            // device work counter
 	int fp64;
-	int grid;              // blocks of the batched launch (chosen by the autotuner)
-	int cand[2];           // autotuner candidates: 1 and 2 blocks per SM
-	float cand_ms[2];
+	// autotuner: cluster sizes of the batched launch (blocks that solve one
+	// model together), each timed on one step; the fastest per inner
+	// iteration is kept
+	static const int kCand = 5;
+	int cs_cand[kCand], grid_cand[kCand];
+	float cand_cost[kCand];
+	int cs, grid;          // chosen cluster size and grid
 	long long steps;
 };
+
+static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
+{
+	cudaLaunchConfig_t lc;
+	memset(&lc, 0, sizeof lc);
+	lc.gridDim = dim3(grid);
+	lc.blockDim = dim3(kBlock);
+	lc.stream = e->st;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = cs;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	lc.attrs = at;
+	lc.numAttrs = 1;
+	void *kargs[] = {&e->dargs, &e->n, &e->queue};
+	return cudaLaunchKernelExC(&lc, stokes_mg_batch_kernel(e->fp64), kargs);
+}
+
+// Blocks of a batched launch with clusters of cs: as many clusters as can be
+// resident at once, but no more than there are models.
+static int batch_grid(mclg_ensemble *e, int cs)
+{
+	cudaLaunchConfig_t lc;
+	memset(&lc, 0, sizeof lc);
+	lc.gridDim = dim3(cs);
+	lc.blockDim = dim3(kBlock);
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = cs;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	lc.attrs = at;
+	lc.numAttrs = 1;
+	int nc = 0;
+	if (cudaOccupancyMaxActiveClusters(&nc, stokes_mg_batch_kernel(e->fp64), &lc) != cudaSuccess) {
+		cudaGetLastError();
+		nc = cs <= 8 ? 2 * e->m[0]->num_sms / cs : 0;
+	}
+	if (nc < 1)
+		return 0;
+	if (nc > e->n)
+		nc = e->n;
+	return (nc < 1 ? 1 : nc) * cs;
+}
 
 extern "C" {
 
@@ -1717,10 +1766,21 @@ int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
 	CKE(cudaMalloc(&e->dargs, asz * (size_t)n));
 	CKE(cudaMemcpyAsync(e->dargs, h.data(), asz * (size_t)n, cudaMemcpyHostToDevice, e->st));
 	CKE(cudaMalloc((void **)&e->queue, sizeof(int)));
-	const int sms = e->m[0]->num_sms;
-	e->cand[0] = sms < n ? sms : n;
-	e->cand[1] = 2 * sms < n ? 2 * sms : n;
-	e->grid = e->cand[1];
+	// 16 blocks per cluster is beyond the portable 8: allowed by an opt-in
+	// attribute, dropped from the candidates where the device refuses it
+	const bool allow16 = cudaFuncSetAttribute(stokes_mg_batch_kernel(e->fp64),
+	                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+	cudaGetLastError();
+	for (int k = 0; k < mclg_ensemble::kCand; k++) {
+		e->cs_cand[k] = 1 << k;
+		e->grid_cand[k] = (k < 4 || allow16) ? batch_grid(e, e->cs_cand[k]) : 0;
+		if (e->grid_cand[k] < e->cs_cand[k]) {   // not launchable: fall back to the previous size
+			e->cs_cand[k] = e->cs_cand[k - 1];
+			e->grid_cand[k] = e->grid_cand[k - 1];
+		}
+	}
+	e->cs = 1;
+	e->grid = e->grid_cand[0];
 	CKE(cudaStreamSynchronize(e->st));
 #undef CKE
 	*out = e;
@@ -1766,16 +1826,16 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
 			return rc;
 	}
-	// autotuner: the first two steps with an extrapolated start time one
-	// candidate grid each; later steps use the faster
+	// autotuner: steps 2, 3, ... (the warm start settles after two steps) time one
+	// candidate cluster size each; later steps use the cheapest per inner iteration
 	int tune = -1;
-	if (e->steps == 2 || e->steps == 3)
+	if (e->steps >= 2 && e->steps < 2 + mclg_ensemble::kCand)
 		tune = (int)(e->steps - 2);
-	const int grid = tune >= 0 ? e->cand[tune] : e->grid;
+	const int cs = tune >= 0 ? e->cs_cand[tune] : e->cs;
+	const int grid = tune >= 0 ? e->grid_cand[tune] : e->grid;
 	CK(cudaEventRecord(e->ev[1], e->st));
 	CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
-	void *kargs[] = {&e->dargs, &e->n, &e->queue};
-	CK(cudaLaunchKernel(stokes_mg_batch_kernel(e->fp64), dim3(grid), dim3(kBlock), kargs, 0, e->st));
+	CK(launch_batch(e, cs, grid));
 	CK(cudaEventRecord(e->ev[2], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
@@ -1789,9 +1849,18 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	cudaEventElapsedTime(&ms_total, e->ev[0], e->ev[3]);
 	cudaEventElapsedTime(&ms_solver, e->ev[1], e->ev[2]);
 	if (tune >= 0) {
-		e->cand_ms[tune] = ms_solver;
-		if (tune == 1)
-			e->grid = e->cand_ms[0] <= e->cand_ms[1] ? e->cand[0] : e->cand[1];
+		long long inner = 0;
+		for (int i = 0; i < e->n; i++)
+			inner += e->m[i]->sc_host->cg_cycles;
+		e->cand_cost[tune] = ms_solver / (float)(inner > 0 ? inner : 1);
+		if (tune == mclg_ensemble::kCand - 1) {
+			int best = 0;
+			for (int k = 1; k < mclg_ensemble::kCand; k++)
+				if (e->cand_cost[k] < e->cand_cost[best])
+					best = k;
+			e->cs = e->cs_cand[best];
+			e->grid = e->grid_cand[best];
+		}
 	}
 	long long l1 = 0;
 	for (int i = 0; i < e->n; i++)
@@ -1817,7 +1886,7 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		c->timestep++;
 	}
 	if (grid_used)
-		*grid_used = grid;
+		*grid_used = cs;
 	e->steps++;
 	return MCLG_OK;
 }
