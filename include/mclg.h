@@ -245,6 +245,32 @@ int mclg_stokes_GT(mclg_ctx *ctx, int lev, const double *x, double *p);       /*
 enum { MCLG_HEAT_K = 0, MCLG_HEAT_C = 1 };
 int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /* K_prod_d_heat, Update_temperature.c:935-962 */
 
+/* ---- |grad T| adaptive refinement (no reference counterpart) --------------
+ * The reference refines only by the fixed patterns of initial_refine
+ * (Tree.c:184-300; adaptive_mesh_refine is empty, Tree.c:95-99).  Leaves are
+ * finest-level Morton start codes (Mcode >> 4 of the finest level), sorted,
+ * covering the box.
+ *   mclg_create_leaves   a model on a given leaf set instead of develop_mode;
+ *   mclg_amr_flags       per finest-level element (Morton order): |grad T| at
+ *                        its centre > frac * max over elements (device, IEEE
+ *                        rounding, bit-reproducible on the CPU);
+ *   mclg_amr_remesh      flags -> a new tree (flagged leaves' cells at
+ *                        target_level, the rest at base_level, 2:1 balanced
+ *                        across edges and corners) -> the model rebuilt on it
+ *                        in place, T carried over by bilinear interpolation,
+ *                        time step and model time kept.  Refined meshes run
+ *                        the FP64 replica solver (precision=fp64).
+ * Host-only counterparts for checking the tree and the transfer without a GPU:
+ * mclg_mesh_new_leaves, mclg_mesh_amr_leaves, mclg_mesh_transfer. */
+int mclg_create_leaves(mclg_ctx **ctx, const mclg_config *cfg, const int *leaves, size_t n);
+int mclg_amr_flags(mclg_ctx *ctx, double frac, unsigned char *flags, size_t n, double *gmax);
+int mclg_amr_remesh(mclg_ctx *ctx, double frac, int base_level, int target_level, size_t *nel);
+int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n);
+int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, size_t nflags, int base_level,
+                         int target_level, int *leaves, size_t cap, size_t *n);
+int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_t n_from,
+                       const mclg_mesh_handle *to, double *T_to, size_t n_to);
+
 /* ---- batched ensembles (no reference counterpart) ------------------------
  * n independent models, each built from its own configuration (converged
  * solvers on uniform meshes, all with the same precision and element aspect

@@ -141,6 +141,12 @@ def lib():
                                      C.c_ulonglong, fp]),
         "mclg_cnn_save": (C.c_int, [vp, C.c_char_p]), "mclg_cnn_load": (C.c_int, [C.POINTER(vp), C.c_char_p]),
         "mclg_guess_set": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "mclg_create_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
+        "mclg_amr_flags": (C.c_int, [vp, C.c_double, C.POINTER(C.c_ubyte), sz, dp]),
+        "mclg_amr_remesh": (C.c_int, [vp, C.c_double, C.c_int, C.c_int, C.POINTER(sz)]),
+        "mclg_mesh_new_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
+        "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
+        "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_size": (C.c_int, [vp]), "mclg_ensemble_member": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "mclg_ensemble_initial_temperature": (C.c_int, [vp]),
@@ -252,13 +258,23 @@ class Cnn:
         return trace[:iters]
 
 
-class Mesh:
-    """Host-only mesh of Main.c:33-52 (quadtree, numbering, BC codes, hanging nodes)."""
+def _uptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_ubyte))
 
-    def __init__(self, config):
+
+class Mesh:
+    """Host-only mesh of Main.c:33-52 (quadtree, numbering, BC codes, hanging nodes).
+    leaves: build from finest-level Morton start codes instead of develop_mode."""
+
+    def __init__(self, config, leaves=None):
         self._h = C.c_void_p()
         self.config = config
-        _check(lib().mclg_mesh_new(C.byref(self._h), C.byref(config)), "mesh_new")
+        if leaves is None:
+            _check(lib().mclg_mesh_new(C.byref(self._h), C.byref(config)), "mesh_new")
+        else:
+            lv = np.ascontiguousarray(leaves, np.int32)
+            _check(lib().mclg_mesh_new_leaves(C.byref(self._h), C.byref(config), _iptr(lv), lv.size),
+                   "mesh_new_leaves")
         s = self.get("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
 
@@ -295,6 +311,23 @@ class Mesh:
         _check(lib().mclg_mesh_initial_temperature(self._h, lev, _dptr(out), n), "mesh_initial_temperature")
         return out
 
+    def amr_leaves(self, flags, base_level, target_level):
+        """Leaves of the refined tree for per-element flags of the finest level."""
+        f = np.ascontiguousarray(flags, np.uint8)
+        cap = 1 << (2 * (self.max_level - 1))
+        out = np.zeros(cap, np.int32)
+        n = C.c_size_t()
+        _check(lib().mclg_mesh_amr_leaves(self._h, _uptr(f), f.size, base_level, target_level, _iptr(out), cap,
+                                           C.byref(n)), "mesh_amr_leaves")
+        return out[:n.value].copy()
+
+    def transfer(self, T, to):
+        """T (finest-level nodes of this mesh) interpolated onto `to`'s nodes."""
+        T = np.ascontiguousarray(T, np.float64)
+        out = np.zeros(to.nno)
+        _check(lib().mclg_mesh_transfer(self._h, _dptr(T), T.size, to._h, _dptr(out), out.size), "mesh_transfer")
+        return out
+
     def write_output(self, data_dir, timestep, T, V0, V1, stress, vis):
         """Output.c's text files for host fields of the finest level (G.node order)."""
         f = [np.ascontiguousarray(a, np.float64) for a in (T, V0, V1, stress, vis)]
@@ -308,14 +341,17 @@ class Mesh:
 class Model:
     """One device-resident model; method names follow the reference's calls."""
 
-    def __init__(self, config, _handle=None):
+    def __init__(self, config, _handle=None, leaves=None):
         self.config = config
         self._c = C.c_void_p()
         self._owned = _handle is None
-        if _handle is None:
-            _check(lib().mclg_create(C.byref(self._c), C.byref(config)), "create")
-        else:
+        if _handle is not None:
             self._c = _handle
+        elif leaves is not None:
+            lv = np.ascontiguousarray(leaves, np.int32)
+            _check(lib().mclg_create_leaves(C.byref(self._c), C.byref(config), _iptr(lv), lv.size), "create_leaves")
+        else:
+            _check(lib().mclg_create(C.byref(self._c), C.byref(config)), "create")
         s = self.mesh("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
         self.timestep = 0
@@ -427,6 +463,21 @@ class Model:
         p = np.zeros(self.nel)
         _check(lib().mclg_stokes_GT(self._c, -1, _dptr(x), _dptr(p)), "stokes_GT")
         return p
+
+    def amr_flags(self, frac=0.2):
+        """Per finest-level element: |grad T| > frac * max (device); returns (flags, max)."""
+        f = np.zeros(self.nel, np.uint8)
+        gmax = C.c_double()
+        _check(lib().mclg_amr_flags(self._c, frac, _uptr(f), f.size, C.byref(gmax)), "amr_flags")
+        return f, gmax.value
+
+    def remesh(self, frac, base_level, target_level):
+        """Refine by |grad T| and rebuild the model on the new mesh in place."""
+        n = C.c_size_t()
+        _check(lib().mclg_amr_remesh(self._c, frac, base_level, target_level, C.byref(n)), "amr_remesh")
+        s = self.mesh("sizes")
+        self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
+        return n.value
 
     def guess_set(self, mode, grid=128, net=None):
         """Learned initial guess: GUESS_OFF, GUESS_RECORD (features and targets

@@ -576,7 +576,8 @@ const char *mclg_status_string(int s)
 
 void mclg_destroy(mclg_ctx *c);
 
-int mclg_create(mclg_ctx **out, const mclg_config *cfg)
+// leaves != NULL: the mesh is built from that leaf set instead of develop_mode
+static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves, long nleaves)
 {
 	if (out == NULL || cfg == NULL)
 		return MCLG_BAD_INPUT;
@@ -599,7 +600,7 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
 	c->cfg = *cfg;
-	int rc = mclg_mesh_build(&c->mesh, cfg);
+	int rc = leaves ? mclg_mesh_build_leaves(&c->mesh, cfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, cfg);
 	if (rc != MCLG_OK) {
 		mclg_mesh_free(&c->mesh);
 		free(c);
@@ -725,6 +726,18 @@ int mclg_create(mclg_ctx **out, const mclg_config *cfg)
 	CKD(cudaStreamSynchronize(c->st));
 	return MCLG_OK;
 #undef CKD
+}
+
+int mclg_create(mclg_ctx **out, const mclg_config *cfg)
+{
+	return create_impl(out, cfg, NULL, 0);
+}
+
+int mclg_create_leaves(mclg_ctx **out, const mclg_config *cfg, const int *leaves, size_t n)
+{
+	if (out == NULL || cfg == NULL || leaves == NULL)
+		return MCLG_BAD_INPUT;
+	return create_impl(out, cfg, leaves, (long)n);
 }
 
 void mclg_destroy(mclg_ctx *c)
@@ -1888,6 +1901,102 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	if (grid_used)
 		*grid_used = cs;
 	e->steps++;
+	return MCLG_OK;
+}
+
+}  // extern "C"
+
+// ---- |grad T| adaptive refinement ----------------------------------------------------
+namespace mclg {
+void amr_flags(cudaStream_t st, const DevLevel &L, const double *T, double frac, double *g, unsigned char *flags,
+               double *gmax);
+}
+
+extern "C" {
+
+int mclg_amr_flags(mclg_ctx *c, double frac, unsigned char *flags, size_t n, double *gmax)
+{
+	if (c == NULL || flags == NULL || !(frac >= 0.0))
+		return MCLG_BAD_INPUT;
+	if (n != (size_t)c->L.nel) {
+		mclg_set_error("flag buffer has %zu entries, the mesh %d elements", n, c->L.nel);
+		return MCLG_BAD_INPUT;
+	}
+	double *g = NULL, *dmax = NULL;
+	unsigned char *df = NULL;
+	cudaError_t e = cudaMalloc((void **)&g, (n + 1) * sizeof(double));
+	if (e == cudaSuccess) e = cudaMalloc((void **)&df, n + 1);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&dmax, sizeof(double));
+	if (e == cudaSuccess) {
+		amr_flags(c->st, c->L, c->T, frac, g, df, dmax);
+		c->launches += 2;
+		e = cudaGetLastError();
+	}
+	double hm = 0.0;
+	if (e == cudaSuccess) e = cudaMemcpyAsync(flags, df, n, cudaMemcpyDeviceToHost, c->st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&hm, dmax, sizeof(double), cudaMemcpyDeviceToHost, c->st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+	cudaFree(g);
+	cudaFree(df);
+	cudaFree(dmax);
+	if (e != cudaSuccess)
+		return cuda_fail(e, "mclg_amr_flags");
+	if (gmax)
+		*gmax = hm;
+	return MCLG_OK;
+}
+
+// Flags on the device, the new tree and the temperature transfer on the host,
+// then the context is rebuilt on the new mesh in place: the handle stays
+// valid, time step and model time carry over, velocity and pressure restart
+// from zero.
+int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, size_t *nel_out)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	const size_t ne = (size_t)c->L.nel, nn = (size_t)c->L.nno;
+	std::vector<unsigned char> flags(ne);
+	int rc = mclg_amr_flags(c, frac, flags.data(), ne, NULL);
+	if (rc)
+		return rc;
+	int *leaves = NULL;
+	long nl = 0;
+	rc = mclg_amr_build_leaves(&c->mesh, flags.data(), base_level, target_level, &leaves, &nl);
+	if (rc)
+		return rc;
+	mclg_config cfg = c->cfg;
+	mclg_ctx *n = NULL;
+	rc = create_impl(&n, &cfg, leaves, nl);
+	free(leaves);
+	if (rc)
+		return rc;
+	std::vector<double> T_old(nn), T_new((size_t)n->L.nno);
+	rc = mclg_get_field(c, MCLG_F_T, -1, T_old.data(), nn);
+	if (rc == MCLG_OK)
+		rc = mclg_amr_transfer(&c->mesh, T_old.data(), &n->mesh, T_new.data());
+	if (rc == MCLG_OK)
+		rc = mclg_set_field(n, MCLG_F_T, -1, T_new.data(), T_new.size());
+	if (rc == MCLG_OK) {
+		cudaError_t e = cudaMemcpyAsync(n->sc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToDevice, n->st);
+		if (e == cudaSuccess)
+			e = cudaStreamSynchronize(n->st);
+		if (e != cudaSuccess)
+			rc = cuda_fail(e, "mclg_amr_remesh");
+	}
+	if (rc) {
+		mclg_destroy(n);
+		return rc;
+	}
+	n->timestep = c->timestep;
+	n->launches = c->launches;
+	// the caller's handle takes the new state; the old state is released
+	mclg_ctx tmp;
+	memcpy(&tmp, c, sizeof tmp);
+	memcpy(c, n, sizeof tmp);
+	memcpy(n, &tmp, sizeof tmp);
+	mclg_destroy(n);
+	if (nel_out)
+		*nel_out = (size_t)c->L.nel;
 	return MCLG_OK;
 }
 

@@ -62,6 +62,13 @@ typedef struct mclg_mesh {
 
 /* Build the mesh the way Main.c:33-52 does on its first step, for one rank. */
 int mclg_mesh_build(mclg_mesh *m, const mclg_config *cfg);
+/* The same mesh stack from a given leaf set (finest-level Morton start codes). */
+int mclg_mesh_build_leaves(mclg_mesh *m, const mclg_config *cfg, const int *leaves, long n);
+/* |grad T| refinement (mclg_amr.c): leaves of a new tree from per-element flags
+ * of the finest level of m; *leaves is malloc'ed. */
+int mclg_amr_build_leaves(const mclg_mesh *m, const unsigned char *flags, int base_level, int target_level,
+                          int **leaves, long *n);
+int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to);
 void mclg_mesh_free(mclg_mesh *m);
 /* Binary search in the sorted node list (node_index, Array_work.c:106-129). */
 int mclg_node_index(const mclg_level *L, int gid);

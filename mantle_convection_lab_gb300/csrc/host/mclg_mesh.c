@@ -504,7 +504,10 @@ oom:
 	return MCLG_BAD_INPUT;
 }
 
-int mclg_mesh_build(mclg_mesh *m, const mclg_config *c)
+/* leaves != NULL: the finest-level Morton start codes of a given leaf set
+ * (sorted, covering the domain) replace initial_refine; the last leaf's level
+ * then comes from the codes left to the end of the domain. */
+static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves, long nleaves)
 {
 	int lev, fl, rc;
 	ivec head = {0};
@@ -540,7 +543,23 @@ int mclg_mesh_build(mclg_mesh *m, const mclg_config *c)
 	/* build_quad_tree (Tree.c:67-93) */
 	t.out = &head;
 	t.fine_nel = m->max_nel[fl];
-	rc = initial_refine(&t, &head, c->develop_mode, m->max_level);
+	if (leaves != NULL) {
+		long i;
+		for (i = 0; i < nleaves; i++) {
+			if (leaves[i] < 0 || leaves[i] >= m->max_nel[fl] || (i > 0 && leaves[i] <= leaves[i - 1])) {
+				free(head.a);
+				mclg_set_error("leaf %ld: codes must increase within [0, %d)", i, m->max_nel[fl]);
+				return MCLG_BAD_INPUT;
+			}
+			if (ivec_push(&head, leaves[i]) != 0) {
+				free(head.a);
+				return MCLG_BAD_INPUT;
+			}
+		}
+		rc = MCLG_OK;
+	} else {
+		rc = initial_refine(&t, &head, c->develop_mode, m->max_level);
+	}
 	if (rc != MCLG_OK) {
 		free(head.a);
 		return rc;
@@ -559,8 +578,11 @@ int mclg_mesh_build(mclg_mesh *m, const mclg_config *c)
 		for (e = 0; e < n - 1; e++)
 			L->Mcode[e] = (L->Mcode[e] << MCLG_LEVEL_BITS) | log4i(m->max_nel[fl] / (L->Mcode[e + 1] - L->Mcode[e]));
 		e = n - 1;
-		L->Mcode[e] = (L->Mcode[e] << MCLG_LEVEL_BITS)
-		            | log4i(m->max_nel[fl] / (L->Mcode[e] - (L->Mcode[e - 1] >> MCLG_LEVEL_BITS)));
+		if (leaves != NULL)
+			L->Mcode[e] = (L->Mcode[e] << MCLG_LEVEL_BITS) | log4i(m->max_nel[fl] / (m->max_nel[fl] - L->Mcode[e]));
+		else
+			L->Mcode[e] = (L->Mcode[e] << MCLG_LEVEL_BITS)
+			            | log4i(m->max_nel[fl] / (L->Mcode[e] - (L->Mcode[e - 1] >> MCLG_LEVEL_BITS)));
 	}
 	/* project_Mcode (Tree.c:361-389) down to mg_min_level */
 	for (lev = fl; lev > m->min_level; lev--) {
@@ -591,6 +613,21 @@ int mclg_mesh_build(mclg_mesh *m, const mclg_config *c)
 		m->uniform = (L->nel == m->max_nel[fl] && L->nh == 0);
 	}
 	return MCLG_OK;
+}
+
+int mclg_mesh_build(mclg_mesh *m, const mclg_config *c)
+{
+	return mesh_build_impl(m, c, NULL, 0);
+}
+
+int mclg_mesh_build_leaves(mclg_mesh *m, const mclg_config *c, const int *leaves, long n)
+{
+	if (leaves == NULL || n < 2) {
+		memset(m, 0, sizeof *m);
+		mclg_set_error("a leaf list needs at least 2 leaves");
+		return MCLG_BAD_INPUT;
+	}
+	return mesh_build_impl(m, c, leaves, n);
 }
 
 void mclg_mesh_free(mclg_mesh *m)

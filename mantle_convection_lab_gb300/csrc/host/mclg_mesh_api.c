@@ -11,7 +11,7 @@ struct mclg_mesh_handle {
 	mclg_config cfg;
 };
 
-int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg)
+static int mesh_new(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, long n)
 {
 	int rc;
 	mclg_mesh_handle *p;
@@ -22,7 +22,7 @@ int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg)
 	if (p == NULL)
 		return MCLG_BAD_INPUT;
 	p->cfg = *cfg;
-	rc = mclg_mesh_build(&p->mesh, cfg);
+	rc = leaves ? mclg_mesh_build_leaves(&p->mesh, cfg, leaves, n) : mclg_mesh_build(&p->mesh, cfg);
 	if (rc != MCLG_OK) {
 		mclg_mesh_free(&p->mesh);
 		free(p);
@@ -30,6 +30,18 @@ int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg)
 	}
 	*h = p;
 	return MCLG_OK;
+}
+
+int mclg_mesh_new(mclg_mesh_handle **h, const mclg_config *cfg)
+{
+	return mesh_new(h, cfg, NULL, 0);
+}
+
+int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n)
+{
+	if (leaves == NULL)
+		return MCLG_BAD_INPUT;
+	return mesh_new(h, cfg, leaves, (long)n);
 }
 
 void mclg_mesh_delete(mclg_mesh_handle *h)
@@ -188,4 +200,44 @@ int mclg_mesh_write_output(const mclg_mesh_handle *h, const char *data_dir, int 
 		return MCLG_BAD_INPUT;
 	}
 	return mclg_write_output(data_dir ? data_dir : h->cfg.data_dir, timestep, L, T, V0, V1, stress, vis);
+}
+
+int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, size_t nflags, int base_level,
+                         int target_level, int *leaves, size_t cap, size_t *n)
+{
+	int *tmp = NULL;
+	long cnt = 0;
+	int rc;
+	if (h == NULL || flags == NULL || leaves == NULL || n == NULL)
+		return MCLG_BAD_INPUT;
+	if (nflags != (size_t)h->mesh.lev[h->mesh.max_level - 1].nel) {
+		mclg_set_error("flag buffer has %zu entries, the mesh %d elements", nflags,
+		               h->mesh.lev[h->mesh.max_level - 1].nel);
+		return MCLG_BAD_INPUT;
+	}
+	rc = mclg_amr_build_leaves(&h->mesh, flags, base_level, target_level, &tmp, &cnt);
+	if (rc)
+		return rc;
+	*n = (size_t)cnt;
+	if ((size_t)cnt > cap) {
+		free(tmp);
+		mclg_set_error("the refined tree has %ld leaves, the buffer holds %zu", cnt, cap);
+		return MCLG_BAD_INPUT;
+	}
+	memcpy(leaves, tmp, (size_t)cnt * sizeof(int));
+	free(tmp);
+	return MCLG_OK;
+}
+
+int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_t n_from,
+                       const mclg_mesh_handle *to, double *T_to, size_t n_to)
+{
+	if (from == NULL || to == NULL || T_from == NULL || T_to == NULL)
+		return MCLG_BAD_INPUT;
+	if (n_from != (size_t)from->mesh.lev[from->mesh.max_level - 1].nno ||
+	    n_to != (size_t)to->mesh.lev[to->mesh.max_level - 1].nno) {
+		mclg_set_error("field buffers do not match the meshes' node counts");
+		return MCLG_BAD_INPUT;
+	}
+	return mclg_amr_transfer(&from->mesh, T_from, &to->mesh, T_to);
 }

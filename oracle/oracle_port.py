@@ -56,14 +56,15 @@ def _p(a):
 
 
 class Oracle:
-    """One CPU model built from a .input file (or a Config) and the engine's host mesh."""
+    """One CPU model built from a .input file (or a Config) and the engine's host
+    mesh (from develop_mode, or from a leaf list)."""
 
-    def __init__(self, cfg, threads=1):
+    def __init__(self, cfg, threads=1, leaves=None):
         from mantle_convection_lab_gb300.api import Config, Mesh
         if isinstance(cfg, (str, os.PathLike)):
             cfg = Config.from_input(cfg)
         self.cfg = cfg
-        m = Mesh(cfg)
+        m = Mesh(cfg, leaves=leaves)
         fl = m.max_level - 1
         nel, nno = m.nel, m.nno
         node = m.get("node")
