@@ -1,0 +1,58 @@
+"""Configuration 2: |grad T| adaptive refinement with periodic remeshing.
+
+    with AmrRun() as run:           # configs/cfg2_amr_128.input
+        for _ in range(200):
+            st = run.step()         # remeshes before every 10th step
+
+The model starts on the uniform 128 x 128 base grid (leaf level 7 of the
+1024 x 1024 finest grid).  Before step 0 and every `remesh_every` steps the
+device flags elements with |grad T| > frac * max, the host builds the new
+2:1-balanced tree (flagged regions at level base + extra) and the model is
+rebuilt on it in place with T carried over (mclg_amr_remesh).
+"""
+import os
+
+import numpy as np
+
+from .api import Config, Model
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CFG2_INPUT = os.path.join(HERE, "configs", "cfg2_amr_128.input")
+
+
+def uniform_leaves(finest_level, base_level):
+    """Leaf start codes of the uniform grid at base_level inside finest_level."""
+    return np.arange(0, 1 << (2 * finest_level), 1 << (2 * (finest_level - base_level)), dtype=np.int32)
+
+
+class AmrRun:
+    def __init__(self, config=None, base_level=7, extra_levels=3, frac=0.2, remesh_every=10):
+        self.config = config if config is not None else Config.from_input(CFG2_INPUT)
+        self.F = self.config.level - 1
+        self.base, self.target = base_level, min(base_level + extra_levels, self.F)
+        self.frac, self.every = frac, remesh_every
+        self.model = Model(self.config, leaves=uniform_leaves(self.F, self.base))
+        self.model.initial_temperature()
+        self.steps = 0
+        self.remeshes = 0
+
+    def remesh(self):
+        n = self.model.remesh(self.frac, self.base, self.target)
+        self.remeshes += 1
+        return n
+
+    def step(self):
+        if self.steps % self.every == 0:
+            self.remesh()
+        st = self.model.step()
+        self.steps += 1
+        return st
+
+    def close(self):
+        self.model.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
