@@ -98,6 +98,17 @@ CASES = {
     "dev14_l7": ("level=7\nmg_min_level=5\nmax_timestep=0\nmax_citcom_cycle=40\ndevelop_mode=14\nRayleigh=1e5\nA=0.0\n"
                  "ic_kind=1\nic_seed=11\nic_noise=1e-4\nT_mantle_perturb=0.01\nT_wave_number=1\n",
                  None, True),
+    # the reference's other inner solvers: multigrid V-cycles with Gauss-Seidel smoothing
+    # (solver="mg") and plain Gauss-Seidel (solver="gs"), uniform 16x16 and a hanging-node mesh
+    "mg_l5": ("level=5\nmg_min_level=2\nmax_timestep=2\ndevelop_mode=0\nRayleigh=1e5\nA=0.0\n"
+              "ic_kind=1\nic_seed=42\nic_noise=1e-4\nT_mantle_perturb=0.01\nT_wave_number=1\n"
+              "solver=\"mg\"\naccuracy=1e-10\nmax_citcom_cycle=400\n", None, True),
+    "gs_l5": ("level=5\nmg_min_level=2\nmax_timestep=1\ndevelop_mode=0\nRayleigh=1e5\nA=0.0\n"
+              "ic_kind=1\nic_seed=42\nic_noise=1e-4\nT_mantle_perturb=0.01\nT_wave_number=1\n"
+              "solver=\"gs\"\naccuracy=1e-10\nmax_citcom_cycle=400\n", None, True),
+    "mg11_l6": ("level=6\nmg_min_level=3\nmax_timestep=0\ndevelop_mode=11\nRayleigh=1e5\nA=0.0\n"
+                "ic_kind=1\nic_seed=7\nic_noise=1e-3\nT_mantle_perturb=0.01\nT_wave_number=1\n"
+                "solver=\"mg\"\naccuracy=1e-10\nmax_citcom_cycle=400\n", None, True),
     # configuration 3 shape at 32x32: tanh layers + seeded modes, viscosity contrast 1e5
     "vc_l6": ("level=6\nmg_min_level=3\nmax_timestep=2\ndevelop_mode=0\nRayleigh=1e6\n"
               "A=11.512925464970229\nic_kind=2\nic_seed=2024\nic_noise=0.0\nic_bl_thickness=0.02\n"
