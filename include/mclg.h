@@ -50,7 +50,7 @@ enum {
  */
 typedef struct mclg_config {
 	char data_dir[256];      /* data_dir (".")                         Input.c:7 */
-	char solver[8];          /* solver: "cg" | "jc" ("jc")             Input.c:10 */
+	char solver[8];          /* solver: "cg" | "jc" | "gs" | "mg" ("jc") Input.c:10 */
 	int level;               /* level: finest level + 1 (1)            Input.c:12 */
 	int mg_min_level;        /* mg_min_level (1)                       Input.c:13 */
 	int nprox, nproz;        /* nprox/nproz: must be 1 on one device   Input.c:20-21 */
@@ -105,6 +105,10 @@ typedef struct mclg_config {
 	int guess_smooth;        /* learned guess: binomial filter passes on the network's output (2) */
 	int stokes_method;       /* converged solvers' correction solve: 0 Uzawa with inner MG-PCG (the
 	                            reference's outer loop), 1 MINRES with a block-diagonal preconditioner (0) */
+	/* the reference's multigrid inner solver, solver="mg" (Solver.c:668-768) */
+	int mg_cycle;            /* V-cycles per inner solve (2)            Input.c:86 */
+	int mg_finest_iteration; /* Gauss-Seidel sweeps before restriction (4)  Input.c:65 */
+	int mg_coarse_iteration; /* Gauss-Seidel sweeps after prolongation (4)  Input.c:64 */
 } mclg_config;
 
 typedef struct mclg_step_stats {
@@ -207,7 +211,17 @@ enum {
 	MCLG_M_LM = 6,       /* [8*nel]    G.lm[lev][d][a][e], (d,a)-major                */
 	MCLG_M_HANG = 7,     /* [3*nh]     hanging node, parent 0, parent 1 (global ids)  */
 	MCLG_M_VBC = 8,      /* [2*nno]    G.bc.v_bc[lev][d] codes ('V','S','N',...)       */
-	MCLG_M_TBC = 9       /* [nno]      G.bc.T_bc[lev] codes                           */
+	MCLG_M_TBC = 9,      /* [nno]      G.bc.T_bc[lev] codes                           */
+	/* the reference's multigrid transfer maps (solver="mg"), equation-indexed: */
+	MCLG_M_INTERP = 10,  /* [5*neq]    lev > mg_min_level: G.interp[lev].local_eq_n, then
+	                                   local_eq[0..3] (equations of lev-1, -1 unused or fixed)
+	                                   Connection.c:708-930 */
+	MCLG_M_PROJECT = 11, /* [neq]      lev < finest: the equation of lev+1 whose residual
+	                                   equation l of lev takes (G.project[lev].local_u), -1 none
+	                                   Connection.c:1051-1250 */
+	MCLG_M_GS_WAVE = 12  /* [nno]      Gauss-Seidel wavefront of each node: nodes of one
+	                                   wavefront share no matrix entry, and sweeping the
+	                                   wavefronts in order reproduces the sequential sweep */
 };
 /* lev < 0 selects the finest level.  n is the caller's buffer length; the
  * call fails with MCLG_BAD_INPUT when it does not match the array size. */

@@ -70,6 +70,12 @@ int mclg_amr_build_leaves(const mclg_mesh *m, const unsigned char *flags, int ba
                           int **leaves, long *n);
 int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to);
 void mclg_mesh_free(mclg_mesh *m);
+/* The reference's multigrid maps and the Gauss-Seidel wavefronts (mclg_refmg.c).
+ * interp: lev in (min_level, max_level); n[neq(lev)], src[4*neq(lev)] (src[i*neq + u]).
+ * project: lev in [min_level, max_level-1); up_eq[neq(lev)].  waves: wave[nno]. */
+int mclg_refmg_interp(const mclg_mesh *m, int lev, int *n, int *src);
+int mclg_refmg_project(const mclg_mesh *m, int lev, int *up_eq);
+int mclg_refmg_waves(const mclg_level *L, int *wave);
 /* Binary search in the sorted node list (node_index, Array_work.c:106-129). */
 int mclg_node_index(const mclg_level *L, int gid);
 

@@ -217,6 +217,9 @@ void mclg_config_defaults(mclg_config *c)
 	c->mg_block_n = 8;
 	c->guess_smooth = 2;
 	c->stokes_method = 0;
+	c->mg_cycle = 2;
+	c->mg_finest_iteration = 4;
+	c->mg_coarse_iteration = 4;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -309,6 +312,10 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_int(&pl, "mg_block_n", &c->mg_block_n, 8);
 	get_int(&pl, "guess_smooth", &c->guess_smooth, 2);
 	get_int(&pl, "stokes_method", &c->stokes_method, 0);
+	/* Input.c:64-65, 86 */
+	get_int(&pl, "mg_cycle", &c->mg_cycle, 2);
+	get_int(&pl, "mg_finest_iteration", &c->mg_finest_iteration, 4);
+	get_int(&pl, "mg_coarse_iteration", &c->mg_coarse_iteration, 4);
 	free(pl.e);
 	return MCLG_OK;
 }

@@ -83,6 +83,9 @@ int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t 
 	case MCLG_M_HANG: need = 3 * (size_t)L->nh; break;
 	case MCLG_M_VBC: need = 2 * nn; break;
 	case MCLG_M_TBC: need = nn; break;
+	case MCLG_M_INTERP: need = 5 * (size_t)L->neq; break;
+	case MCLG_M_PROJECT: need = (size_t)L->neq; break;
+	case MCLG_M_GS_WAVE: need = nn; break;
 	default:
 		mclg_set_error("unknown mesh array %d", which);
 		return MCLG_BAD_INPUT;
@@ -124,6 +127,20 @@ int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t 
 		for (i = 0; i < nn; i++)
 			out[i] = (unsigned char)L->T_bc[i];
 		break;
+	case MCLG_M_INTERP:
+	case MCLG_M_PROJECT: {
+		const int lv = (int)(L - m->lev);
+		const int rc = which == MCLG_M_INTERP ? mclg_refmg_interp(m, lv, out, out + L->neq)
+		                                      : mclg_refmg_project(m, lv, out);
+		if (rc != MCLG_OK) {
+			mclg_set_error("level %d has no %s map (levels %d..%d)", lv,
+			               which == MCLG_M_INTERP ? "interpolation" : "projection", m->min_level,
+			               m->max_level - 1);
+			return rc;
+		}
+		break;
+	}
+	case MCLG_M_GS_WAVE: mclg_refmg_waves(L, out); break;
 	}
 	return MCLG_OK;
 }

@@ -14,6 +14,9 @@
  *   K / F / G assembly      Build_matrix.c:42-381, 720-744
  *   citcom_solver (Uzawa)   Solver.c:14-249, initial_d_p :251-278
  *   Conj_Grad / jacobi      Solver.c:1589-1864, K_prod_d :360-386
+ *   gauss_seidel            Solver.c:1866-1929
+ *   multigrid / MG          Solver.c:668-768, get_residual :1291-1317, project_res
+ *                           :770-832 and interp_error :1009-1143 (the local parts)
  *   G_prod_p / GT_prod_d    Solver.c:569-591, 645-666
  *   enforce_constrain_veq   Solver.c:1368-1482
  *   v_to_nodes, stress      Solver.c:1319-1366, Grain_size_evolution.c:154-213
@@ -44,16 +47,32 @@ typedef struct orc {
 	double *dxh, *dzh, *jac, *area;
 	int *id, *hid, *p2n_cnt, *p2n_el;
 	double Ra, A, refT, lmj, Q, theta, accuracy, citcom_accu, vmin, vmax;
-	int max_citcom, max_cg, precond, check_v_only, solver_jc, zero_P, AMR, auto_acc;
+	int max_citcom, max_cg, precond, check_v_only, solver, zero_P, AMR, auto_acc;
 	double N[4][4], dNdxi[4][4], dNdeta[4][4], dNdxi_c[4], dNdeta_c[4];
 	double *T, *vis, *buoy, *V0, *V1, *stress, *d, *p, *F, *Kdiag;
 	int *Kncol, *Kcol, *Gncol, *Gcol;
 	double *Kval, *Gval;
 	int *HKncol, *HKcol, *HCncol, *HCcol;
-	double *HKval, *HCval, *HF, *tau0, *tau1, *hd;
+	double *HKval, *HCval, *HAval, *HF, *tau0, *tau1, *hd;
 	double dt, model_time, res_m, res_c;
 	int p_init, uzawa_cycles, cg_cycles, heat_cycles;
+	struct orc_mg *mg;   /* solver="mg": the coarser levels and the transfer maps */
 } orc;
+
+/* solver codes (G.solver, Input.c:10) */
+enum { SOLVER_CG = 0, SOLVER_JC = 1, SOLVER_GS = 2, SOLVER_MG = 3 };
+
+/* The multigrid hierarchy of solver="mg": lv[0] is mg_min_level, lv[nlev-1]
+ * the owning (finest) level.  Maps are the reference's, equation-indexed:
+ * itp_n[k] / itp_src[k] (k >= 1) from level k-1 to level k
+ * (G.interp[lev].local_eq_n / local_eq), prj[k] (k < nlev-1) the equation of
+ * level k+1 whose residual equation l of level k takes (G.project). */
+typedef struct orc_mg {
+	int nlev, cycles, fine_it, coarse_it;
+	struct orc *lv[16];
+	int *itp_n[16], *itp_src[16], *prj[16];
+	double *err[16];     /* G.err[lev] */
+} orc_mg;
 
 static void shape_tables(orc *o)
 {
@@ -507,9 +526,122 @@ static int jacobi(orc *o, const double *b, double *x, double accu, int max_cycle
 	return cycle;
 }
 
+/* gauss_seidel, Solver.c:1866-1929: rows in equation order, each from the
+ * newest x, until the largest change is below accu */
+static int gauss_seidel(const orc *o, const double *b, double *x, double accu, int max_cycle)
+{
+	int n = o->neq, i, cycle = 0;
+	double *xt = malloc(sizeof(double) * (size_t)(n + 1)), *prod = malloc(sizeof(double) * (size_t)(n + 1));
+	while (cycle < max_cycle) {
+		double diff = 0.0;
+		for (i = 0; i < n; i++) {
+			xt[i] = x[i];
+			prod[i] = 0.0;
+		}
+		for (i = 0; i < n; i++) {
+			double diag = 1.0;
+			int j;
+			for (j = 0; j < o->Kncol[i]; j++) {
+				int c = o->Kcol[(size_t)i * VCOL + j];
+				if (c != i)
+					prod[i] += o->Kval[(size_t)i * VCOL + j] * x[c];
+				else
+					diag = o->Kval[(size_t)i * VCOL + j];
+			}
+			x[i] = (b[i] - prod[i]) / diag;
+		}
+		cycle++;
+		for (i = 0; i < n; i++)
+			if (fabs(x[i] - xt[i]) > diff)
+				diff = fabs(x[i] - xt[i]);
+		if (diff < accu)
+			break;
+	}
+	free(xt);
+	free(prod);
+	return cycle;
+}
+
+/* get_residual, Solver.c:1291-1317: res = b - K x, column by column */
+static void get_residual(const orc *o, const double *b, const double *x, double *res)
+{
+	int i, j;
+	for (i = 0; i < o->neq; i++)
+		res[i] = b[i];
+	for (i = 0; i < o->neq; i++)
+		for (j = 0; j < o->Kncol[i]; j++)
+			res[i] -= o->Kval[(size_t)i * VCOL + j] * x[o->Kcol[(size_t)i * VCOL + j]];
+}
+
+/* MG, Solver.c:715-768, at hierarchy index k (> 0).  Below the top, x is
+ * err[k] itself, so interp_error overwrites it before x += err[k] doubles it,
+ * as in the reference. */
+static void mg_level(orc_mg *g, int k, const double *b, double *x, double accu)
+{
+	orc *u = g->lv[k], *l = g->lv[k - 1];
+	double *res_u = malloc(sizeof(double) * (size_t)(u->neq + 1));
+	double *res_l = calloc((size_t)l->neq + 1, sizeof(double));
+	double *eu = g->err[k], *el = g->err[k - 1];
+	int i, j;
+	gauss_seidel(u, b, x, accu, g->fine_it);
+	get_residual(u, b, x, res_u);
+	for (i = 0; i < l->neq; i++) /* project_res, :770-783 */
+		if (g->prj[k - 1][i] >= 0)
+			res_l[i] = res_u[g->prj[k - 1][i]];
+	if (k - 1 == 0)
+		gauss_seidel(l, res_l, el, accu, 1000);
+	else
+		mg_level(g, k - 1, res_l, el, accu);
+	for (i = 0; i < u->neq; i++) { /* interp_error, :1029-1046 */
+		const int n = g->itp_n[k][i];
+		if (n <= 0)
+			continue;
+		eu[i] = 0.0;
+		for (j = 0; j < n; j++) {
+			const int s = g->itp_src[k][(size_t)j * u->neq + i];
+			if (s != -1)
+				eu[i] += el[s];
+		}
+		eu[i] /= n;
+	}
+	for (i = 0; i < u->neq; i++)
+		x[i] += eu[i];
+	gauss_seidel(u, b, x, accu, g->coarse_it);
+	free(res_u);
+	free(res_l);
+}
+
+/* multigrid, Solver.c:668-713 */
+static int multigrid(orc *o, const double *b, double *x, double accu)
+{
+	orc_mg *g = o->mg;
+	const int top = g->nlev - 1;
+	int k, i, cycle = 0, conv = 0;
+	double *xt = malloc(sizeof(double) * (size_t)(o->neq + 1));
+	for (k = 0; k < g->nlev; k++)
+		memset(g->err[k], 0, sizeof(double) * (size_t)g->lv[k]->neq);
+	while (!conv && cycle < g->cycles) {
+		double diff = 0.0;
+		memcpy(xt, x, sizeof(double) * (size_t)o->neq);
+		mg_level(g, top, b, x, accu);
+		for (i = 0; i < o->neq; i++) /* check_convergency, :1267-1289 */
+			if (fabs(x[i] - xt[i]) > diff)
+				diff = fabs(x[i] - xt[i]);
+		conv = diff < accu;
+		cycle++;
+	}
+	free(xt);
+	return cycle;
+}
+
 static int inner(orc *o, const double *b, double *x, double accu)
 {
-	return o->solver_jc ? jacobi(o, b, x, accu, 1000) : conj_grad(o, b, x, accu, o->max_cg);
+	switch (o->solver) {
+	case SOLVER_JC: return jacobi(o, b, x, accu, 1000);
+	case SOLVER_GS: return gauss_seidel(o, b, x, accu, 1000);
+	case SOLVER_MG: return multigrid(o, b, x, accu);
+	default: return conj_grad(o, b, x, accu, o->max_cg);
+	}
 }
 
 /* citcom_solver, Solver.c:14-249 */
@@ -799,7 +931,6 @@ static double advection_dt(const orc *o)
 	return (dt < diff) ? dt : diff;
 }
 
-static double *g_HAval;
 
 static void heat_prod(const orc *o, const double *val, const int *col, const int *ncol, int width,
                       const double *x, double *y)
@@ -902,9 +1033,9 @@ static void update_temperature(orc *o)
 	for (i = 0; i < n; i++) {
 		int j;
 		for (j = 0; j < o->HKncol[i]; j++)
-			g_HAval[(size_t)i * TCOL + j] = o->HCval[(size_t)i * TCOL + j] / tdt + o->HKval[(size_t)i * TCOL + j];
+			o->HAval[(size_t)i * TCOL + j] = o->HCval[(size_t)i * TCOL + j] / tdt + o->HKval[(size_t)i * TCOL + j];
 	}
-	o->heat_cycles = conj_grad_heat(o, g_HAval, B, o->hd, 1e-3, 1000);
+	o->heat_cycles = conj_grad_heat(o, o->HAval, B, o->hd, 1e-3, 1000);
 	for (i = 0; i < o->nno; i++)
 		o->T[i] = o->hid[i] >= 0 ? o->hd[o->hid[i]] : o->tbcval[i];
 	free(B);
@@ -928,7 +1059,7 @@ orc *orc_new(int nel, int nno, int gnox, int gnoz, int fine_level, const int *ie
 	o->theta = dparam[5]; o->accuracy = dparam[6]; o->citcom_accu = dparam[7]; o->vmin = dparam[8];
 	o->vmax = dparam[9];
 	o->max_citcom = iparam[0]; o->max_cg = iparam[1]; o->precond = iparam[2]; o->check_v_only = iparam[3];
-	o->solver_jc = iparam[4]; o->zero_P = iparam[5]; o->AMR = iparam[6]; o->auto_acc = iparam[7];
+	o->solver = iparam[4]; o->zero_P = iparam[5]; o->AMR = iparam[6]; o->auto_acc = iparam[7];
 	o->threads = iparam[8] > 0 ? iparam[8] : 1;
 	shape_tables(o);
 	o->dxh = malloc(sizeof(double) * nel); o->dzh = malloc(sizeof(double) * nel);
@@ -968,8 +1099,7 @@ orc *orc_new(int nel, int nno, int gnox, int gnoz, int fine_level, const int *ie
 	o->HKval = calloc((size_t)(o->hneq + 1) * TCOL, sizeof(double)); o->HCval = calloc((size_t)(o->hneq + 1) * TCOL, sizeof(double));
 	o->HF = calloc(o->hneq + 1, sizeof(double)); o->hd = calloc(o->hneq + 1, sizeof(double));
 	o->tau0 = calloc(nel, sizeof(double)); o->tau1 = calloc(nel, sizeof(double));
-	free(g_HAval);
-	g_HAval = calloc((size_t)(o->hneq + 1) * TCOL, sizeof(double));
+	o->HAval = calloc((size_t)(o->hneq + 1) * TCOL, sizeof(double));
 	return o;
 }
 
@@ -977,15 +1107,65 @@ void orc_free(orc *o)
 {
 	if (!o)
 		return;
+	if (o->mg) {
+		int k;
+		for (k = 0; k < o->mg->nlev; k++) {
+			free(o->mg->err[k]); free(o->mg->itp_n[k]); free(o->mg->itp_src[k]); free(o->mg->prj[k]);
+		}
+		free(o->mg);
+	}
 	free(o->dxh); free(o->dzh); free(o->jac); free(o->area); free(o->id); free(o->hid); free(o->p2n_cnt);
 	free(o->p2n_el); free(o->T); free(o->vis); free(o->buoy); free(o->V0); free(o->V1); free(o->stress);
 	free(o->d); free(o->p); free(o->F); free(o->Kdiag); free(o->Kncol); free(o->Gncol); free(o->Kcol);
 	free(o->Gcol); free(o->Kval); free(o->Gval); free(o->HKncol); free(o->HCncol); free(o->HKcol);
-	free(o->HCcol); free(o->HKval); free(o->HCval); free(o->HF); free(o->hd); free(o->tau0); free(o->tau1);
+	free(o->HCcol); free(o->HKval); free(o->HCval); free(o->HAval); free(o->HF); free(o->hd); free(o->tau0); free(o->tau1);
 	free(o);
 }
 
+/* solver="mg": attach the coarser levels (lv[nlev-1] == top) and the maps;
+ * the maps are copied. */
+int orc_mg_attach(orc *top, int nlev, orc **lv, int **itp_n, int **itp_src, int **prj, int cycles, int fine_it,
+                  int coarse_it)
+{
+	orc_mg *g;
+	int k;
+	if (nlev < 2 || nlev > 16 || lv[nlev - 1] != top)
+		return -1;
+	g = calloc(1, sizeof(orc_mg));
+	g->nlev = nlev; g->cycles = cycles; g->fine_it = fine_it; g->coarse_it = coarse_it;
+	for (k = 0; k < nlev; k++) {
+		const size_t n = (size_t)lv[k]->neq + 1;
+		g->lv[k] = lv[k];
+		g->err[k] = calloc(n, sizeof(double));
+		if (k > 0) {
+			g->itp_n[k] = malloc(n * sizeof(int));
+			g->itp_src[k] = malloc(4 * n * sizeof(int));
+			memcpy(g->itp_n[k], itp_n[k], (n - 1) * sizeof(int));
+			memcpy(g->itp_src[k], itp_src[k], 4 * (n - 1) * sizeof(int));
+		}
+		if (k < nlev - 1) {
+			g->prj[k] = malloc(n * sizeof(int));
+			memcpy(g->prj[k], prj[k], (n - 1) * sizeof(int));
+		}
+	}
+	top->mg = g;
+	return 0;
+}
+
 void orc_set_T(orc *o, const double *T) { memcpy(o->T, T, sizeof(double) * (size_t)o->nno); }
+
+/* viscosity and K of the coarser levels (Viscosity.c:8, Build_matrix.c:8 run
+ * over every level); their T stays the initial temperature */
+static void assemble_coarse(orc *o)
+{
+	int k;
+	if (o->mg == NULL)
+		return;
+	for (k = 0; k < o->mg->nlev - 1; k++) {
+		viscosity(o->mg->lv[k]);
+		assemble_stokes(o->mg->lv[k]);
+	}
+}
 
 /* One time step of Main.c:58-64 (no output).  stats: uzawa, cg, heat cycles,
  * dt, model_time, residual momentum, residual continuity. */
@@ -994,6 +1174,7 @@ void orc_step(orc *o, double *stats)
 	buoyancy_force(o);
 	viscosity(o);
 	assemble_stokes(o);
+	assemble_coarse(o);
 	solve_velocity_pressure(o);
 	update_temperature(o);
 	stats[0] = o->uzawa_cycles; stats[1] = o->cg_cycles; stats[2] = o->heat_cycles;
@@ -1006,6 +1187,7 @@ void orc_stokes(orc *o, double *stats)
 	buoyancy_force(o);
 	viscosity(o);
 	assemble_stokes(o);
+	assemble_coarse(o);
 	solve_velocity_pressure(o);
 	stats[0] = o->uzawa_cycles; stats[1] = o->cg_cycles; stats[5] = o->res_m; stats[6] = o->res_c;
 }
@@ -1015,6 +1197,7 @@ void orc_assemble(orc *o)
 	buoyancy_force(o);
 	viscosity(o);
 	assemble_stokes(o);
+	assemble_coarse(o);
 }
 
 /* which: 0 T, 1 V0, 2 V1, 3 P, 4 d, 5 stress, 6 vis, 7 buoyancy, 8 F, 9 Kdiag, 10 tau0, 11 tau1, 12 heat F */

@@ -48,6 +48,8 @@ def lib():
         _L.orc_sizes.argtypes = [vp, vp]
         _L.orc_cg_sample.restype = C.c_int
         _L.orc_cg_sample.argtypes = [vp, C.c_int]
+        _L.orc_mg_attach.restype = C.c_int
+        _L.orc_mg_attach.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
     return _L
 
 
@@ -55,9 +57,15 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
+SOLVERS = {b"cg": 0, b"jc": 1, b"gs": 2, b"mg": 3}
+
+
 class Oracle:
     """One CPU model built from a .input file (or a Config) and the engine's host
-    mesh (from develop_mode, or from a leaf list)."""
+    mesh (from develop_mode, or from a leaf list).  With solver="mg" every
+    level from mg_min_level up gets its own CPU model (its K from the level's
+    initial temperature, as in the reference) and the transfer maps of
+    oracle/mg_oracle.py."""
 
     def __init__(self, cfg, threads=1, leaves=None):
         from mantle_convection_lab_gb300.api import Config, Mesh
@@ -65,47 +73,89 @@ class Oracle:
             cfg = Config.from_input(cfg)
         self.cfg = cfg
         m = Mesh(cfg, leaves=leaves)
-        fl = m.max_level - 1
-        nel, nno = m.nel, m.nno
-        node = m.get("node")
-        ien = m.get("ien")
-        pos = np.searchsorted(node, ien)
+        self.mesh = m
         self._keep = []
-        k = self._keep.append
-        self.ienl = np.ascontiguousarray(pos, np.int32); k(self.ienl)
-        self.elev = np.ascontiguousarray(m.get("Mcode") & 15, np.int32); k(self.elev)
-        self.node = node.astype(np.int32); k(self.node)
-        self.X = m.get("X"); k(self.X)
-        self.vbc = np.ascontiguousarray(m.get("v_bc").astype(np.uint8)); k(self.vbc)
-        self.vbcval = m.get("v_bc_val"); k(self.vbcval)
-        self.tbc = np.ascontiguousarray(m.get("T_bc").astype(np.uint8)); k(self.tbc)
-        self.tbcval = m.get("T_bc_val"); k(self.tbcval)
-        hang = m.get("hang").reshape(3, -1) if m.nh else np.zeros((3, 0), np.int32)
-        self.hang = np.ascontiguousarray(np.searchsorted(node, hang), np.int32); k(self.hang)
+        self._lv = []
+        fl = m.max_level - 1
+        self._o = self._level(fl, threads)
+        sz = np.zeros(4, np.int32)
+        lib().orc_sizes(self._o, _p(sz))
+        self.nel, self.nno, self.neq, self.hneq = map(int, sz)
+        if cfg.solver == b"mg":
+            self._attach_mg(threads)
+        self.set_T(m.initial_temperature())
+
+    def _level(self, lev, threads):
+        m, cfg, k = self.mesh, self.cfg, self._keep.append
+        node = m.get("node", lev)
+        nel, nno = m.get("Mcode", lev).size, node.size
+        ienl = np.ascontiguousarray(np.searchsorted(node, m.get("ien", lev)), np.int32); k(ienl)
+        elev = np.ascontiguousarray(m.get("Mcode", lev) & 15, np.int32); k(elev)
+        node = node.astype(np.int32); k(node)
+        X = m.get("X", lev); k(X)
+        vbc = np.ascontiguousarray(m.get("v_bc", lev).astype(np.uint8)); k(vbc)
+        vbcval = m.get("v_bc_val", lev); k(vbcval)
+        tbc = np.ascontiguousarray(m.get("T_bc", lev).astype(np.uint8)); k(tbc)
+        tbcval = m.get("T_bc_val", lev); k(tbcval)
+        hang = m.get("hang", lev).reshape(3, -1)
         nh = hang.shape[1]
+        hang = np.ascontiguousarray(np.searchsorted(node, hang), np.int32); k(hang)
         L, H = cfg.model_length, cfg.model_height
         dx = np.array([L / (1 << l) for l in range(16)]); k(dx)
         dz = np.array([H / (1 << l) for l in range(16)]); k(dz)
         dpar = np.array([cfg.Rayleigh, cfg.A, cfg.refT, cfg.lower_mantle_jump, cfg.Q, cfg.theta, cfg.accuracy,
                          cfg.citcom_solver_accu, cfg.vis_min, cfg.vis_max]); k(dpar)
         ipar = np.array([cfg.max_citcom_cycle, cfg.max_cg_cycle, cfg.cg_precondition, cfg.check_v_only,
-                         int(cfg.solver == b"jc"), cfg.zero_P, cfg.AMR, cfg.auto_accuracy, threads],
+                         SOLVERS.get(bytes(cfg.solver), 0), cfg.zero_P, cfg.AMR, cfg.auto_accuracy, threads],
                         np.int32); k(ipar)
-        hp = [self.hang[i] if nh else np.zeros(1, np.int32) for i in range(3)]
+        hp = [hang[i] if nh else np.zeros(1, np.int32) for i in range(3)]
         self._keep.extend(hp)
-        self._o = lib().orc_new(nel, nno, m.gnox, m.gnoz, fl, _p(self.ienl), _p(self.elev), _p(self.node),
-                                _p(self.X), _p(self.vbc), _p(self.vbcval), _p(self.tbc), _p(self.tbcval), nh,
-                                _p(hp[0]), _p(hp[1]), _p(hp[2]), _p(dx), _p(dz), _p(dpar), _p(ipar))
-        sz = np.zeros(4, np.int32)
-        lib().orc_sizes(self._o, _p(sz))
-        self.nel, self.nno, self.neq, self.hneq = map(int, sz)
-        self.mesh = m
-        self.set_T(m.initial_temperature())
+        if lev == m.max_level - 1:
+            self.ienl, self.elev, self.node, self.X = ienl, elev, node, X
+        return lib().orc_new(nel, nno, m.gnox, m.gnoz, lev, _p(ienl), _p(elev), _p(node), _p(X), _p(vbc),
+                             _p(vbcval), _p(tbc), _p(tbcval), nh, _p(hp[0]), _p(hp[1]), _p(hp[2]), _p(dx),
+                             _p(dz), _p(dpar), _p(ipar))
+
+    def _attach_mg(self, threads):
+        import mg_oracle
+        m, cfg = self.mesh, self.cfg
+        lo, fl = cfg.mg_min_level, m.max_level - 1
+        arr = {lev: mg_oracle.level_arrays(m, lev) for lev in range(lo, fl + 1)}
+        orcs, itp_n, itp_src, prj = [], [], [], []
+        for lev in range(lo, fl + 1):
+            if lev < fl:
+                o = self._level(lev, threads)
+                T = np.ascontiguousarray(m.initial_temperature(lev)); self._keep.append(T)
+                lib().orc_set_T(o, _p(T))
+                self._lv.append(o)
+                orcs.append(o)
+                prj.append(np.ascontiguousarray(mg_oracle.project(arr[lev], arr[lev + 1]), np.int32))
+            else:
+                orcs.append(self._o)
+                prj.append(np.zeros(1, np.int32))
+            if lev > lo:
+                n, src = mg_oracle.interp(arr[lev - 1], arr[lev], lev - 1)
+                itp_n.append(np.ascontiguousarray(n, np.int32))
+                itp_src.append(np.ascontiguousarray(src, np.int32))
+            else:
+                itp_n.append(np.zeros(1, np.int32))
+                itp_src.append(np.zeros(1, np.int32))
+        self._keep.extend(itp_n + itp_src + prj)
+        ptrs = lambda xs: (C.c_void_p * len(xs))(*[x.ctypes.data for x in xs])
+        lv = (C.c_void_p * len(orcs))(*orcs)
+        self._keep.append(lv)
+        rc = lib().orc_mg_attach(self._o, len(orcs), lv, ptrs(itp_n), ptrs(itp_src), ptrs(prj), cfg.mg_cycle,
+                                 cfg.mg_finest_iteration, cfg.mg_coarse_iteration)
+        if rc != 0:
+            raise ValueError("mg hierarchy needs 2..16 levels")
 
     def close(self):
         if self._o:
             lib().orc_free(self._o)
             self._o = None
+        for o in self._lv:
+            lib().orc_free(o)
+        self._lv = []
 
     __del__ = close
 
