@@ -426,9 +426,11 @@ class Model:
                 "BAB": self.nel, "tau0": self.nel, "tau1": self.nel, "heat_F": self.heat_neq,
                 "X0": self.nno, "X1": self.nno}[which]
 
-    def get(self, which):
-        out = np.zeros(self._fsize(which), np.float64)
-        _check(lib().mclg_get_field(self._c, FIELDS[which], -1, _dptr(out), out.size), f"get {which}")
+    def get(self, which, lev=-1):
+        """A field of the finest level; with solver="mg", T and vis of a coarser level `lev` too."""
+        n = self._fsize(which) if lev < 0 or lev == self.max_level - 1 else self.mesh("sizes", lev)[1]
+        out = np.zeros(n, np.float64)
+        _check(lib().mclg_get_field(self._c, FIELDS[which], lev, _dptr(out), out.size), f"get {which}")
         return out
 
     def set(self, which, values):
@@ -447,10 +449,11 @@ class Model:
         return out
 
     # --- single operators ---
-    def stokes_matvec(self, x):
+    def stokes_matvec(self, x, lev=-1):
+        """K x on the finest level; with solver="mg" on a coarser level `lev` too."""
         x = np.ascontiguousarray(x, np.float64)
-        y = np.zeros(self.neq)
-        _check(lib().mclg_stokes_matvec(self._c, -1, _dptr(x), _dptr(y)), "stokes_matvec")
+        y = np.zeros(self.neq if lev < 0 or lev == self.max_level - 1 else self.mesh("sizes", lev)[2])
+        _check(lib().mclg_stokes_matvec(self._c, lev, _dptr(x), _dptr(y)), "stokes_matvec")
         return y
 
     def stokes_G(self, p):

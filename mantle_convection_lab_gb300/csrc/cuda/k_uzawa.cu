@@ -169,9 +169,212 @@ __device__ int jacobi_solve(cg::grid_group &g, GridRed &red, const UzawaArgs &a,
 	return cycle;
 }
 
+// ---- the reference's own inner solvers: gauss_seidel and multigrid --------
+// Both run in one thread block (block 0 of the cooperative Uzawa kernel; the
+// other blocks wait at the next grid barrier).  The sequential sweep becomes
+// a sweep over wavefronts: nodes of one wavefront share no matrix entry, and
+// every node's lower neighbours sit in earlier wavefronts and its upper ones
+// in later wavefronts, so each row reads exactly the values the sequential
+// sweep reads.  Rows sum their columns in the reference's order with every
+// product and sum rounded on its own (__dmul_rn / __dadd_rn: no fused
+// multiply-add), so the arithmetic is the reference's.
+
+// Both rows of node A (gauss_seidel, Solver.c:1883-1902): the row's own
+// column skipped and taken as the diagonal; row 1 reads row 0's new value.
+__device__ __forceinline__ void ref_gs_node(const RefLevel &R, const double2 *__restrict__ b, double2 *x, int A)
+{
+	const int nno = R.nno, ks = R.self_slot[A];
+	double2 xa = x[A];
+	if (R.vbc[A] != 'V') {
+		double s = 0.0, dg = 1.0;
+		for (int k = 0; k < R.nbw; k++) {
+			const double4 kb = R.K[(size_t)k * nno + A];
+			if (k == ks) {
+				dg = kb.x;
+				s = __dadd_rn(s, __dmul_rn(kb.y, xa.y));
+				continue;
+			}
+			const int B = R.nb[(size_t)k * nno + A];
+			if (B == A)   // padding slot
+				continue;
+			const double2 xb = x[B];
+			s = __dadd_rn(s, __dmul_rn(kb.x, xb.x));
+			s = __dadd_rn(s, __dmul_rn(kb.y, xb.y));
+		}
+		xa.x = (b[A].x - s) / dg;
+	}
+	if (R.vbc[nno + A] != 'V') {
+		double s = 0.0, dg = 1.0;
+		for (int k = 0; k < R.nbw; k++) {
+			const double4 kb = R.K[(size_t)k * nno + A];
+			if (k == ks) {
+				s = __dadd_rn(s, __dmul_rn(kb.z, xa.x));
+				dg = kb.w;
+				continue;
+			}
+			const int B = R.nb[(size_t)k * nno + A];
+			if (B == A)
+				continue;
+			const double2 xb = x[B];
+			s = __dadd_rn(s, __dmul_rn(kb.z, xb.x));
+			s = __dadd_rn(s, __dmul_rn(kb.w, xb.y));
+		}
+		xa.y = (b[A].y - s) / dg;
+	}
+	x[A] = xa;
+}
+
+// gauss_seidel (Solver.c:1866-1929): sweeps until the largest change is
+// below accu, at most max_cycle.  Block-wide; returns the sweeps done.
+__device__ int ref_gs(const RefLevel &R, const double2 *b, double2 *x, double accu, int max_cycle)
+{
+	const int tid = threadIdx.x, nth = blockDim.x;
+	int cycle = 0;
+	while (cycle < max_cycle) {
+		for (int A = tid; A < R.nno; A += nth)
+			R.xt[A] = x[A];
+		__syncthreads();
+		for (int w = 0; w < R.nwave; w++) {
+			const int i1 = R.wave_off[w + 1];
+			for (int i = R.wave_off[w] + tid; i < i1; i += nth)
+				ref_gs_node(R, b, x, R.wave[i]);
+			__syncthreads();
+		}
+		cycle++;
+		double mx[1] = {0.0};
+		for (int A = tid; A < R.nno; A += nth) {
+			const double2 xn = x[A], xo = R.xt[A];
+			if (R.vbc[A] != 'V')
+				mx[0] = fmax(mx[0], fabs(xn.x - xo.x));
+			if (R.vbc[R.nno + A] != 'V')
+				mx[0] = fmax(mx[0], fabs(xn.y - xo.y));
+		}
+		block_reduce<1>(mx, 1u);
+		if (mx[0] < accu)
+			break;
+	}
+	return cycle;
+}
+
+// get_residual (Solver.c:1291-1317): res = b, minus each column's product in turn.
+__device__ void ref_residual(const RefLevel &R, const double2 *__restrict__ b, const double2 *__restrict__ x,
+                             double2 *__restrict__ res)
+{
+	const int nno = R.nno;
+	for (int A = threadIdx.x; A < nno; A += blockDim.x) {
+		const int ks = R.self_slot[A];
+		double r0 = b[A].x, r1 = b[A].y;
+		for (int k = 0; k < R.nbw; k++) {
+			const int B = R.nb[(size_t)k * nno + A];
+			if (B == A && k != ks)
+				continue;
+			const double4 kb = R.K[(size_t)k * nno + A];
+			const double2 xb = x[B];
+			r0 = __dsub_rn(r0, __dmul_rn(kb.x, xb.x));
+			r0 = __dsub_rn(r0, __dmul_rn(kb.y, xb.y));
+			r1 = __dsub_rn(r1, __dmul_rn(kb.z, xb.x));
+			r1 = __dsub_rn(r1, __dmul_rn(kb.w, xb.y));
+		}
+		res[A] = make_double2(R.vbc[A] != 'V' ? r0 : 0.0, R.vbc[nno + A] != 'V' ? r1 : 0.0);
+	}
+}
+
+// multigrid (Solver.c:668-713) with MG (Solver.c:715-768) unrolled into a
+// descent and an ascent.  Below the finest level MG's x is G.err[lev]
+// itself: interp_error overwrites the entries it sets and x += err then
+// doubles every entry, as in the reference.  G.err is zeroed once per call,
+// not per V-cycle.  Returns the V-cycles done.
+__device__ int ref_mg(const RefMG &M, const double2 *b_top, double2 *x_top, double accu)
+{
+	const int tid = threadIdx.x, nth = blockDim.x, top = M.nlev - 1;
+	for (int k = 0; k < M.nlev; k++)
+		for (int A = tid; A < M.lev[k].nno; A += nth)
+			M.lev[k].err[A] = make_double2(0.0, 0.0);
+	__syncthreads();
+	int cycle = 0;
+	while (cycle < M.cycles) {
+		const RefLevel &T = M.lev[top];
+		for (int A = tid; A < T.nno; A += nth)   // multigrid's x_tmp
+			T.rhs[A] = x_top[A];
+		__syncthreads();
+		for (int k = top; k > 0; k--) {
+			const RefLevel &R = M.lev[k], &Lo = M.lev[k - 1];
+			const double2 *b = k == top ? b_top : R.rhs;
+			double2 *x = k == top ? x_top : R.err;
+			ref_gs(R, b, x, accu, M.fine_it);
+			ref_residual(R, b, x, R.res);
+			__syncthreads();
+			const double *ru = reinterpret_cast<const double *>(R.res);
+			for (int A = tid; A < Lo.nno; A += nth) {   // project_res (Solver.c:770-783)
+				const int u0 = Lo.prj[A], u1 = Lo.prj[Lo.nno + A];
+				Lo.rhs[A] = make_double2(u0 >= 0 ? ru[u0] : 0.0, u1 >= 0 ? ru[u1] : 0.0);
+			}
+			__syncthreads();
+		}
+		ref_gs(M.lev[0], M.lev[0].rhs, M.lev[0].err, accu, 1000);
+		for (int k = 1; k <= top; k++) {
+			const RefLevel &R = M.lev[k], &Lo = M.lev[k - 1];
+			const double2 *b = k == top ? b_top : R.rhs;
+			double2 *x = k == top ? x_top : R.err;
+			const double *el = reinterpret_cast<const double *>(Lo.err);
+			double *eu = reinterpret_cast<double *>(R.err);
+			for (int A = tid; A < R.nno; A += nth)   // interp_error (Solver.c:1029-1046)
+				for (int c = 0; c < 2; c++) {
+					const int n = R.itp_n[c * R.nno + A];
+					if (n <= 0)
+						continue;
+					double s = 0.0;
+					for (int i = 0; i < n; i++) {
+						const int l = R.itp_src[(size_t)(i * 2 + c) * R.nno + A];
+						if (l != -1)
+							s = __dadd_rn(s, el[l]);
+					}
+					eu[2 * A + c] = s / n;
+				}
+			__syncthreads();
+			for (int A = tid; A < R.nno; A += nth) {
+				const double2 e = R.err[A];
+				double2 xv = x[A];
+				xv.x = __dadd_rn(xv.x, e.x);
+				xv.y = __dadd_rn(xv.y, e.y);
+				x[A] = xv;
+			}
+			__syncthreads();
+			ref_gs(R, b, x, accu, M.coarse_it);
+		}
+		cycle++;
+		double mx[1] = {0.0};   // check_convergency (Solver.c:1267-1289)
+		for (int A = tid; A < T.nno; A += nth) {
+			const double2 xn = x_top[A], xo = T.rhs[A];
+			if (T.vbc[A] != 'V')
+				mx[0] = fmax(mx[0], fabs(xn.x - xo.x));
+			if (T.vbc[T.nno + A] != 'V')
+				mx[0] = fmax(mx[0], fabs(xn.y - xo.y));
+		}
+		block_reduce<1>(mx, 1u);
+		if (mx[0] < accu)
+			break;
+	}
+	return cycle;
+}
+
+// REF: the kernel instance that runs the reference's gauss_seidel / multigrid
+// (a separate instance keeps the CG instance's registers as they were).
+template <bool REF>
 __device__ int inner_solve(cg::grid_group &g, const UzawaArgs &a, GridRed &red, const StokesOp &op, double2 *b,
                            double2 *x, double accu, int *status)
 {
+	if (REF) {
+		__shared__ int done;
+		if (blockIdx.x == 0) {
+			const int n = a.ref_kind == kRefMG ? ref_mg(*a.ref, b, x, accu)
+			                                   : ref_gs(a.ref->lev[a.ref->nlev - 1], b, x, accu, 1000);
+			if (threadIdx.x == 0)
+				done = n;
+		}
+		g.sync();
+		return blockIdx.x == 0 ? done : 0;
+	}
 	if (a.solver_jc)
 		return jacobi_solve(g, red, a, b, x, a.xt, accu, 1000, status);
 	return cg_solve(g, red, op, reinterpret_cast<const double *>(b), reinterpret_cast<double *>(x),
@@ -180,6 +383,7 @@ __device__ int inner_solve(cg::grid_group &g, const UzawaArgs &a, GridRed &red, 
 	                a.precond != 0, false, status);
 }
 
+template <bool REF>
 __global__ void __launch_bounds__(kBlock) k_uzawa(UzawaArgs a)
 {
 	cg::grid_group g = cg::this_grid();
@@ -213,7 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_uzawa(UzawaArgs a)
 		a.Ah[A] = make_double2(vfree(L, A, 0) ? f.x - g0 - k0 : 0.0, vfree(L, A, 1) ? f.y - g1 - k1 : 0.0);
 	}
 	g.sync();
-	int cg_total = inner_solve(g, a, red, op, a.Ah, a.u1, accu, status);
+	int cg_total = inner_solve<REF>(g, a, red, op, a.Ah, a.u1, accu, status);
 	for (int A = tid; A < L.nno; A += nth) {
 		double2 dv = a.d[A];
 		const double2 u = a.u1[A];
@@ -255,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) k_uzawa(UzawaArgs a)
 			a.u1[A] = make_double2(0.0, 0.0);
 		}
 		g.sync();
-		cg_total += inner_solve(g, a, red, op, a.Ah, a.u1, accu, status);
+		cg_total += inner_solve<REF>(g, a, red, op, a.Ah, a.u1, accu, status);
 		double sa[1] = {0.0};
 		for (int e = tid; e < L.nel; e += nth) {
 			const double t = gtmul_elem(L, a.u1, e);
@@ -369,7 +573,7 @@ __global__ void __launch_bounds__(kBlock) k_v_to_nodes(DevLevel L, const double2
 	V[A] = make_double2(vfree(L, A, 0) ? dv.x : L.vbcval[A], vfree(L, A, 1) ? dv.y : L.vbcval[L.nno + A]);
 }
 
-void *uzawa_kernel_ptr() { return (void *)k_uzawa; }
+void *uzawa_kernel_ptr(int ref) { return ref ? (void *)k_uzawa<true> : (void *)k_uzawa<false>; }
 void *kmul_kernel_ptr() { return (void *)k_kmul; }
 
 }  // namespace mclg

@@ -14,7 +14,7 @@ namespace mclg {
 void upload_shape_tables_elem(const ShapeTables &s, cudaStream_t st);
 void upload_shape_tables_uzawa(const ShapeTables &s, cudaStream_t st);
 void upload_shape_tables_heat(const ShapeTables &s, cudaStream_t st);
-void *uzawa_kernel_ptr();
+void *uzawa_kernel_ptr(int ref);
 void *heat_cg_kernel_ptr();
 __global__ void k_buoy_rowavg(DevLevel L, const double *T, double Ra, double *avg);
 __global__ void k_buoy_vis(DevLevel L, const double *T, double Ra, const double *avg, double Aexp, double refT,
@@ -100,6 +100,15 @@ struct mclg_ctx {
 	bool g_extrap, g_feat;        // this step's solve started from extrapolation / computed features
 	bool st_borrowed;             // the stream belongs to an ensemble
 	int git_prev;                 // inner iterations of the last step solved from the last solution (-1: none)
+	// the reference's own inner solvers (solver="gs" / "mg"): levels ref_lo..fl
+	int ref_kind, ref_lo;
+	RefMG *ref_dev;
+	DevLevelBuf ref_lb[MCLG_MAX_LEVEL];   // coarser levels (the finest is lb)
+	DevLevel ref_L[MCLG_MAX_LEVEL];
+	double *ref_T[MCLG_MAX_LEVEL], *ref_vis[MCLG_MAX_LEVEL];
+	double4 *ref_K[MCLG_MAX_LEVEL];
+	void **ref_ptr;
+	int ref_nptr, ref_cap;
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -163,11 +172,10 @@ static void shape_tables(ShapeTables &S)
 	S.dNdeta_c[3] = 0.25 * (1.0 + xi) * (-1.0);
 }
 
-static int upload_level(mclg_ctx *c, int lev)
+static int upload_level_into(mclg_ctx *c, int lev, DevLevelBuf &b, DevLevel &L)
 {
 	const mclg_mesh &m = c->mesh;
 	const mclg_level &H = m.lev[lev];
-	DevLevelBuf &b = c->lb;
 	const size_t ne = H.nel, nn = H.nno, nh = H.nh;
 	cudaStream_t st = c->st;
 	std::vector<int> ienl(H.ienl, H.ienl + 4 * ne);
@@ -203,7 +211,6 @@ static int upload_level(mclg_ctx *c, int lev)
 	CK(upload(&b.dx, m.dx, MCLG_MAX_LEVEL, st));
 	CK(upload(&b.dz, m.dz, MCLG_MAX_LEVEL, st));
 	CK(cudaStreamSynchronize(st));
-	DevLevel &L = c->L;
 	L.nel = (int)ne;
 	L.nno = (int)nn;
 	L.nbw = H.nbw;
@@ -237,6 +244,22 @@ static int upload_level(mclg_ctx *c, int lev)
 	L.dx = b.dx;
 	L.dz = b.dz;
 	return MCLG_OK;
+}
+
+static int upload_level(mclg_ctx *c, int lev)
+{
+	return upload_level_into(c, lev, c->lb, c->L);
+}
+
+static void free_level_buf(DevLevelBuf &b)
+{
+	void *ptrs[] = {b.node, b.ienl, b.elev, b.p2n_cnt, b.p2n_el, b.p2n_a, b.nb, b.hang_ni, b.hang_ci0, b.hang_ci1,
+	                b.cell_elem, b.kslot, b.self_slot, b.dxh, b.dzh, b.jac, b.area, b.vbcval, b.tbcval, b.X, b.dx,
+	                b.dz, b.vbc, b.tbc};
+	for (void *q : ptrs)
+		if (q)
+			cudaFree(q);
+	memset(&b, 0, sizeof b);
 }
 
 static int coop_blocks(void *kernel, int num_sms, int work)
@@ -396,6 +419,226 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 
 // History buffers of the converged solvers: the last two solutions (for
 // warm_start=3 and the learned guess) and a second candidate guess.
+// ---- the reference's own inner solvers: solver="gs" and solver="mg" ---------
+static int blocks_for(size_t n)
+{
+	return (int)((n + kBlock - 1) / kBlock);
+}
+
+static int check_launch(mclg_ctx *c, const char *what)
+{
+	cudaError_t e = cudaGetLastError();
+	c->launches++;
+	if (e != cudaSuccess)
+		return cuda_fail(e, what);
+	return MCLG_OK;
+}
+
+static cudaError_t ref_track(mclg_ctx *c, void *p)
+{
+	if (c->ref_nptr == c->ref_cap) {
+		const int cap = c->ref_cap ? 2 * c->ref_cap : 64;
+		void **q = (void **)realloc(c->ref_ptr, cap * sizeof(void *));
+		if (q == NULL) {
+			cudaFree(p);
+			return cudaErrorMemoryAllocation;
+		}
+		c->ref_ptr = q;
+		c->ref_cap = cap;
+	}
+	c->ref_ptr[c->ref_nptr++] = p;
+	return cudaSuccess;
+}
+
+template <class T>
+static cudaError_t ref_zeros(mclg_ctx *c, T **p, size_t n)
+{
+	cudaError_t e = dalloc(p, n);
+	if (e != cudaSuccess)
+		return e;
+	if ((e = ref_track(c, *p)) != cudaSuccess)
+		return e;
+	return cudaMemsetAsync(*p, 0, (n + 1) * sizeof(T), c->st);
+}
+
+template <class T>
+static cudaError_t ref_upload(mclg_ctx *c, T **p, const std::vector<T> &h)
+{
+	cudaError_t e = upload(p, h.data(), h.size(), c->st);
+	if (e != cudaSuccess)
+		return e;
+	return ref_track(c, *p);
+}
+
+// Node-layout dof (2*node + direction) of every equation of a level.
+static std::vector<int> eq_dofs(const mclg_level &H)
+{
+	std::vector<int> dof(H.neq > 0 ? H.neq : 1, -1);
+	for (int A = 0; A < H.nno; A++)
+		for (int d = 0; d < 2; d++) {
+			const int eq = H.id[(size_t)d * H.nno + A];
+			if (eq >= 0)
+				dof[eq] = 2 * A + d;
+		}
+	return dof;
+}
+
+// The hierarchy of solver="mg" (mg_min_level .. finest; Connection.c:20-29
+// builds its maps) or the finest level alone for solver="gs": per level the
+// Gauss-Seidel wavefronts, work vectors and transfer maps, and below the
+// finest level the operator K of the level's own initial temperature.  The
+// reference assembles every level every step (Viscosity.c:8,
+// Build_matrix.c:8) but only the finest level's T changes, so the coarse K
+// are built once here.
+static int ref_setup(mclg_ctx *c)
+{
+	const mclg_mesh &m = c->mesh;
+	const mclg_config &f = c->cfg;
+	c->ref_kind = strcmp(f.solver, "mg") == 0 ? kRefMG : kRefGS;
+	const int top = c->fl, lo = c->ref_kind == kRefMG ? m.min_level : top;
+	if (c->ref_kind == kRefMG && lo >= top) {   // Solver.c:677-682
+		mclg_set_error("solver=\"mg\" needs mg_min_level (%d) below level-1 (%d)", lo, top);
+		return MCLG_BAD_INPUT;
+	}
+	if (c->ref_kind == kRefMG && (f.mg_cycle < 0 || f.mg_finest_iteration < 0 || f.mg_coarse_iteration < 0)) {
+		mclg_set_error("mg_cycle, mg_finest_iteration and mg_coarse_iteration must be >= 0");
+		return MCLG_BAD_INPUT;
+	}
+	c->ref_lo = lo;
+	RefMG h;
+	memset(&h, 0, sizeof h);
+	h.nlev = top - lo + 1;
+	h.cycles = f.mg_cycle;
+	h.fine_it = f.mg_finest_iteration;
+	h.coarse_it = f.mg_coarse_iteration;
+	double *zeros_gnoz = NULL;
+	CK(ref_zeros(c, &zeros_gnoz, (size_t)m.gnoz));
+	for (int lev = lo; lev <= top; lev++) {
+		const int k = lev - lo;
+		const mclg_level &H = m.lev[lev];
+		const size_t nn = H.nno;
+		RefLevel &R = h.lev[k];
+		if (lev == top) {
+			c->ref_L[k] = c->L;
+			R.K = c->K;
+		} else {
+			DevLevel &L = c->ref_L[k];
+			memset(&L, 0, sizeof L);
+			int rc = upload_level_into(c, lev, c->ref_lb[k], L);
+			if (rc != MCLG_OK)
+				return rc;
+			std::vector<double> T(nn);
+			if ((rc = mclg_host_initial_temperature(&m, &f, lev, T.data())) != MCLG_OK)
+				return rc;
+			double *buoy = NULL;
+			double2 *F = NULL, *Kd = NULL;
+			CK(ref_upload(c, &c->ref_T[k], T));
+			CK(ref_zeros(c, &c->ref_vis[k], nn));
+			CK(ref_zeros(c, &buoy, nn));
+			CK(ref_zeros(c, &c->ref_K[k], (size_t)H.nbw * nn));
+			CK(ref_zeros(c, &F, nn));
+			CK(ref_zeros(c, &Kd, nn));
+			// viscosity of the level's T; the buoyancy (Ra = 0 here) only feeds F, which no level below the finest uses
+			k_buoy_vis<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->ref_T[k], 0.0, zeros_gnoz, f.A, f.refT,
+			                                                 f.lower_mantle_jump, f.vis_min, f.vis_max, buoy,
+			                                                 c->ref_vis[k]);
+			if ((rc = check_launch(c, "k_buoy_vis")))
+				return rc;
+			k_assemble_stokes<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->ref_vis[k], buoy, c->ref_K[k], F, Kd, 1);
+			if ((rc = check_launch(c, "k_assemble_stokes")))
+				return rc;
+			R.K = c->ref_K[k];
+		}
+		const DevLevel &L = c->ref_L[k];
+		R.nno = (int)nn;
+		R.nbw = H.nbw;
+		R.nb = L.nb;
+		R.self_slot = L.self_slot;
+		R.vbc = L.vbc;
+		// Gauss-Seidel wavefronts, nodes grouped by wavefront
+		std::vector<int> wave(nn), order(nn), off;
+		mclg_refmg_waves(&H, wave.data());
+		int nw = 0;
+		for (size_t A = 0; A < nn; A++)
+			nw = wave[A] + 1 > nw ? wave[A] + 1 : nw;
+		off.assign((size_t)nw + 1, 0);
+		for (size_t A = 0; A < nn; A++)
+			off[wave[A] + 1]++;
+		for (int w = 0; w < nw; w++)
+			off[w + 1] += off[w];
+		std::vector<int> fill(off.begin(), off.end() - 1);
+		for (size_t A = 0; A < nn; A++)
+			order[fill[wave[A]]++] = (int)A;
+		R.nwave = nw;
+		CK(ref_upload(c, (int **)&R.wave, order));
+		CK(ref_upload(c, (int **)&R.wave_off, off));
+		CK(ref_zeros(c, &R.err, nn));
+		CK(ref_zeros(c, &R.rhs, nn));
+		CK(ref_zeros(c, &R.res, nn));
+		CK(ref_zeros(c, &R.xt, nn));
+		// interp_error's map from the level below (Connection.c:708-930)
+		std::vector<int> itp_n(2 * nn, 0), itp_src(8 * nn, -1);
+		if (k > 0) {
+			const int neq = H.neq;
+			std::vector<int> n(neq > 0 ? neq : 1), src(4 * (size_t)(neq > 0 ? neq : 1));
+			if (mclg_refmg_interp(&m, lev, n.data(), src.data()) != MCLG_OK) {
+				mclg_set_error("level %d: interpolation map has more than 4 terms", lev);
+				return MCLG_BAD_INPUT;
+			}
+			const std::vector<int> lo_dof = eq_dofs(m.lev[lev - 1]);
+			for (size_t A = 0; A < nn; A++)
+				for (int d = 0; d < 2; d++) {
+					const int eu = H.id[(size_t)d * nn + A];
+					if (eu < 0)
+						continue;
+					itp_n[(size_t)d * nn + A] = n[eu];
+					for (int i = 0; i < 4; i++) {
+						const int el = src[(size_t)i * neq + eu];
+						itp_src[(size_t)(i * 2 + d) * nn + A] = el >= 0 ? lo_dof[el] : -1;
+					}
+				}
+		}
+		CK(ref_upload(c, (int **)&R.itp_n, itp_n));
+		CK(ref_upload(c, (int **)&R.itp_src, itp_src));
+		// project_res's map to the level above (Connection.c:1051-1251)
+		std::vector<int> prj(2 * nn, -1);
+		if (lev < top) {
+			std::vector<int> up_eq(H.neq > 0 ? H.neq : 1);
+			mclg_refmg_project(&m, lev, up_eq.data());
+			const std::vector<int> up_dof = eq_dofs(m.lev[lev + 1]);
+			for (size_t A = 0; A < nn; A++)
+				for (int d = 0; d < 2; d++) {
+					const int el = H.id[(size_t)d * nn + A];
+					if (el < 0)
+						continue;
+					if (up_eq[el] < 0) {   // the reference would read res_u[-1] or leave res_l unset
+						mclg_set_error("level %d: equation %d has no equation on level %d to take its residual from",
+						               lev, el, lev + 1);
+						return MCLG_BAD_INPUT;
+					}
+					prj[(size_t)d * nn + A] = up_dof[up_eq[el]];
+				}
+		}
+		CK(ref_upload(c, (int **)&R.prj, prj));
+	}
+	void *p = NULL;
+	CK(cudaMalloc(&p, sizeof(RefMG)));
+	CK(ref_track(c, p));
+	c->ref_dev = (RefMG *)p;
+	CK(cudaMemcpyAsync(c->ref_dev, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
+// A level below the finest that is resident on the device (solver="mg"); k is its index in the hierarchy.
+static bool coarse_level(const mclg_ctx *c, int lev, int *k)
+{
+	if (c->ref_kind != kRefMG || lev < c->ref_lo || lev >= c->fl)
+		return false;
+	*k = lev - c->ref_lo;
+	return true;
+}
+
 static int alloc_history(mclg_ctx *c)
 {
 	if (c->d_h1 != NULL)
@@ -586,8 +829,9 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 		mclg_set_error("lg_mul and grain_damage paths are not part of this engine (set both to 0)");
 		return MCLG_BAD_INPUT;
 	}
-	if (strcmp(cfg->solver, "cg") != 0 && strcmp(cfg->solver, "jc") != 0) {
-		mclg_set_error("solver=\"%s\": this engine runs \"cg\" and \"jc\"", cfg->solver);
+	const bool ref_solver = strcmp(cfg->solver, "gs") == 0 || strcmp(cfg->solver, "mg") == 0;
+	if (strcmp(cfg->solver, "cg") != 0 && strcmp(cfg->solver, "jc") != 0 && !ref_solver) {
+		mclg_set_error("solver=\"%s\": the reference's solvers are \"cg\", \"jc\", \"gs\" and \"mg\"", cfg->solver);
 		return MCLG_BAD_INPUT;
 	}
 	int ndev = 0;
@@ -692,8 +936,13 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	CKD(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
 	CKD(cudaMemsetAsync(c->V, 0, nn * sizeof(double2), c->st));
 	CKD(cudaMemsetAsync(c->T, 0, nn * sizeof(double), c->st));
+	if (ref_solver && cfg->precision == 0 && (rc = ref_setup(c)) != MCLG_OK) {
+		mclg_destroy(c);
+		*out = NULL;
+		return rc;
+	}
 	const int work = (int)(nn > ne ? nn : ne);
-	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(), c->num_sms, work);
+	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(c->ref_kind != kRefNone), c->num_sms, work);
 	c->coop_heat = coop_blocks(heat_cg_kernel_ptr(), c->num_sms, (int)nn);
 	if (cfg->precision != 0) {
 		if (!c->mesh.uniform) {
@@ -746,10 +995,13 @@ void mclg_destroy(mclg_ctx *c)
 		return;
 	if (c->st)
 		cudaStreamSynchronize(c->st);
-	void *ptrs[] = {c->lb.node, c->lb.ienl, c->lb.elev, c->lb.p2n_cnt, c->lb.p2n_el, c->lb.p2n_a, c->lb.nb,
-	                c->lb.hang_ni, c->lb.hang_ci0, c->lb.hang_ci1, c->lb.cell_elem, c->lb.kslot, c->lb.self_slot,
-	                c->lb.dxh, c->lb.dzh, c->lb.jac, c->lb.area, c->lb.vbcval, c->lb.tbcval, c->lb.X, c->lb.dx,
-	                c->lb.dz, c->lb.vbc, c->lb.tbc, c->T, c->vis, c->buoy, c->avg, c->stress, c->stress_e, c->V,
+	free_level_buf(c->lb);
+	for (int k = 0; k < MCLG_MAX_LEVEL; k++)
+		free_level_buf(c->ref_lb[k]);
+	for (int i = 0; i < c->ref_nptr; i++)
+		cudaFree(c->ref_ptr[i]);
+	free(c->ref_ptr);
+	void *ptrs[] = {c->T, c->vis, c->buoy, c->avg, c->stress, c->stress_e, c->V,
 	                c->K, c->F, c->Kdiag, c->idiag, c->d, c->u1, c->Ah, c->r, c->s, c->dd, c->q, c->xt, c->bab,
 	                c->p, c->tau0, c->tau1, c->HK, c->HC, c->HF, c->HA, c->HB, c->hx, c->hidiag, c->hr, c->hs,
 	                c->hd, c->hq, c->mins, c->red_part, c->sc, c->tmpA, c->tmpB};
@@ -777,19 +1029,6 @@ void mclg_destroy(mclg_ctx *c)
 	free(c);
 }
 
-static int blocks_for(size_t n)
-{
-	return (int)((n + kBlock - 1) / kBlock);
-}
-
-static int check_launch(mclg_ctx *c, const char *what)
-{
-	cudaError_t e = cudaGetLastError();
-	c->launches++;
-	if (e != cudaSuccess)
-		return cuda_fail(e, what);
-	return MCLG_OK;
-}
 
 int mclg_initial_temperature(mclg_ctx *c)
 {
@@ -917,8 +1156,11 @@ static int launch_uzawa(mclg_ctx *c)
 	a.neq = c->mesh.lev[c->fl].neq;
 	a.citcom_accu = f.citcom_solver_accu;
 	a.accuracy = f.accuracy;
+	a.ref_kind = c->ref_kind;
+	a.ref = c->ref_dev;
 	void *args[] = {&a};
-	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(), dim3(c->coop_uzawa), dim3(kBlock), args, 0, c->st));
+	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(c->ref_kind != kRefNone), dim3(c->coop_uzawa), dim3(kBlock), args, 0,
+	                               c->st));
 	c->launches++;
 	return MCLG_OK;
 }
@@ -1172,6 +1414,18 @@ int mclg_get_field(mclg_ctx *c, int which, int lev, double *out, size_t n)
 {
 	if (c == NULL || out == NULL)
 		return MCLG_BAD_INPUT;
+	int k;
+	if (coarse_level(c, lev, &k) && (which == MCLG_F_T || which == MCLG_F_VIS)) {   // a coarser level's T, vis
+		const size_t need = (size_t)c->mesh.lev[lev].nno;
+		if (n != need) {
+			mclg_set_error("field %d of level %d has %zu entries, buffer has %zu", which, lev, need, n);
+			return MCLG_BAD_INPUT;
+		}
+		CK(cudaMemcpyAsync(out, which == MCLG_F_T ? c->ref_T[k] : c->ref_vis[k], n * sizeof(double),
+		                   cudaMemcpyDeviceToHost, c->st));
+		CK(cudaStreamSynchronize(c->st));
+		return MCLG_OK;
+	}
 	if (lev >= 0 && lev != c->fl) {
 		mclg_set_error("only the finest level (%d) is resident on the device", c->fl);
 		return MCLG_BAD_INPUT;
@@ -1276,9 +1530,9 @@ int mclg_get_mesh(mclg_ctx *c, int which, int lev, int *out, size_t n)
 }
 
 // ---- single operators ----------------------------------------------------
-static int eq_to_node(mclg_ctx *c, const double *x, double *dev)
+static int eq_to_node(mclg_ctx *c, const double *x, double *dev, int lev = -1)
 {
-	const mclg_level &H = c->mesh.lev[c->fl];
+	const mclg_level &H = c->mesh.lev[lev < 0 ? c->fl : lev];
 	const size_t nn = H.nno;
 	std::vector<double> buf(2 * nn, 0.0);
 	for (size_t A = 0; A < nn; A++)
@@ -1292,9 +1546,9 @@ static int eq_to_node(mclg_ctx *c, const double *x, double *dev)
 	return MCLG_OK;
 }
 
-static int node_to_eq(mclg_ctx *c, const double *dev, double *y)
+static int node_to_eq(mclg_ctx *c, const double *dev, double *y, int lev = -1)
 {
-	const mclg_level &H = c->mesh.lev[c->fl];
+	const mclg_level &H = c->mesh.lev[lev < 0 ? c->fl : lev];
 	const size_t nn = H.nno;
 	std::vector<double> buf(2 * nn);
 	CK(cudaMemcpyAsync(buf.data(), dev, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -1319,6 +1573,17 @@ static int check_lev(mclg_ctx *c, int lev)
 
 int mclg_stokes_matvec(mclg_ctx *c, int lev, const double *x, double *y)
 {
+	int k;
+	if (c != NULL && x != NULL && y != NULL && coarse_level(c, lev, &k)) {   // K of a coarser level
+		int rc = eq_to_node(c, x, c->tmpA, lev);
+		if (rc)
+			return rc;
+		k_kmul<<<blocks_for(c->ref_L[k].nno), kBlock, 0, c->st>>>(c->ref_L[k], c->ref_K[k], (const double2 *)c->tmpA,
+		                                                            (double2 *)c->tmpB);
+		if ((rc = check_launch(c, "k_kmul")))
+			return rc;
+		return node_to_eq(c, c->tmpB, y, lev);
+	}
 	if (c == NULL || x == NULL || y == NULL || check_lev(c, lev))
 		return MCLG_BAD_INPUT;
 	int rc = eq_to_node(c, x, c->tmpA);
@@ -1504,8 +1769,11 @@ extern "C" int mclg_solve_velocity_pressure_noalloc(mclg_ctx *c, mclg_step_stats
 	a.neq = c->mesh.lev[c->fl].neq;
 	a.citcom_accu = f.citcom_solver_accu;
 	a.accuracy = f.accuracy;
+	a.ref_kind = c->ref_kind;
+	a.ref = c->ref_dev;
 	void *args[] = {&a};
-	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(), dim3(c->coop_uzawa), dim3(kBlock), args, 0, c->st));
+	CK(cudaLaunchCooperativeKernel(uzawa_kernel_ptr(c->ref_kind != kRefNone), dim3(c->coop_uzawa), dim3(kBlock), args, 0,
+	                               c->st));
 	c->launches++;
 	// compute_stress with the element stresses in the same array
 	k_stress_elem<<<blocks_for(ne), kBlock, 0, c->st>>>(c->L, c->vis, c->V, ev[8]);

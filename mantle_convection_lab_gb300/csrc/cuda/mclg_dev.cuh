@@ -198,6 +198,29 @@ __device__ __forceinline__ void element_g(const ShapeTables &S, double dzh, doub
 __constant__ static const int kSortedCorner[4] = {0, 1, 3, 2};
 
 // ---- kernel argument blocks (shared by the host launch code) ---------------
+// One level of the hierarchy of the reference's own inner solvers
+// (solver="gs": the finest level alone; solver="mg": mg_min_level up to the
+// finest).  Node layout, both directions of node A in one double2.  Transfer
+// entries name a dof of the neighbouring level as 2*node + direction.
+struct RefLevel {
+	int nno, nbw, nwave;
+	const int *nb;                  // [nbw*nno] matrix neighbours (the level's sorted node list)
+	const unsigned char *self_slot; // [nno] slot of the node itself in nb
+	const char *vbc;                // [2*nno] BC codes: 'V' fixed
+	const double4 *K;               // [nbw*nno] 2x2 blocks
+	const int *wave;                // [nno] nodes ordered by Gauss-Seidel wavefront
+	const int *wave_off;            // [nwave+1]
+	const int *itp_n;               // [2*nno] terms of the interpolated error (0: not set), from the level below
+	const int *itp_src;             // [8*nno] itp_src[(i*2+c)*nno + A]: dof of the level below, -1 fixed
+	const int *prj;                 // [2*nno] dof of the level above whose residual this dof takes, -1 fixed
+	double2 *err, *rhs, *res, *xt;  // G.err[lev], projected right-hand side, residual, sweep copy
+};
+struct RefMG {
+	int nlev, cycles, fine_it, coarse_it;   // levels lev[0] (coarsest) .. lev[nlev-1] (finest)
+	RefLevel lev[16];
+};
+enum { kRefNone = 0, kRefGS = 1, kRefMG = 2 };
+
 struct UzawaArgs {
 	DevLevel L;
 	const double4 *K;
@@ -209,6 +232,8 @@ struct UzawaArgs {
 	StepScalars *sc;
 	int max_citcom, max_cg, precond, check_v_only, solver_jc, auto_accuracy, neq;
 	double citcom_accu, accuracy;
+	int ref_kind;          // kRefGS / kRefMG: the inner solve is the reference's gauss_seidel / multigrid
+	const RefMG *ref;      // device copy of the hierarchy
 };
 
 // Scalar heat operator A = C/(theta dt) + K on the neighbour slots.

@@ -152,7 +152,7 @@ def test_create_without_device_reports_no_device():
 
 def test_create_rejects_unsupported_options(tmp_path):
     L = api.lib()
-    for extra, needle in (("lg_mul=1\n", b"lg_mul"), ('solver="mg"\n', b"solver")):
+    for extra, needle in (("lg_mul=1\n", b"lg_mul"), ('solver="sor"\n', b"solver")):
         c = Config.from_input(write(tmp_path, open(golden_input("cfg1_l5")).read() + extra))
         h = C.c_void_p()
         assert L.mclg_create(C.byref(h), C.byref(c)) == api.BAD_INPUT
