@@ -174,13 +174,47 @@ int mclg_solve_velocity_pressure_noalloc(mclg_ctx *ctx, mclg_step_stats *st);
 int mclg_update_temperature(mclg_ctx *ctx, mclg_step_stats *st);      /* Update_temperature.c:3-133 */
 /* output(): Output.c:4-156 text files for the current G.timestep. */
 int mclg_output(mclg_ctx *ctx, const char *data_dir, int timestep);
-/* One whole step: buoyancy .. solve, optional output, update_temperature. */
+/* output() off the critical path: the fields are copied to pinned host memory
+ * on the model's stream and a writer thread formats the files (one thread per
+ * file) while the GPU carries on.  At most two outputs are in flight; a third
+ * call waits for the oldest.  flags: MCLG_OUT_TEXT, Output.c's five text files
+ * byte for byte; MCLG_OUT_BINARY, a full-precision side-car with pressure,
+ * <data_dir>/<%07d>/fields.0.<%07d>.bin ("MCLGOUT1", int32 version, nno, nel,
+ * timestep, double model_time, then X, Z, T, V0, V1 [nno], P [nel],
+ * stress, vis [nno] as doubles).  A write error is returned by the next
+ * output call or by mclg_output_wait. */
+#define MCLG_OUT_TEXT 1
+#define MCLG_OUT_BINARY 2
+int mclg_output_async(mclg_ctx *ctx, const char *data_dir, int timestep, int flags);
+/* every pending output written; the first error of any */
+int mclg_output_wait(mclg_ctx *ctx);
+/* One whole step: buoyancy .. solve, optional output (asynchronous, as
+ * mclg_output_async with MCLG_OUT_TEXT), update_temperature. */
 int mclg_step(mclg_ctx *ctx, int write_output, mclg_step_stats *st);
 /* Same step with the host-buffer round trip a caller without device memory
  * makes: T (nno doubles, G.node order) is copied in before the step and
  * T, V (2*nno) and P (nel) are copied out after it. */
 int mclg_step_host(mclg_ctx *ctx, const double *T_in, double *T_out, double *V_out,
                    double *P_out, mclg_step_stats *st);
+
+/* ---- checkpoint / restart ----------------------------------------------
+ * The reference restarts from a temperature file alone (T_ini=-1,
+ * read_T_from_file, Initial_condition.c:171-195; mclg_create reads it too).
+ * A checkpoint holds the whole state a continued run reads: the finest
+ * level's leaves (so any develop_mode or remeshed tree is rebuilt), T, V,
+ * stress, d, P, the model time and step counter, the converged solvers'
+ * warm-start history and the learned guess's counters, in one binary file
+ * closed by a checksum.  A run restarted from a checkpoint continues bit for
+ * bit as the uninterrupted run; the network of a learned guess is attached
+ * again by the caller (mclg_guess_set). */
+int mclg_checkpoint_save(mclg_ctx *ctx, const char *path);
+/* into a model on the same mesh (MCLG_BAD_INPUT otherwise; MCLG_IO_ERROR for
+ * a truncated or corrupt file) */
+int mclg_checkpoint_load(mclg_ctx *ctx, const char *path);
+/* create a model on the checkpoint's mesh with this configuration, then load */
+int mclg_restart(mclg_ctx **ctx, const mclg_config *cfg, const char *path);
+/* G.timestep and G.model_time of the model */
+int mclg_get_time(mclg_ctx *ctx, int *timestep, double *model_time);
 
 /* ---- state access ------------------------------------------------------ */
 enum {

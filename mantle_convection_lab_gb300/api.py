@@ -30,6 +30,7 @@ FIELDS = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoy
 MESH = {"sizes": 0, "Mcode": 1, "node": 2, "ien": 3, "id": 4, "heat_id": 5, "lm": 6, "hang": 7,
         "v_bc": 8, "T_bc": 9, "interp": 10, "project": 11, "gs_wave": 12}
 MESH_REAL = {"X": 0, "jacobi": 1, "area": 2, "v_bc_val": 3, "T_bc_val": 4}
+OUT_TEXT, OUT_BINARY = 1, 2
 
 
 class MclgError(RuntimeError):
@@ -141,6 +142,9 @@ def lib():
         "mclg_cnn_train": (C.c_int, [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.c_ulonglong, fp]),
         "mclg_cnn_save": (C.c_int, [vp, C.c_char_p]), "mclg_cnn_load": (C.c_int, [C.POINTER(vp), C.c_char_p]),
+        "mclg_checkpoint_save": (C.c_int, [vp, C.c_char_p]), "mclg_checkpoint_load": (C.c_int, [vp, C.c_char_p]),
+        "mclg_restart": (C.c_int, [C.POINTER(vp), vp, C.c_char_p]), "mclg_get_time": (C.c_int, [vp, ip, dp]),
+        "mclg_output_async": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_int]), "mclg_output_wait": (C.c_int, [vp]),
         "mclg_guess_set": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "mclg_create_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
         "mclg_amr_flags": (C.c_int, [vp, C.c_double, C.POINTER(C.c_ubyte), sz, dp]),
@@ -342,12 +346,15 @@ class Mesh:
 class Model:
     """One device-resident model; method names follow the reference's calls."""
 
-    def __init__(self, config, _handle=None, leaves=None):
+    def __init__(self, config, _handle=None, leaves=None, restart=None):
+        """restart: a checkpoint file (mclg_restart): the model is built on its mesh and takes its state."""
         self.config = config
         self._c = C.c_void_p()
         self._owned = _handle is None
         if _handle is not None:
             self._c = _handle
+        elif restart is not None:
+            _check(lib().mclg_restart(C.byref(self._c), C.byref(config), os.fsencode(restart)), "restart")
         elif leaves is not None:
             lv = np.ascontiguousarray(leaves, np.int32)
             _check(lib().mclg_create_leaves(C.byref(self._c), C.byref(config), _iptr(lv), lv.size), "create_leaves")
@@ -356,6 +363,26 @@ class Model:
         s = self.mesh("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
         self.timestep = 0
+        if restart is not None:
+            self.timestep = self._timestep()
+
+    def _timestep(self):
+        return self.time()[0]
+
+    def time(self):
+        """(G.timestep, G.model_time) of the model."""
+        ts, mt = C.c_int(), C.c_double()
+        _check(lib().mclg_get_time(self._c, C.byref(ts), C.byref(mt)), "get_time")
+        return ts.value, mt.value
+
+    def checkpoint(self, path):
+        """Write the whole state to `path` (mclg_checkpoint_save)."""
+        _check(lib().mclg_checkpoint_save(self._c, os.fsencode(path)), "checkpoint_save")
+
+    def load_checkpoint(self, path):
+        """Take the state of a checkpoint written on the same mesh (mclg_checkpoint_load)."""
+        _check(lib().mclg_checkpoint_load(self._c, os.fsencode(path)), "checkpoint_load")
+        self.timestep = self._timestep()
 
     def close(self):
         if self._c and self._owned:
@@ -405,6 +432,16 @@ class Model:
     def output(self, data_dir=None, timestep=None):
         d = None if data_dir is None else os.fsencode(data_dir)
         _check(lib().mclg_output(self._c, d, self.timestep if timestep is None else timestep), "output")
+
+    def output_async(self, data_dir=None, timestep=None, text=True, binary=False):
+        """output() off the critical path (mclg_output_async); output_wait() for completion."""
+        d = None if data_dir is None else os.fsencode(data_dir)
+        flags = (OUT_TEXT if text else 0) | (OUT_BINARY if binary else 0)
+        _check(lib().mclg_output_async(self._c, d, self.timestep if timestep is None else timestep, flags),
+               "output_async")
+
+    def output_wait(self):
+        _check(lib().mclg_output_wait(self._c), "output_wait")
 
     def step(self, write_output=False):
         st = StepStats()

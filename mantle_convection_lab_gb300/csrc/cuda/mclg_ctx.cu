@@ -8,6 +8,7 @@
 #include <vector>
 #include "k_mg.cuh"
 #include "cnn.cuh"
+#include "mclg_writer.cuh"
 #include "../host/mclg_host.h"
 
 namespace mclg {
@@ -109,6 +110,7 @@ struct mclg_ctx {
 	double4 *ref_K[MCLG_MAX_LEVEL];
 	void **ref_ptr;
 	int ref_nptr, ref_cap;
+	OutWriter *writer;            // asynchronous output, created on first use
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -993,6 +995,7 @@ void mclg_destroy(mclg_ctx *c)
 {
 	if (c == NULL)
 		return;
+	writer_free(c->writer);   // pending outputs are written first
 	if (c->st)
 		cudaStreamSynchronize(c->st);
 	free_level_buf(c->lb);
@@ -1274,23 +1277,29 @@ int mclg_update_temperature(mclg_ctx *c, mclg_step_stats *st)
 	return MCLG_OK;
 }
 
-int mclg_output(mclg_ctx *c, const char *dir, int timestep)
+int mclg_output_async(mclg_ctx *c, const char *dir, int timestep, int flags)
+{
+	if (c == NULL || (flags & ~(MCLG_OUT_TEXT | MCLG_OUT_BINARY)) != 0)
+		return MCLG_BAD_INPUT;
+	if (flags == 0)
+		return MCLG_OK;
+	if (c->writer == NULL)
+		c->writer = writer_new();
+	return writer_submit(c->writer, c->st, &c->mesh.lev[c->fl], dir ? dir : c->cfg.data_dir, timestep, flags, c->T,
+	                     c->V, c->stress, c->vis, c->p, (size_t)c->L.nel, &c->sc->model_time);
+}
+
+int mclg_output_wait(mclg_ctx *c)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	const size_t nn = c->L.nno;
-	std::vector<double> T(nn), V(2 * nn), V0(nn), V1(nn), S(nn), vis(nn);
-	CK(cudaMemcpyAsync(T.data(), c->T, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-	CK(cudaMemcpyAsync(V.data(), c->V, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-	CK(cudaMemcpyAsync(S.data(), c->stress, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-	CK(cudaMemcpyAsync(vis.data(), c->vis, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-	CK(cudaStreamSynchronize(c->st));
-	for (size_t i = 0; i < nn; i++) {
-		V0[i] = V[2 * i];
-		V1[i] = V[2 * i + 1];
-	}
-	return mclg_write_output(dir ? dir : c->cfg.data_dir, timestep, &c->mesh.lev[c->fl], T.data(), V0.data(),
-	                         V1.data(), S.data(), vis.data());
+	return c->writer ? writer_wait(c->writer) : MCLG_OK;
+}
+
+int mclg_output(mclg_ctx *c, const char *dir, int timestep)
+{
+	int rc = mclg_output_async(c, dir, timestep, MCLG_OUT_TEXT);
+	return rc ? rc : mclg_output_wait(c);
 }
 
 int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
@@ -1316,7 +1325,7 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 		return rc;
 	CK(cudaEventRecord(c->ev[1], c->st));
 	if (write_output && c->cfg.save_spacing > 0 && c->timestep % c->cfg.save_spacing == 0) {
-		if ((rc = mclg_output(c, NULL, c->timestep)))
+		if ((rc = mclg_output_async(c, NULL, c->timestep, MCLG_OUT_TEXT)))
 			return rc;
 	}
 	CK(cudaEventRecord(c->ev[2], c->st));
@@ -2265,6 +2274,252 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 	mclg_destroy(n);
 	if (nel_out)
 		*nel_out = (size_t)c->L.nel;
+	return MCLG_OK;
+}
+
+// ---- checkpoint / restart ------------------------------------------------------
+// One binary file: a fixed header, the finest level's leaf start codes (the mesh
+// of any develop_mode or remeshed tree), then the fields in node layout and the
+// solver state a continued run reads: T, V, stress, d, p, the warm-start history
+// of the converged solvers, and the learned guess's switch-off counters.  A
+// 64-bit FNV-1a sum over everything before it closes the file.
+static const char kCkpMagic[8] = {'M', 'C', 'L', 'G', 'C', 'K', 'P', '1'};
+
+struct CkpHeader {
+	char magic[8];
+	int32_t version, level, min_level, nel, nno, neq, nleaves, timestep;
+	int32_t p_initialized, has_history, ghist, goff, gbad, git_prev, precision;
+	double model_time, length, height;
+};
+
+static uint64_t fnv1a(uint64_t h, const void *p, size_t n)
+{
+	const unsigned char *b = (const unsigned char *)p;
+	for (size_t i = 0; i < n; i++) {
+		h ^= b[i];
+		h *= 1099511628211ull;
+	}
+	return h;
+}
+
+struct CkpFile {
+	FILE *f;
+	uint64_t h;
+	bool ok;
+	bool put(const void *p, size_t n)
+	{
+		h = fnv1a(h, p, n);
+		ok = ok && fwrite(p, 1, n, f) == n;
+		return ok;
+	}
+	bool get(void *p, size_t n)
+	{
+		ok = ok && fread(p, 1, n, f) == n;
+		if (ok)
+			h = fnv1a(h, p, n);
+		return ok;
+	}
+};
+
+// (device pointer, bytes) of each array the file holds, in file order
+static int ckp_arrays(mclg_ctx *c, bool history, void **ptr, size_t *bytes)
+{
+	const size_t nn = c->L.nno, ne = c->L.nel;
+	int n = 0;
+	ptr[n] = c->T; bytes[n++] = nn * sizeof(double);
+	ptr[n] = c->V; bytes[n++] = nn * sizeof(double2);
+	ptr[n] = c->stress; bytes[n++] = nn * sizeof(double);
+	ptr[n] = c->d; bytes[n++] = nn * sizeof(double2);
+	ptr[n] = c->p; bytes[n++] = ne * sizeof(double);
+	if (history) {
+		ptr[n] = c->d_h2; bytes[n++] = nn * sizeof(double2);
+		ptr[n] = c->p_h2; bytes[n++] = ne * sizeof(double);
+	}
+	return n;
+}
+
+extern "C" int mclg_checkpoint_save(mclg_ctx *c, const char *path)
+{
+	if (c == NULL || path == NULL)
+		return MCLG_BAD_INPUT;
+	const mclg_level &H = c->mesh.lev[c->fl];
+	CkpHeader hd;
+	memset(&hd, 0, sizeof hd);
+	memcpy(hd.magic, kCkpMagic, sizeof hd.magic);
+	hd.version = 1;
+	hd.level = c->mesh.max_level;
+	hd.min_level = c->mesh.min_level;
+	hd.nel = H.nel;
+	hd.nno = H.nno;
+	hd.neq = H.neq;
+	hd.nleaves = H.nel;
+	hd.timestep = c->timestep;
+	hd.p_initialized = c->p_initialized;
+	hd.has_history = c->d_h1 != NULL;
+	hd.ghist = c->ghist;
+	hd.goff = c->goff;
+	hd.gbad = c->gbad;
+	hd.git_prev = c->git_prev;
+	hd.precision = c->cfg.precision;
+	hd.length = c->mesh.length;
+	hd.height = c->mesh.height;
+	CK(cudaMemcpyAsync(&hd.model_time, &c->sc->model_time, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	std::vector<int> leaves(H.nel);
+	for (int e = 0; e < H.nel; e++)
+		leaves[e] = H.Mcode[e] >> MCLG_LEVEL_BITS;
+	void *ptr[8];
+	size_t bytes[8];
+	const int na = ckp_arrays(c, hd.has_history, ptr, bytes);
+	FILE *f = fopen(path, "wb");
+	if (f == NULL) {
+		mclg_set_error("cannot write %s", path);
+		return MCLG_IO_ERROR;
+	}
+	CkpFile w = {f, 14695981039346656037ull, true};
+	w.put(&hd, sizeof hd);
+	w.put(leaves.data(), leaves.size() * sizeof(int));
+	std::vector<unsigned char> buf;
+	for (int i = 0; i < na && w.ok; i++) {
+		buf.resize(bytes[i]);
+		if (cudaMemcpyAsync(buf.data(), ptr[i], bytes[i], cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+		    cudaStreamSynchronize(c->st) != cudaSuccess) {
+			fclose(f);
+			return cuda_fail(cudaGetLastError(), "mclg_checkpoint_save");
+		}
+		w.put(buf.data(), bytes[i]);
+	}
+	const uint64_t sum = w.h;
+	w.ok = w.ok && fwrite(&sum, 1, sizeof sum, f) == sizeof sum;
+	if (fclose(f) != 0 || !w.ok) {
+		mclg_set_error("writing %s failed", path);
+		return MCLG_IO_ERROR;
+	}
+	return MCLG_OK;
+}
+
+// Reads the header and leaves; leaves may be NULL.
+static int ckp_open(const char *path, FILE **fp, CkpFile &r, CkpHeader &hd, std::vector<int> *leaves)
+{
+	FILE *f = fopen(path, "rb");
+	if (f == NULL) {
+		mclg_set_error("cannot read %s", path);
+		return MCLG_IO_ERROR;
+	}
+	r = {f, 14695981039346656037ull, true};
+	if (!r.get(&hd, sizeof hd) || memcmp(hd.magic, kCkpMagic, sizeof hd.magic) != 0 || hd.version != 1 ||
+	    hd.nleaves < 2 || hd.nno < 1 || hd.nel < 1) {
+		fclose(f);
+		mclg_set_error("%s is not a checkpoint of this engine", path);
+		return MCLG_BAD_INPUT;
+	}
+	std::vector<int> lv((size_t)hd.nleaves);
+	if (!r.get(lv.data(), lv.size() * sizeof(int))) {
+		fclose(f);
+		mclg_set_error("%s is truncated", path);
+		return MCLG_IO_ERROR;
+	}
+	if (leaves)
+		leaves->swap(lv);
+	*fp = f;
+	return MCLG_OK;
+}
+
+extern "C" int mclg_checkpoint_load(mclg_ctx *c, const char *path)
+{
+	if (c == NULL || path == NULL)
+		return MCLG_BAD_INPUT;
+	FILE *f = NULL;
+	CkpFile r;
+	CkpHeader hd;
+	std::vector<int> leaves;
+	int rc = ckp_open(path, &f, r, hd, &leaves);
+	if (rc)
+		return rc;
+	const mclg_level &H = c->mesh.lev[c->fl];
+	bool same = hd.level == c->mesh.max_level && hd.nel == H.nel && hd.nno == H.nno && hd.neq == H.neq &&
+	            hd.length == c->mesh.length && hd.height == c->mesh.height;
+	for (int e = 0; same && e < H.nel; e++)
+		same = leaves[e] == (H.Mcode[e] >> MCLG_LEVEL_BITS);
+	if (!same) {
+		fclose(f);
+		mclg_set_error("%s holds another mesh (%d elements at level %d; this model: %d at level %d)", path, hd.nel,
+		               hd.level - 1, H.nel, c->fl);
+		return MCLG_BAD_INPUT;
+	}
+	const bool hist = hd.has_history && c->d_h1 != NULL;
+	void *ptr[8];
+	size_t bytes[8];
+	const int na = ckp_arrays(c, hd.has_history != 0, ptr, bytes);
+	std::vector<std::vector<unsigned char>> data(na);
+	for (int i = 0; i < na; i++) {
+		data[i].resize(bytes[i]);
+		if (!r.get(data[i].data(), bytes[i]))
+			break;
+	}
+	uint64_t sum = 0;
+	const uint64_t want = r.h;
+	const bool tail = r.ok && fread(&sum, 1, sizeof sum, f) == sizeof sum;
+	fclose(f);
+	if (!tail || sum != want) {
+		mclg_set_error("%s is truncated or corrupt (checksum)", path);
+		return MCLG_IO_ERROR;
+	}
+	for (int i = 0; i < na; i++) {
+		if (i >= 5 && !hist)   // a history the model does not keep (warm_start != 3)
+			break;
+		CK(cudaMemcpyAsync(ptr[i], data[i].data(), bytes[i], cudaMemcpyHostToDevice, c->st));
+	}
+	CK(cudaMemcpyAsync(&c->sc->model_time, &hd.model_time, sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	c->timestep = hd.timestep;
+	c->p_initialized = hd.p_initialized;
+	if (c->d_h1 != NULL)
+		c->ghist = hist ? hd.ghist : 0;
+	c->goff = hd.goff;
+	c->gbad = hd.gbad;
+	c->git_prev = hd.git_prev;
+	return MCLG_OK;
+}
+
+extern "C" int mclg_get_time(mclg_ctx *c, int *timestep, double *model_time)
+{
+	if (c == NULL)
+		return MCLG_BAD_INPUT;
+	if (timestep)
+		*timestep = c->timestep;
+	if (model_time) {
+		CK(cudaMemcpyAsync(model_time, &c->sc->model_time, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+		CK(cudaStreamSynchronize(c->st));
+	}
+	return MCLG_OK;
+}
+
+extern "C" int mclg_restart(mclg_ctx **out, const mclg_config *cfg, const char *path)
+{
+	if (out == NULL || cfg == NULL || path == NULL)
+		return MCLG_BAD_INPUT;
+	*out = NULL;
+	FILE *f = NULL;
+	CkpFile r;
+	CkpHeader hd;
+	std::vector<int> leaves;
+	int rc = ckp_open(path, &f, r, hd, &leaves);
+	if (rc)
+		return rc;
+	fclose(f);
+	if (hd.level != cfg->level) {
+		mclg_set_error("%s was written with level=%d, the configuration has level=%d", path, hd.level, cfg->level);
+		return MCLG_BAD_INPUT;
+	}
+	mclg_ctx *c = NULL;
+	if ((rc = create_impl(&c, cfg, leaves.data(), (long)leaves.size())) != MCLG_OK)
+		return rc;
+	if ((rc = mclg_checkpoint_load(c, path)) != MCLG_OK) {
+		mclg_destroy(c);
+		return rc;
+	}
+	*out = c;
 	return MCLG_OK;
 }
 

@@ -82,6 +82,12 @@ int mclg_node_index(const mclg_level *L, int gid);
 /* Initial temperature on one level (Initial_condition.c:3-136, plus T_ini=-2). */
 int mclg_host_initial_temperature(const mclg_mesh *m, const mclg_config *cfg, int lev, double *T);
 
+/* the step's directory, and one of the five files of mclg_write_output (0 coord, 1 temperature,
+ * 2 stress, 3 viscosity, 4 velocity) */
+int mclg_output_dirs(const char *data_dir, int timestep);
+int mclg_write_output_file(const char *data_dir, int timestep, int which, const mclg_level *L,
+                           const double *T, const double *V0, const double *V1, const double *stress,
+                           const double *vis);
 /* Output.c:31-156 text files for one step. */
 int mclg_write_output(const char *data_dir, int timestep, const mclg_level *L,
                       const double *T, const double *V0, const double *V1,

@@ -66,6 +66,12 @@ int main(int argc, char **argv)
 		if (st.status == MCLG_NAN || st.status == MCLG_BREAKDOWN)
 			fprintf(stderr, "step %d: solver status: %s\n", ts, mclg_status_string(st.status));
 	}
+	rc = mclg_output_wait(ctx);   /* the last steps' files */
+	if (rc != MCLG_OK) {
+		fprintf(stderr, "output: %s: %s\n", mclg_status_string(rc), mclg_last_error());
+		mclg_destroy(ctx);
+		return 20 + rc;
+	}
 	fprintf(stderr, "%f seconds of CPU time used in total\n", now() - t0);
 	mclg_destroy(ctx);
 	return 0;

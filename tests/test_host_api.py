@@ -193,3 +193,15 @@ def test_cnn_create_without_device_reports_no_device():
     assert rc == api.NO_DEVICE
     assert L.mclg_cnn_create(C.byref(h), 8, 32, 1, 3, 0) == api.BAD_INPUT   # depth < 2
     assert L.mclg_cnn_load(C.byref(h), b"/nonexistent/net.bin") == api.IO_ERROR
+
+
+def test_restart_reads_the_file_before_the_device(tmp_path):
+    """mclg_restart checks the checkpoint file before it touches a device."""
+    L = api.lib()
+    c = Config.from_input(golden_input("cfg1_l5"))
+    h = C.c_void_p()
+    assert L.mclg_restart(C.byref(h), C.byref(c), str(tmp_path / "none.ckp").encode()) == api.IO_ERROR
+    junk = tmp_path / "junk.ckp"
+    junk.write_bytes(b"not a checkpoint" * 8)
+    assert L.mclg_restart(C.byref(h), C.byref(c), str(junk).encode()) == api.BAD_INPUT
+    assert not h
