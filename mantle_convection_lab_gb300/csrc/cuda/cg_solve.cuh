@@ -16,9 +16,6 @@
 
 namespace mclg {
 
-// Status bits written to StepScalars::status.
-constexpr int kStatCap = 1, kStatNan = 2, kStatBreakdown = 4;
-
 template <class Op>
 __device__ int cg_solve(cg::grid_group &g, GridRed &red, const Op &op, const double *__restrict__ b,
                         double *__restrict__ x, double *__restrict__ r, double *__restrict__ s,

@@ -1,0 +1,583 @@
+// Converged Stokes solve on quadtree meshes with hanging nodes; see k_qt.cuh.
+// One persistent cooperative kernel per time step.  Vectors are node layout
+// (both components of a node together); a primal vector stores its reduced
+// dofs and is read through the constraints (qt_val), a dual vector (operator
+// output, residual) is zero outside the reduced dofs.
+#include <math.h>
+#include "k_qt.cuh"
+
+namespace mclg {
+
+MCLG_SHAPE_UPLOAD(upload_shape_tables_qt)
+
+// ---- values through the constraints ----------------------------------------------
+// dof (2*node + component) of a primal vector: stored if reduced, the weighted
+// sum of its reduced dofs if constrained, 0 if fixed.
+template <class T, class X>
+__device__ __forceinline__ X qt_val(const QtLevel<T> &L, const X *__restrict__ xf, int dof)
+{
+	const unsigned char k = L.kind[dof];
+	if (k == 1)
+		return xf[dof];
+	X s = X(0);
+	if (k == 2)
+		for (int i = L.ex_off[dof]; i < L.ex_off[dof + 1]; i++)
+			s += (X)L.ex_w[i] * xf[L.ex_src[i]];
+	return s;
+}
+
+// Both rows of node j of K x~ (x~ the expanded x), with K in the level's TI
+// blocks or its FP64 blocks.
+template <class T, class K4, class X>
+__device__ __forceinline__ void qt_rows(const QtLevel<T> &L, const K4 *__restrict__ K, const X *__restrict__ xf, int j,
+                                        X &y0, X &y1)
+{
+	X s0 = X(0), s1 = X(0);
+	for (int k = 0; k < L.nbw; k++) {
+		const int B = L.nb[(size_t)k * L.nno + j];
+		const K4 kb = K[(size_t)k * L.nno + j];
+		const X x0 = qt_val(L, xf, 2 * B), x1 = qt_val(L, xf, 2 * B + 1);
+		s0 += (X)kb.x * x0 + (X)kb.y * x1;
+		s1 += (X)kb.z * x0 + (X)kb.w * x1;
+	}
+	y0 = s0;
+	y1 = s1;
+}
+
+// (C^T K C x) at both dofs of node A: the node's own rows plus the rows of
+// the constrained dofs whose expansion holds them; 0 outside reduced dofs.
+template <class T, class K4, class X>
+__device__ __forceinline__ void qt_op_node(const QtLevel<T> &L, const K4 *__restrict__ K, const X *__restrict__ xf,
+                                           int A, X &y0, X &y1)
+{
+	X y[2];
+	qt_rows(L, K, xf, A, y[0], y[1]);
+#pragma unroll
+	for (int c = 0; c < 2; c++) {
+		const int dof = 2 * A + c;
+		if (L.kind[dof] != 1) {
+			y[c] = X(0);
+			continue;
+		}
+		for (int i = L.fo_off[dof]; i < L.fo_off[dof + 1]; i++) {
+			const int h = L.fo_dof[i];
+			X h0, h1;
+			qt_rows(L, K, xf, h >> 1, h0, h1);
+			y[c] += (X)L.fo_w[i] * ((h & 1) ? h1 : h0);
+		}
+	}
+	y0 = y[0];
+	y1 = y[1];
+}
+
+// (C^T G p) at both dofs of node A (FP64, the finest level)
+template <class T>
+__device__ __forceinline__ void qt_g_node(const QtLevel<T> &Q, const DevLevel &L, const double *__restrict__ p, int A,
+                                          double &y0, double &y1)
+{
+	double y[2];
+	gmul_node(L, p, A, y[0], y[1]);
+#pragma unroll
+	for (int c = 0; c < 2; c++) {
+		const int dof = 2 * A + c;
+		if (Q.kind[dof] != 1) {
+			y[c] = 0.0;
+			continue;
+		}
+		for (int i = Q.fo_off[dof]; i < Q.fo_off[dof + 1]; i++) {
+			const int h = Q.fo_dof[i];
+			double h0, h1;
+			gmul_node(L, p, h >> 1, h0, h1);
+			y[c] += (double)Q.fo_w[i] * ((h & 1) ? h1 : h0);
+		}
+	}
+	y0 = y[0];
+	y1 = y[1];
+}
+
+// (G^T C u)_e of a primal vector u (flat, X) on the finest level
+template <class T, class X>
+__device__ __forceinline__ double qt_gt_elem(const QtLevel<T> &Q, const DevLevel &L, const X *__restrict__ uf, int e)
+{
+	double s = 0.0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		const int A = L.ienl[a * L.nel + e];
+		double g0, g1;
+		element_g(cS, L.dzh[e], L.dxh[e], a, g0, g1);
+		s += g0 * (double)qt_val(Q, uf, 2 * A);
+		s += g1 * (double)qt_val(Q, uf, 2 * A + 1);
+	}
+	return s;
+}
+
+// ---- the V-cycle (TI) -------------------------------------------------------------
+// One damped Jacobi sweep on the constrained operator: xo = xi + w D^-1 (b - A xi).
+template <class TI>
+__device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const typename Q2T<TI>::t *xi,
+                                         typename Q2T<TI>::t *xo, int tid, int nth)
+{
+	typedef typename Q2T<TI>::t V;
+	const TI *xf = reinterpret_cast<const TI *>(xi);
+	for (int A = tid; A < L.nno; A += nth) {
+		TI y0, y1;
+		qt_op_node(L, L.K, xf, A, y0, y1);
+		const V x = xi[A], b = L.b[A];
+		V o;
+		o.x = L.kind[2 * A] == 1 ? x.x + omega * L.invD[2 * A] * (b.x - y0) : TI(0);
+		o.y = L.kind[2 * A + 1] == 1 ? x.y + omega * L.invD[2 * A + 1] * (b.y - y1) : TI(0);
+		xo[A] = o;
+	}
+}
+
+// z = V-cycle(b) with b in the finest level's b; returns the buffer holding z.
+template <class TI>
+__device__ const typename Q2T<TI>::t *qt_vcycle(cg::grid_group &g, const QtHier<TI> &H, int tid, int nth)
+{
+	typedef typename Q2T<TI>::t V;
+	const int top = H.nlev - 1;
+	int cur[16];
+	for (int l = top; l >= 1; l--) {
+		const QtLevel<TI> &L = H.lv[l];
+		V *x0 = L.x[0];
+		for (int A = tid; A < L.nno; A += nth) {   // first sweep from zero: w D^-1 b
+			const V b = L.b[A];
+			V o;
+			o.x = H.omega * L.invD[2 * A] * b.x;
+			o.y = H.omega * L.invD[2 * A + 1] * b.y;
+			x0[A] = o;
+		}
+		cur[l] = 0;
+		g.sync();
+		for (int s = 1; s < H.smooth; s++) {
+			qt_sweep(L, H.omega, L.x[cur[l]], L.x[1 - cur[l]], tid, nth);
+			cur[l] = 1 - cur[l];
+			g.sync();
+		}
+		const TI *xf = reinterpret_cast<const TI *>(L.x[cur[l]]);
+		for (int A = tid; A < L.nno; A += nth) {
+			TI y0, y1;
+			qt_op_node(L, L.K, xf, A, y0, y1);
+			const V b = L.b[A];
+			V r;
+			r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
+			r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
+			L.r[A] = r;
+		}
+		g.sync();
+		const QtLevel<TI> &C = H.lv[l - 1];
+		const TI *rf = reinterpret_cast<const TI *>(L.r);
+		TI *cb = reinterpret_cast<TI *>(C.b);
+		for (int d = tid; d < 2 * C.nno; d += nth) {   // restriction: P^T by rows
+			TI s = TI(0);
+			for (int i = C.r_off[d]; i < C.r_off[d + 1]; i++)
+				s += C.r_w[i] * rf[C.r_src[i]];
+			cb[d] = s;
+		}
+		g.sync();
+	}
+	{   // coarsest level: the dense inverse on its reduced dofs
+		const QtLevel<TI> &C = H.lv[0];
+		const TI *bf = reinterpret_cast<const TI *>(C.b);
+		TI *xf = reinterpret_cast<TI *>(C.x[0]);
+		for (int i = tid; i < H.nc; i += nth) {
+			TI s = TI(0);
+			for (int j = 0; j < H.nc; j++)
+				s += H.cinv[(size_t)i * H.nc + j] * bf[H.cdof[j]];
+			xf[H.cdof[i]] = s;
+		}
+		cur[0] = 0;
+		g.sync();
+	}
+	for (int l = 1; l <= top; l++) {
+		const QtLevel<TI> &L = H.lv[l];
+		const TI *xc = reinterpret_cast<const TI *>(H.lv[l - 1].x[cur[l - 1]]);
+		TI *xf = reinterpret_cast<TI *>(L.x[cur[l]]);
+		for (int d = tid; d < 2 * L.nno; d += nth) {   // prolongation, added
+			if (L.p_off[d] == L.p_off[d + 1])
+				continue;
+			TI s = TI(0);
+			for (int i = L.p_off[d]; i < L.p_off[d + 1]; i++)
+				s += L.p_w[i] * xc[L.p_src[i]];
+			xf[d] += s;
+		}
+		g.sync();
+		for (int s = 0; s < H.smooth; s++) {
+			qt_sweep(L, H.omega, L.x[cur[l]], L.x[1 - cur[l]], tid, nth);
+			cur[l] = 1 - cur[l];
+			g.sync();
+		}
+	}
+	return H.lv[top].x[cur[top]];
+}
+
+// Dense inverse of the coarsest level's constrained operator on its reduced
+// dofs, columns from the operator applied to unit vectors (FP64), inverted
+// by Gauss-Jordan (the operator is SPD: no pivoting).  Block 0 only.
+template <class TI>
+__device__ void qt_coarse_build(const QtHier<TI> &H)
+{
+	const QtLevel<TI> &C = H.lv[0];
+	const int nc = H.nc, w2 = 2 * nc;
+	double *M = H.cwork, *e = H.cvec;
+	for (int k = threadIdx.x; k < nc * w2; k += blockDim.x)
+		M[k] = ((k % w2) == nc + k / w2) ? 1.0 : 0.0;
+	for (int k = threadIdx.x; k < 2 * C.nno; k += blockDim.x)
+		e[k] = 0.0;
+	__syncthreads();
+	for (int j = 0; j < nc; j++) {
+		if (threadIdx.x == 0)
+			e[H.cdof[j]] = 1.0;
+		__syncthreads();
+		for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+			const int d = H.cdof[i];
+			double y0, y1;
+			qt_op_node(C, C.K64, (const double *)e, d >> 1, y0, y1);
+			M[(size_t)i * w2 + j] = (d & 1) ? y1 : y0;
+		}
+		__syncthreads();
+		if (threadIdx.x == 0)
+			e[H.cdof[j]] = 0.0;
+		__syncthreads();
+	}
+	__shared__ double piv;
+	for (int k = 0; k < nc; k++) {
+		if (threadIdx.x == 0)
+			piv = M[(size_t)k * w2 + k];
+		__syncthreads();
+		for (int c = threadIdx.x; c < w2; c += blockDim.x)
+			M[(size_t)k * w2 + c] /= piv;
+		__syncthreads();
+		for (int r = threadIdx.x; r < nc; r += blockDim.x) {
+			if (r == k)
+				continue;
+			const double f = M[(size_t)r * w2 + k];
+			if (f != 0.0)
+				for (int c = 0; c < w2; c++)
+					M[(size_t)r * w2 + c] -= f * M[(size_t)k * w2 + c];
+		}
+		__syncthreads();
+	}
+	for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) {
+		const int r = k / nc, c = k - r * nc;
+		H.cinv[k] = (TI)M[(size_t)r * w2 + nc + c];
+	}
+	__syncthreads();
+}
+
+// ---- FP64 residual and the preconditioner ------------------------------------------
+// R = [C^T (F - K d - G p) ; G^T C d] (FP64); rs = |R_m|^2, |R_c|^2, |C^T F|^2.
+template <class TI>
+__device__ void qt_residual(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, const double2 *d, const double *p,
+                            double (&rs)[3], int tid, int nth)
+{
+	const DevLevel &L = a.L;
+	const QtLevel<TI> &Q = a.H.lv[a.H.nlev - 1];
+	const double *df = reinterpret_cast<const double *>(d);
+	const double *Ff = reinterpret_cast<const double *>(a.F);
+	rs[0] = rs[1] = rs[2] = 0.0;
+	for (int A = tid; A < L.nno; A += nth) {
+		double k0, k1, g0, g1;
+		qt_op_node(Q, Q.K64, df, A, k0, k1);
+		qt_g_node(Q, L, p, A, g0, g1);
+		double f[2] = {0.0, 0.0};
+		for (int c = 0; c < 2; c++) {   // C^T F
+			const int dof = 2 * A + c;
+			if (Q.kind[dof] != 1)
+				continue;
+			f[c] = Ff[dof];
+			for (int i = Q.fo_off[dof]; i < Q.fo_off[dof + 1]; i++)
+				f[c] += (double)Q.fo_w[i] * Ff[Q.fo_dof[i]];
+		}
+		const double2 r = make_double2(Q.kind[2 * A] == 1 ? f[0] - k0 - g0 : 0.0,
+		                               Q.kind[2 * A + 1] == 1 ? f[1] - k1 - g1 : 0.0);
+		a.R[A] = r;
+		rs[0] += r.x * r.x + r.y * r.y;
+		rs[2] += f[0] * f[0] + f[1] * f[1];
+	}
+	for (int e = tid; e < L.nel; e += nth) {
+		const double c = qt_gt_elem(Q, L, df, e);
+		a.Rc[e] = c;
+		rs[1] += c * c;
+	}
+	grid_reduce<3>(g, red, rs, 0u);
+}
+
+// z = M^-1 v, M = diag(V-cycle, BAB); returns <z, v>.
+template <class TI>
+__device__ double qt_precond(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, const double2 *vu, const double *vp,
+                             typename Q2T<TI>::t *zu, double *zp, int tid, int nth)
+{
+	typedef typename Q2T<TI>::t V;
+	const QtHier<TI> &H = a.H;
+	const QtLevel<TI> &Q = H.lv[H.nlev - 1];
+	for (int A = tid; A < Q.nno; A += nth) {
+		const double2 v = vu[A];
+		V w;
+		w.x = (TI)v.x;
+		w.y = (TI)v.y;
+		Q.b[A] = w;
+	}
+	g.sync();
+	const V *x = qt_vcycle(g, H, tid, nth);
+	double dot[1] = {0.0};
+	for (int A = tid; A < Q.nno; A += nth) {
+		const V z = x[A];
+		zu[A] = z;
+		const double2 v = vu[A];
+		dot[0] += (double)z.x * v.x + (double)z.y * v.y;
+	}
+	for (int e = tid; e < a.L.nel; e += nth) {
+		const double z = vp[e] / a.bab[e];
+		zp[e] = z;
+		dot[0] += z * vp[e];
+	}
+	grid_reduce<1>(g, red, dot, 0u);
+	return dot[0];
+}
+
+// Correction solve by preconditioned MINRES (Elman, Silvester and Wathen,
+// "Finite Elements and Fast Iterative Solvers", Alg. 4.1) on the constrained
+// system [C^T K C, C^T G; G^T C, 0][x_u; x_p] = [R_m; -R_c] from zero; K in TI,
+// G in FP64, Lanczos and direction vectors FP64; x into a.dd, a.dpv.
+template <class TI>
+__device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, double rtol, int maxit, int *status,
+                         int tid, int nth)
+{
+	typedef typename Q2T<TI>::t V;
+	const DevLevel &L = a.L;
+	const QtLevel<TI> &Q = a.H.lv[a.H.nlev - 1];
+	const int nn = L.nno, ne = L.nel;
+	double2 *vu[2] = {a.mv[0], a.mv[1]}, *wu[2] = {a.mw[0], a.mw[1]};
+	double *vp[2] = {a.mvp[0], a.mvp[1]}, *zp[2] = {a.mzp[0], a.mzp[1]}, *wp[2] = {a.mwp[0], a.mwp[1]};
+	V *zu[2] = {a.mz[0], a.mz[1]};
+	const double2 zero2 = make_double2(0.0, 0.0);
+	for (int A = tid; A < nn; A += nth) {
+		vu[0][A] = a.R[A];
+		vu[1][A] = zero2;
+		wu[0][A] = zero2;
+		wu[1][A] = zero2;
+		a.dd[A] = zero2;
+	}
+	for (int e = tid; e < ne; e += nth) {
+		vp[0][e] = -a.Rc[e];
+		vp[1][e] = 0.0;
+		wp[0][e] = 0.0;
+		wp[1][e] = 0.0;
+		a.dpv[e] = 0.0;
+	}
+	g.sync();
+	double gam2 = qt_precond(g, red, a, vu[0], vp[0], zu[0], zp[0], tid, nth);
+	if (!(gam2 > 0.0))
+		return 0;
+	double gam = sqrt(gam2), gam_prev = 1.0;
+	const double eta0 = gam;
+	double eta = gam, c_prev = 1.0, c_cur = 1.0, s_prev = 0.0, s_cur = 0.0;
+	int cv = 0, cw = 0, it = 0;
+	while (it < maxit) {
+		const TI *zf = reinterpret_cast<const TI *>(zu[cv]);
+		double dl[1] = {0.0};
+		for (int A = tid; A < nn; A += nth) {
+			TI k0, k1;
+			double g0, g1;
+			qt_op_node(Q, Q.K, zf, A, k0, k1);
+			qt_g_node(Q, L, zp[cv], A, g0, g1);
+			const double2 az = make_double2((double)k0 + g0, (double)k1 + g1);
+			a.Kd[A] = az;
+			const V z = zu[cv][A];
+			dl[0] += az.x * (double)z.x + az.y * (double)z.y;
+		}
+		for (int e = tid; e < ne; e += nth) {
+			const double t = qt_gt_elem(Q, L, zf, e);
+			a.Ahp[e] = t;
+			dl[0] += t * zp[cv][e];
+		}
+		grid_reduce<1>(g, red, dl, 0u);
+		const double delta = dl[0] / (gam * gam);
+		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
+		for (int A = tid; A < nn; A += nth) {
+			const double2 az = a.Kd[A], v = vu[cv][A], vo = vu[1 - cv][A];
+			vu[1 - cv][A] = make_double2(az.x * ig - dg * v.x - gg * vo.x, az.y * ig - dg * v.y - gg * vo.y);
+		}
+		for (int e = tid; e < ne; e += nth)
+			vp[1 - cv][e] = a.Ahp[e] * ig - dg * vp[cv][e] - gg * vp[1 - cv][e];
+		g.sync();
+		const double gn2 = qt_precond(g, red, a, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv], tid, nth);
+		const double gam_next = sqrt(fmax(gn2, 0.0));
+		const double a0 = c_cur * delta - c_prev * s_cur * gam;
+		const double a1 = sqrt(a0 * a0 + gam_next * gam_next);
+		const double a2 = s_cur * delta + c_prev * c_cur * gam;
+		const double a3 = s_prev * gam;
+		if (!(a1 > 0.0) || !isfinite(a1)) {
+			if (!isfinite(a1) && tid == 0)
+				atomicOr(status, kStatNan);
+			break;
+		}
+		const double c_next = a0 / a1, s_next = gam_next / a1;
+		const double ia1 = 1.0 / a1, step = c_next * eta;
+		for (int A = tid; A < nn; A += nth) {
+			const V z = zu[cv][A];
+			const double2 wo = wu[1 - cw][A], w = wu[cw][A];
+			const double2 wn = make_double2(((double)z.x * ig - a3 * wo.x - a2 * w.x) * ia1,
+			                                ((double)z.y * ig - a3 * wo.y - a2 * w.y) * ia1);
+			wu[1 - cw][A] = wn;
+			double2 x = a.dd[A];
+			x.x += step * wn.x;
+			x.y += step * wn.y;
+			a.dd[A] = x;
+		}
+		for (int e = tid; e < ne; e += nth) {
+			const double wn = (zp[cv][e] * ig - a3 * wp[1 - cw][e] - a2 * wp[cw][e]) * ia1;
+			wp[1 - cw][e] = wn;
+			a.dpv[e] += step * wn;
+		}
+		eta = -s_next * eta;
+		it++;
+		cv = 1 - cv;
+		cw = 1 - cw;
+		gam_prev = gam;
+		gam = gam_next;
+		c_prev = c_cur;
+		c_cur = c_next;
+		s_prev = s_cur;
+		s_cur = s_next;
+		if (!isfinite(eta)) {
+			if (tid == 0)
+				atomicOr(status, kStatNan);
+			break;
+		}
+		if (!(fabs(eta) > rtol * eta0) || !(gam > 0.0))
+			break;
+		g.sync();
+	}
+	g.sync();
+	return it;
+}
+
+template <class TI>
+__global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
+{
+	typedef typename V4T<TI>::t K4;
+	cg::grid_group g = cg::this_grid();
+	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const QtHier<TI> &H = a.H;
+	const DevLevel &L = a.L;
+	GridRed red = a.red;
+	int *status = &a.sc->status;
+
+	// -- per step: every level's operator in TI and its constrained diagonal
+	for (int l = 0; l < H.nlev; l++) {
+		const QtLevel<TI> &Q = H.lv[l];
+		const size_t nk = (size_t)Q.nbw * Q.nno;
+		for (size_t k = tid; k < nk; k += nth) {
+			const double4 v = Q.K64[k];
+			K4 t;
+			t.x = (TI)v.x;
+			t.y = (TI)v.y;
+			t.z = (TI)v.z;
+			t.w = (TI)v.w;
+			Q.K[k] = t;
+		}
+		for (int dof = tid; dof < 2 * Q.nno; dof += nth) {
+			double D = 0.0;
+			for (int i = Q.dg_off[dof]; i < Q.dg_off[dof + 1]; i++) {
+				const double4 kb = Q.K64[(size_t)Q.dg_slot[i] * Q.nno + Q.dg_node[i]];
+				D += Q.dg_w[i] * ((dof & 1) ? kb.w : kb.x);
+			}
+			Q.invD[dof] = Q.kind[dof] == 1 && D > 0.0 ? (TI)(1.0 / D) : TI(0);
+		}
+	}
+	g.sync();
+	if (blockIdx.x == 0)
+		qt_coarse_build(H);
+	g.sync();
+
+	int refine = 0, minres_total = 0, vcycles = 0, capped = 0;
+	double res_m = 0.0, res_c = 0.0;
+	while (true) {
+		double rs[3];
+		qt_residual(g, red, a, a.d, a.p, rs, tid, nth);
+		const double fnorm = sqrt(rs[2]);
+		res_m = sqrt(rs[0]) / fnorm;
+		res_c = sqrt(rs[1]) / fnorm;
+		const double res = sqrt(rs[0] + rs[1]) / fnorm;
+		if (!isfinite(res)) {
+			if (tid == 0)
+				atomicOr(status, kStatNan);
+			break;
+		}
+		if (!(res >= a.rtol))
+			break;
+		if (refine >= a.max_refine) {
+			capped = 1;
+			break;
+		}
+		refine++;
+		// far from the target a pass reduces by 1e-2, close to it by what is
+		// left (factor 2 margin), not below outer_rtol
+		const double prt = res > 1e4 * a.rtol ? 1e-2 : fmax(a.outer_rtol, 0.5 * a.rtol / res);
+		const int it = qt_minres(g, red, a, prt, a.max_outer, status, tid, nth);
+		minres_total += it;
+		vcycles += it + 1;
+		for (int A = tid; A < L.nno; A += nth) {
+			const double2 c = a.dd[A];
+			double2 v = a.d[A];
+			v.x += c.x;
+			v.y += c.y;
+			a.d[A] = v;
+		}
+		for (int e = tid; e < L.nel; e += nth)
+			a.p[e] += a.dpv[e];
+		g.sync();
+	}
+	if (capped && tid == 0)
+		atomicOr(status, kStatCap);
+	// the hanging nodes' values, and the velocity with its boundary values (v_to_nodes)
+	const QtLevel<TI> &Q = H.lv[H.nlev - 1];
+	double *df = reinterpret_cast<double *>(a.d);
+	for (int A = tid; A < L.nno; A += nth) {
+		double v[2];
+		for (int c = 0; c < 2; c++)
+			v[c] = qt_val(Q, (const double *)df, 2 * A + c);
+		a.V[A] = make_double2(vfree(L, A, 0) ? v[0] : L.vbcval[A], vfree(L, A, 1) ? v[1] : L.vbcval[L.nno + A]);
+	}
+	g.sync();
+	for (int A = tid; A < L.nno; A += nth)
+		for (int c = 0; c < 2; c++)
+			if (Q.kind[2 * A + c] == 2)
+				df[2 * A + c] = vfree(L, A, c) ? (c ? a.V[A].y : a.V[A].x) : 0.0;
+	if (tid == 0) {
+		StepScalars *sc = a.sc;
+		sc->uzawa_cycles = minres_total;
+		sc->cg_cycles = vcycles;
+		sc->refine_passes = refine;
+		sc->res_m = res_m;
+		sc->res_c = res_c;
+		sc->dv = 0.0;
+		sc->dp = 0.0;
+	}
+}
+
+// linear extrapolation of the last two solutions: x = 2 x1 - x2
+__global__ void __launch_bounds__(kBlock) k_qt_extrapolate(int n2, int ne, const double *d1, const double *d2,
+                                                           const double *p1, const double *p2, double *d, double *p)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n2)
+		d[i] = 2.0 * d1[i] - d2[i];
+	if (i < ne)
+		p[i] = 2.0 * p1[i] - p2[i];
+}
+
+// coarse-level viscosity: the finer level's value at the same node
+__global__ void __launch_bounds__(kBlock) k_qt_inject(int n, const int *map, const double *src, double *dst)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n)
+		dst[i] = src[map[i]];
+}
+
+void *qt_kernel(int fp64) { return fp64 ? (void *)k_stokes_qt<double> : (void *)k_stokes_qt<float>; }
+
+}  // namespace mclg

@@ -30,42 +30,6 @@ __device__ __forceinline__ void kmul_node(const DevLevel &L, const double4 *__re
 	y1 = vfree(L, A, 1) ? s1 : 0.0;
 }
 
-// G p at node A (G_prod_p, Solver.c:569-591): row entries in element order.
-__device__ __forceinline__ void gmul_node(const DevLevel &L, const double *__restrict__ p, int A,
-                                          double &y0, double &y1)
-{
-	double s0 = 0.0, s1 = 0.0;
-	for (int k = 0; k < L.p2n_cnt[A]; k++) {
-		const int e = L.p2n_el[k * L.nno + A], a = L.p2n_a[k * L.nno + A];
-		double g0, g1;
-		element_g(cS, L.dzh[e], L.dxh[e], a, g0, g1);
-		s0 += g0 * p[e];
-		s1 += g1 * p[e];
-	}
-	y0 = vfree(L, A, 0) ? s0 : 0.0;
-	y1 = vfree(L, A, 1) ? s1 : 0.0;
-}
-
-// (G^T u)_e (GT_prod_d, Solver.c:645-666): the element's free dofs in
-// ascending equation order.
-__device__ __forceinline__ double gtmul_elem(const DevLevel &L, const double2 *__restrict__ u, int e)
-{
-	double s = 0.0;
-#pragma unroll
-	for (int c = 0; c < 4; c++) {
-		const int a = kSortedCorner[c];
-		const int A = L.ienl[a * L.nel + e];
-		double g0, g1;
-		element_g(cS, L.dzh[e], L.dxh[e], a, g0, g1);
-		const double2 ua = u[A];
-		if (vfree(L, A, 0))
-			s += g0 * ua.x;
-		if (vfree(L, A, 1))
-			s += g1 * ua.y;
-	}
-	return s;
-}
-
 // Hanging-node overwrite (enforce_constrain_veq, Solver.c:1368-1482):
 // x_h = (x_c0 + x_c1)/2 per component, a Dirichlet parent contributing its
 // BC value.  A Dirichlet component of the hanging node itself is left alone

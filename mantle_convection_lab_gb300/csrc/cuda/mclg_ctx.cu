@@ -9,6 +9,7 @@
 #include "k_mg.cuh"
 #include "cnn.cuh"
 #include "mclg_writer.cuh"
+#include "k_qt.cuh"
 #include "../host/mclg_host.h"
 
 namespace mclg {
@@ -23,6 +24,10 @@ __global__ void k_buoy_vis(DevLevel L, const double *T, double Ra, const double 
 __global__ void k_assemble_stokes(DevLevel L, const double *vis, const double *buoy, double4 *K, double2 *F,
                                   double2 *Kdiag, int withK);
 void upload_shape_tables_mg(const ShapeTables &s, cudaStream_t st);
+void upload_shape_tables_qt(const ShapeTables &s, cudaStream_t st);
+__global__ void k_qt_extrapolate(int n2, int ne, const double *d1, const double *d2, const double *p1, const double *p2,
+                                 double *d, double *p);
+__global__ void k_qt_inject(int n, const int *map, const double *src, double *dst);
 void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st);
 void *stokes_mg_kernel(int fp64);
 void *stokes_mg_batch_kernel(int fp64);
@@ -104,12 +109,20 @@ struct mclg_ctx {
 	// the reference's own inner solvers (solver="gs" / "mg"): levels ref_lo..fl
 	int ref_kind, ref_lo;
 	RefMG *ref_dev;
-	DevLevelBuf ref_lb[MCLG_MAX_LEVEL];   // coarser levels (the finest is lb)
-	DevLevel ref_L[MCLG_MAX_LEVEL];
-	double *ref_T[MCLG_MAX_LEVEL], *ref_vis[MCLG_MAX_LEVEL];
-	double4 *ref_K[MCLG_MAX_LEVEL];
-	void **ref_ptr;
+	// levels below the finest resident on the device (solver="mg", and the
+	// converged solver on refined meshes), indexed from the coarsest used
+	DevLevelBuf lvl_lb[MCLG_MAX_LEVEL];   // (the finest is lb)
+	DevLevel lvl_L[MCLG_MAX_LEVEL];
+	double *lvl_T[MCLG_MAX_LEVEL], *lvl_vis[MCLG_MAX_LEVEL], *lvl_buoy[MCLG_MAX_LEVEL];
+	double4 *lvl_K[MCLG_MAX_LEVEL];
+	double2 *lvl_F[MCLG_MAX_LEVEL], *lvl_Kd[MCLG_MAX_LEVEL];
+	int *lvl_map[MCLG_MAX_LEVEL];         // node -> the same node one level up
+	void **ref_ptr;                       // device allocations of the above, freed together
 	int ref_nptr, ref_cap;
+	// converged solver on refined meshes (precision 1/2 with hanging nodes)
+	int qt_on, coop_qt;
+	QtArgs<float> qtf;
+	QtArgs<double> qtd;
 	OutWriter *writer;            // asynchronous output, created on first use
 };
 
@@ -436,7 +449,7 @@ static int check_launch(mclg_ctx *c, const char *what)
 	return MCLG_OK;
 }
 
-static cudaError_t ref_track(mclg_ctx *c, void *p)
+static cudaError_t dev_track(mclg_ctx *c, void *p)
 {
 	if (c->ref_nptr == c->ref_cap) {
 		const int cap = c->ref_cap ? 2 * c->ref_cap : 64;
@@ -453,23 +466,23 @@ static cudaError_t ref_track(mclg_ctx *c, void *p)
 }
 
 template <class T>
-static cudaError_t ref_zeros(mclg_ctx *c, T **p, size_t n)
+static cudaError_t dev_zeros(mclg_ctx *c, T **p, size_t n)
 {
 	cudaError_t e = dalloc(p, n);
 	if (e != cudaSuccess)
 		return e;
-	if ((e = ref_track(c, *p)) != cudaSuccess)
+	if ((e = dev_track(c, *p)) != cudaSuccess)
 		return e;
 	return cudaMemsetAsync(*p, 0, (n + 1) * sizeof(T), c->st);
 }
 
 template <class T>
-static cudaError_t ref_upload(mclg_ctx *c, T **p, const std::vector<T> &h)
+static cudaError_t dev_upload(mclg_ctx *c, T **p, const std::vector<T> &h)
 {
 	cudaError_t e = upload(p, h.data(), h.size(), c->st);
 	if (e != cudaSuccess)
 		return e;
-	return ref_track(c, *p);
+	return dev_track(c, *p);
 }
 
 // Node-layout dof (2*node + direction) of every equation of a level.
@@ -514,19 +527,19 @@ static int ref_setup(mclg_ctx *c)
 	h.fine_it = f.mg_finest_iteration;
 	h.coarse_it = f.mg_coarse_iteration;
 	double *zeros_gnoz = NULL;
-	CK(ref_zeros(c, &zeros_gnoz, (size_t)m.gnoz));
+	CK(dev_zeros(c, &zeros_gnoz, (size_t)m.gnoz));
 	for (int lev = lo; lev <= top; lev++) {
 		const int k = lev - lo;
 		const mclg_level &H = m.lev[lev];
 		const size_t nn = H.nno;
 		RefLevel &R = h.lev[k];
 		if (lev == top) {
-			c->ref_L[k] = c->L;
+			c->lvl_L[k] = c->L;
 			R.K = c->K;
 		} else {
-			DevLevel &L = c->ref_L[k];
+			DevLevel &L = c->lvl_L[k];
 			memset(&L, 0, sizeof L);
-			int rc = upload_level_into(c, lev, c->ref_lb[k], L);
+			int rc = upload_level_into(c, lev, c->lvl_lb[k], L);
 			if (rc != MCLG_OK)
 				return rc;
 			std::vector<double> T(nn);
@@ -534,24 +547,24 @@ static int ref_setup(mclg_ctx *c)
 				return rc;
 			double *buoy = NULL;
 			double2 *F = NULL, *Kd = NULL;
-			CK(ref_upload(c, &c->ref_T[k], T));
-			CK(ref_zeros(c, &c->ref_vis[k], nn));
-			CK(ref_zeros(c, &buoy, nn));
-			CK(ref_zeros(c, &c->ref_K[k], (size_t)H.nbw * nn));
-			CK(ref_zeros(c, &F, nn));
-			CK(ref_zeros(c, &Kd, nn));
+			CK(dev_upload(c, &c->lvl_T[k], T));
+			CK(dev_zeros(c, &c->lvl_vis[k], nn));
+			CK(dev_zeros(c, &buoy, nn));
+			CK(dev_zeros(c, &c->lvl_K[k], (size_t)H.nbw * nn));
+			CK(dev_zeros(c, &F, nn));
+			CK(dev_zeros(c, &Kd, nn));
 			// viscosity of the level's T; the buoyancy (Ra = 0 here) only feeds F, which no level below the finest uses
-			k_buoy_vis<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->ref_T[k], 0.0, zeros_gnoz, f.A, f.refT,
+			k_buoy_vis<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->lvl_T[k], 0.0, zeros_gnoz, f.A, f.refT,
 			                                                 f.lower_mantle_jump, f.vis_min, f.vis_max, buoy,
-			                                                 c->ref_vis[k]);
+			                                                 c->lvl_vis[k]);
 			if ((rc = check_launch(c, "k_buoy_vis")))
 				return rc;
-			k_assemble_stokes<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->ref_vis[k], buoy, c->ref_K[k], F, Kd, 1);
+			k_assemble_stokes<<<blocks_for(nn), kBlock, 0, c->st>>>(L, c->lvl_vis[k], buoy, c->lvl_K[k], F, Kd, 1);
 			if ((rc = check_launch(c, "k_assemble_stokes")))
 				return rc;
-			R.K = c->ref_K[k];
+			R.K = c->lvl_K[k];
 		}
-		const DevLevel &L = c->ref_L[k];
+		const DevLevel &L = c->lvl_L[k];
 		R.nno = (int)nn;
 		R.nbw = H.nbw;
 		R.nb = L.nb;
@@ -572,12 +585,12 @@ static int ref_setup(mclg_ctx *c)
 		for (size_t A = 0; A < nn; A++)
 			order[fill[wave[A]]++] = (int)A;
 		R.nwave = nw;
-		CK(ref_upload(c, (int **)&R.wave, order));
-		CK(ref_upload(c, (int **)&R.wave_off, off));
-		CK(ref_zeros(c, &R.err, nn));
-		CK(ref_zeros(c, &R.rhs, nn));
-		CK(ref_zeros(c, &R.res, nn));
-		CK(ref_zeros(c, &R.xt, nn));
+		CK(dev_upload(c, (int **)&R.wave, order));
+		CK(dev_upload(c, (int **)&R.wave_off, off));
+		CK(dev_zeros(c, &R.err, nn));
+		CK(dev_zeros(c, &R.rhs, nn));
+		CK(dev_zeros(c, &R.res, nn));
+		CK(dev_zeros(c, &R.xt, nn));
 		// interp_error's map from the level below (Connection.c:708-930)
 		std::vector<int> itp_n(2 * nn, 0), itp_src(8 * nn, -1);
 		if (k > 0) {
@@ -600,8 +613,8 @@ static int ref_setup(mclg_ctx *c)
 					}
 				}
 		}
-		CK(ref_upload(c, (int **)&R.itp_n, itp_n));
-		CK(ref_upload(c, (int **)&R.itp_src, itp_src));
+		CK(dev_upload(c, (int **)&R.itp_n, itp_n));
+		CK(dev_upload(c, (int **)&R.itp_src, itp_src));
 		// project_res's map to the level above (Connection.c:1051-1251)
 		std::vector<int> prj(2 * nn, -1);
 		if (lev < top) {
@@ -621,11 +634,11 @@ static int ref_setup(mclg_ctx *c)
 					prj[(size_t)d * nn + A] = up_dof[up_eq[el]];
 				}
 		}
-		CK(ref_upload(c, (int **)&R.prj, prj));
+		CK(dev_upload(c, (int **)&R.prj, prj));
 	}
 	void *p = NULL;
 	CK(cudaMalloc(&p, sizeof(RefMG)));
-	CK(ref_track(c, p));
+	CK(dev_track(c, p));
 	c->ref_dev = (RefMG *)p;
 	CK(cudaMemcpyAsync(c->ref_dev, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
 	CK(cudaStreamSynchronize(c->st));
@@ -639,6 +652,232 @@ static bool coarse_level(const mclg_ctx *c, int lev, int *k)
 		return false;
 	*k = lev - c->ref_lo;
 	return true;
+}
+
+// ---- converged solver on refined meshes ------------------------------------------
+template <class TW, class TS>
+static cudaError_t dev_upload_cast(mclg_ctx *c, TW **p, const TS *h, size_t n)
+{
+	std::vector<TW> v(n ? n : 1);
+	for (size_t i = 0; i < n; i++)
+		v[i] = (TW)h[i];
+	return dev_upload(c, p, v);
+}
+
+template <class T>
+static cudaError_t dev_upload_n(mclg_ctx *c, T **p, const T *h, size_t n)
+{
+	std::vector<T> v(h, h + n);
+	if (v.empty())
+		v.push_back(T());
+	return dev_upload(c, p, v);
+}
+
+// Levels mg_min_level .. finest of the mesh, their constrained-space lists
+// (mclg_qtmg.c), the TI operators and work vectors, the coarsest level's
+// dense inverse and the FP64 MINRES vectors.
+template <class TI>
+static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
+{
+	typedef typename Q2T<TI>::t V;
+	typedef typename V4T<TI>::t K4;
+	const mclg_mesh &m = c->mesh;
+	const mclg_config &f = c->cfg;
+	const int top = c->fl, lo = m.min_level, nlev = top - lo + 1;
+	if (nlev < 2 || nlev > 16) {
+		mclg_set_error("the refined-mesh solver needs 2..16 levels (mg_min_level %d, finest %d)", lo, top);
+		return MCLG_BAD_INPUT;
+	}
+	for (int l = lo; l <= top; l++)
+		for (int i = 0; i < 2 * m.lev[l].nno; i++)
+			if (m.lev[l].v_bc[i] == 'V' && m.lev[l].v_bc_val[i] != 0.0) {
+				mclg_set_error("the refined-mesh solver takes homogeneous velocity boundary values only");
+				return MCLG_BAD_INPUT;
+			}
+	std::vector<mclg_qt_level> q((size_t)nlev);
+	int rc = mclg_qt_build(&m, lo, q.data());
+	struct Free {
+		std::vector<mclg_qt_level> &q;
+		~Free()
+		{
+			for (auto &x : q)
+				mclg_qt_free(&x);
+		}
+	} guard{q};
+	if (rc != MCLG_OK)
+		return rc;
+	memset(&a, 0, sizeof a);
+	a.L = c->L;
+	a.F = c->F;
+	a.bab = c->bab;
+	a.d = c->d;
+	a.V = c->V;
+	a.p = c->p;
+	QtHier<TI> &H = a.H;
+	H.nlev = nlev;
+	H.smooth = f.mg_smooth > 0 ? f.mg_smooth : 1;
+	H.omega = (TI)f.mg_omega;
+	for (int l = lo; l <= top; l++) {
+		const int k = l - lo;
+		const mclg_level &ML = m.lev[l];
+		const mclg_qt_level &S = q[k];
+		QtLevel<TI> &Q = H.lv[k];
+		const size_t nn = ML.nno, nk = (size_t)ML.nbw * nn;
+		if (l == top) {
+			Q.nb = c->L.nb;
+			Q.K64 = c->K;
+		} else {
+			DevLevel &L = c->lvl_L[k];
+			memset(&L, 0, sizeof L);
+			if ((rc = upload_level_into(c, l, c->lvl_lb[k], L)) != MCLG_OK)
+				return rc;
+			CK(dev_zeros(c, &c->lvl_K[k], nk));
+			CK(dev_zeros(c, &c->lvl_vis[k], nn));
+			CK(dev_zeros(c, &c->lvl_buoy[k], nn));
+			CK(dev_zeros(c, &c->lvl_F[k], nn));
+			CK(dev_zeros(c, &c->lvl_Kd[k], nn));
+			CK(dev_upload_n(c, &c->lvl_map[k], S.node_map, nn));
+			Q.nb = L.nb;
+			Q.K64 = c->lvl_K[k];
+		}
+		Q.nno = (int)nn;
+		Q.nbw = ML.nbw;
+		K4 *Kt = NULL;
+		TI *invD = NULL;
+		CK(dev_zeros(c, &Kt, nk));
+		CK(dev_zeros(c, &invD, 2 * nn));
+		Q.K = Kt;
+		Q.invD = invD;
+		const size_t nd = 2 * nn;
+		CK(dev_upload_n(c, (unsigned char **)&Q.kind, S.kind, nd));
+		CK(dev_upload_n(c, (int **)&Q.ex_off, S.ex_off, nd + 1));
+		CK(dev_upload_n(c, (int **)&Q.ex_src, S.ex_src, (size_t)S.n_ex));
+		CK(dev_upload_cast(c, (TI **)&Q.ex_w, S.ex_w, (size_t)S.n_ex));
+		CK(dev_upload_n(c, (int **)&Q.fo_off, S.fo_off, nd + 1));
+		CK(dev_upload_n(c, (int **)&Q.fo_dof, S.fo_dof, (size_t)S.n_fo));
+		CK(dev_upload_cast(c, (TI **)&Q.fo_w, S.fo_w, (size_t)S.n_fo));
+		CK(dev_upload_n(c, (int **)&Q.dg_off, S.dg_off, nd + 1));
+		CK(dev_upload_n(c, (int **)&Q.dg_node, S.dg_node, (size_t)S.n_dg));
+		CK(dev_upload_n(c, (int **)&Q.dg_slot, S.dg_slot, (size_t)S.n_dg));
+		CK(dev_upload_n(c, (double **)&Q.dg_w, S.dg_w, (size_t)S.n_dg));
+		if (k > 0) {
+			CK(dev_upload_n(c, (int **)&Q.p_off, S.p_off, nd + 1));
+			CK(dev_upload_n(c, (int **)&Q.p_src, S.p_src, (size_t)S.n_p));
+			CK(dev_upload_cast(c, (TI **)&Q.p_w, S.p_w, (size_t)S.n_p));
+		}
+		if (l < top) {
+			CK(dev_upload_n(c, (int **)&Q.r_off, S.r_off, nd + 1));
+			CK(dev_upload_n(c, (int **)&Q.r_src, S.r_src, (size_t)S.n_r));
+			CK(dev_upload_cast(c, (TI **)&Q.r_w, S.r_w, (size_t)S.n_r));
+		}
+		for (int i = 0; i < 2; i++)
+			CK(dev_zeros(c, &Q.x[i], nn));
+		CK(dev_zeros(c, &Q.b, nn));
+		CK(dev_zeros(c, &Q.r, nn));
+	}
+	// the coarsest level's reduced dofs and its dense inverse's storage
+	{
+		const mclg_qt_level &S = q[0];
+		std::vector<int> cd;
+		for (int d = 0; d < 2 * S.nno; d++)
+			if (S.kind[d] == 1)
+				cd.push_back(d);
+		if (cd.empty() || cd.size() > 1024) {
+			mclg_set_error("the coarsest level (%d) has %zu unknowns; it needs 1..1024 (lower mg_min_level)", lo,
+			               cd.size());
+			return MCLG_BAD_INPUT;
+		}
+		H.nc = (int)cd.size();
+		CK(dev_upload(c, (int **)&H.cdof, cd));
+		CK(dev_zeros(c, &H.cwork, (size_t)H.nc * 2 * H.nc));
+		CK(dev_zeros(c, &H.cinv, (size_t)H.nc * H.nc));
+		CK(dev_zeros(c, &H.cvec, 2 * (size_t)S.nno));
+	}
+	const size_t nn = c->L.nno, ne = c->L.nel;
+	CK(dev_zeros(c, &a.R, nn));
+	CK(dev_zeros(c, &a.Kd, nn));
+	CK(dev_zeros(c, &a.dd, nn));
+	CK(dev_zeros(c, &a.u1, nn));
+	CK(dev_zeros(c, &a.Rc, ne));
+	CK(dev_zeros(c, &a.dpv, ne));
+	CK(dev_zeros(c, &a.Ahp, ne));
+	for (int i = 0; i < 2; i++) {
+		CK(dev_zeros(c, &a.mv[i], nn));
+		CK(dev_zeros(c, &a.mw[i], nn));
+		CK(dev_zeros(c, &a.mvp[i], ne));
+		CK(dev_zeros(c, &a.mzp[i], ne));
+		CK(dev_zeros(c, &a.mwp[i], ne));
+		CK(dev_zeros(c, &a.mz[i], nn));
+	}
+	a.red.part = c->red_part;
+	a.red.flip = 0;
+	a.sc = c->sc;
+	a.rtol = f.stokes_rtol;
+	a.outer_rtol = f.outer_rtol;
+	a.max_refine = f.max_refine;
+	a.max_outer = f.max_outer;
+	(void)sizeof(V);
+	ShapeTables S;
+	shape_tables(S);
+	upload_shape_tables_qt(S, c->st);
+	CK(cudaStreamSynchronize(c->st));
+	c->qt_on = 1;
+	return MCLG_OK;
+}
+
+// One converged solve on a refined mesh: warm start, the coarse levels'
+// viscosity (the finer level's value at the same node) and K, the kernel,
+// the warm-start history.
+static int launch_stokes_qt(mclg_ctx *c)
+{
+	const mclg_config &f = c->cfg;
+	const size_t nn = c->L.nno, ne = c->L.nel;
+	int rc;
+	if (f.warm_start != 1 && f.warm_start != 3)
+		CK(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
+	if (f.warm_start == 0)
+		CK(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
+	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
+	CK(cudaMemsetAsync(&c->sc->guess_used, 0xff, sizeof(int), c->st));
+	const bool track = c->d_h1 != NULL;
+	if (track) {
+		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+		if (f.warm_start == 3 && c->ghist >= 2) {
+			const size_t n = 2 * nn > ne ? 2 * nn : ne;
+			k_qt_extrapolate<<<blocks_for(n), kBlock, 0, c->st>>>((int)(2 * nn), (int)ne, (const double *)c->d_h1,
+			                                                       (const double *)c->d_h2, c->p_h1, c->p_h2,
+			                                                       (double *)c->d, c->p);
+			if ((rc = check_launch(c, "k_qt_extrapolate")))
+				return rc;
+		}
+	}
+	const int nlev = c->cfg.precision == 2 ? c->qtd.H.nlev : c->qtf.H.nlev;
+	for (int k = nlev - 2; k >= 0; k--) {
+		const DevLevel &L = c->lvl_L[k];
+		const double *src = k == nlev - 2 ? c->vis : c->lvl_vis[k + 1];
+		k_qt_inject<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L.nno, c->lvl_map[k], src, c->lvl_vis[k]);
+		if ((rc = check_launch(c, "k_qt_inject")))
+			return rc;
+		k_assemble_stokes<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->lvl_vis[k], c->lvl_buoy[k], c->lvl_K[k],
+		                                                           c->lvl_F[k], c->lvl_Kd[k], 1);
+		if ((rc = check_launch(c, "k_assemble_stokes")))
+			return rc;
+	}
+	if (c->cfg.precision == 2) {
+		void *args[] = {&c->qtd};
+		CK(cudaLaunchCooperativeKernel(qt_kernel(1), dim3(c->coop_qt), dim3(kBlock), args, 0, c->st));
+	} else {
+		void *args[] = {&c->qtf};
+		CK(cudaLaunchCooperativeKernel(qt_kernel(0), dim3(c->coop_qt), dim3(kBlock), args, 0, c->st));
+	}
+	c->launches++;
+	if (track) {
+		std::swap(c->d_h1, c->d_h2);
+		std::swap(c->p_h1, c->p_h2);
+		c->ghist++;
+	}
+	return MCLG_OK;
 }
 
 static int alloc_history(mclg_ctx *c)
@@ -799,7 +1038,9 @@ static int launch_uzawa(mclg_ctx *c);
 
 static int launch_stokes(mclg_ctx *c)
 {
-	return c->cfg.precision == 0 ? launch_uzawa(c) : launch_stokes_mg(c);
+	if (c->cfg.precision == 0)
+		return launch_uzawa(c);
+	return c->qt_on ? launch_stokes_qt(c) : launch_stokes_mg(c);
 }
 
 extern "C" {
@@ -846,7 +1087,17 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
 	c->cfg = *cfg;
-	int rc = leaves ? mclg_mesh_build_leaves(&c->mesh, cfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, cfg);
+	// the converged solvers' hierarchy on a refined mesh goes down to a grid of
+	// mg_coarse elements per side: the mesh keeps levels that far down
+	mclg_config mcfg = *cfg;
+	if (cfg->precision != 0) {
+		int cl = 1;
+		while ((1 << (cl + 1)) <= cfg->mg_coarse)
+			cl++;
+		if (cl < mcfg.mg_min_level)
+			mcfg.mg_min_level = cl;
+	}
+	int rc = leaves ? mclg_mesh_build_leaves(&c->mesh, &mcfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, &mcfg);
 	if (rc != MCLG_OK) {
 		mclg_mesh_free(&c->mesh);
 		free(c);
@@ -946,13 +1197,22 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	const int work = (int)(nn > ne ? nn : ne);
 	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(c->ref_kind != kRefNone), c->num_sms, work);
 	c->coop_heat = coop_blocks(heat_cg_kernel_ptr(), c->num_sms, (int)nn);
-	if (cfg->precision != 0) {
-		if (!c->mesh.uniform) {
-			mclg_set_error("precision=mixed/fp64mg needs a uniform mesh (develop_mode=0); use precision=fp64");
+	if (cfg->precision != 0 && !c->mesh.uniform) {
+		rc = cfg->precision == 2 ? qt_setup<double>(c, c->qtd) : qt_setup<float>(c, c->qtf);
+		if (rc == MCLG_OK)
+			c->coop_qt = coop_blocks(qt_kernel(cfg->precision == 2), c->num_sms, (int)nn);
+		if (rc == MCLG_OK && c->coop_qt < 1) {
+			mclg_set_error("cooperative occupancy query failed");
+			rc = MCLG_CUDA_ERROR;
+		}
+		if (rc == MCLG_OK && cfg->warm_start == 3)
+			rc = alloc_history(c);
+		if (rc != MCLG_OK) {
 			mclg_destroy(c);
 			*out = NULL;
-			return MCLG_BAD_INPUT;
+			return rc;
 		}
+	} else if (cfg->precision != 0) {
 		rc = cfg->precision == 2 ? mg_setup<double>(c, c->mgd) : mg_setup<float>(c, c->mgf);
 		if (rc != MCLG_OK) {
 			mclg_destroy(c);
@@ -1000,7 +1260,7 @@ void mclg_destroy(mclg_ctx *c)
 		cudaStreamSynchronize(c->st);
 	free_level_buf(c->lb);
 	for (int k = 0; k < MCLG_MAX_LEVEL; k++)
-		free_level_buf(c->ref_lb[k]);
+		free_level_buf(c->lvl_lb[k]);
 	for (int i = 0; i < c->ref_nptr; i++)
 		cudaFree(c->ref_ptr[i]);
 	free(c->ref_ptr);
@@ -1081,7 +1341,7 @@ int mclg_velocity_pressure_KGF_matrix(mclg_ctx *c)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	const int withK = c->cfg.precision == 0;
+	const int withK = c->cfg.precision == 0 || c->qt_on;
 	k_assemble_stokes<<<blocks_for(c->L.nno), kBlock, 0, c->st>>>(c->L, c->vis, c->buoy, c->K, c->F, c->Kdiag,
 	                                                               withK);
 	int rc = check_launch(c, "k_assemble_stokes");
@@ -1430,7 +1690,7 @@ int mclg_get_field(mclg_ctx *c, int which, int lev, double *out, size_t n)
 			mclg_set_error("field %d of level %d has %zu entries, buffer has %zu", which, lev, need, n);
 			return MCLG_BAD_INPUT;
 		}
-		CK(cudaMemcpyAsync(out, which == MCLG_F_T ? c->ref_T[k] : c->ref_vis[k], n * sizeof(double),
+		CK(cudaMemcpyAsync(out, which == MCLG_F_T ? c->lvl_T[k] : c->lvl_vis[k], n * sizeof(double),
 		                   cudaMemcpyDeviceToHost, c->st));
 		CK(cudaStreamSynchronize(c->st));
 		return MCLG_OK;
@@ -1587,7 +1847,7 @@ int mclg_stokes_matvec(mclg_ctx *c, int lev, const double *x, double *y)
 		int rc = eq_to_node(c, x, c->tmpA, lev);
 		if (rc)
 			return rc;
-		k_kmul<<<blocks_for(c->ref_L[k].nno), kBlock, 0, c->st>>>(c->ref_L[k], c->ref_K[k], (const double2 *)c->tmpA,
+		k_kmul<<<blocks_for(c->lvl_L[k].nno), kBlock, 0, c->st>>>(c->lvl_L[k], c->lvl_K[k], (const double2 *)c->tmpA,
 		                                                            (double2 *)c->tmpB);
 		if ((rc = check_launch(c, "k_kmul")))
 			return rc;

@@ -69,6 +69,9 @@ struct DevLevel {
 
 // Scalars shared by the kernels of one step, resident on the device so that
 // no kernel needs a host round trip.
+// Status bits written to StepScalars::status.
+constexpr int kStatCap = 1, kStatNan = 2, kStatBreakdown = 4;
+
 struct StepScalars {
 	double dt, model_time;
 	double accuracy;            // inner tolerance in use (auto_accuracy may rescale it)
@@ -196,6 +199,42 @@ __device__ __forceinline__ void element_g(const ShapeTables &S, double dzh, doub
 // Corner order of an element sorted by node index: ien corners 0=(x,z),
 // 1=(x,z+s), 2=(x+s,z+s), 3=(x+s,z) have node ids n0 < n1 < n3 < n2.
 __constant__ static const int kSortedCorner[4] = {0, 1, 3, 2};
+
+// G p at node A (G_prod_p, Solver.c:569-591): row entries in element order.
+__device__ __forceinline__ void gmul_node(const DevLevel &L, const double *__restrict__ p, int A,
+                                          double &y0, double &y1)
+{
+	double s0 = 0.0, s1 = 0.0;
+	for (int k = 0; k < L.p2n_cnt[A]; k++) {
+		const int e = L.p2n_el[k * L.nno + A], a = L.p2n_a[k * L.nno + A];
+		double g0, g1;
+		element_g(cS, L.dzh[e], L.dxh[e], a, g0, g1);
+		s0 += g0 * p[e];
+		s1 += g1 * p[e];
+	}
+	y0 = vfree(L, A, 0) ? s0 : 0.0;
+	y1 = vfree(L, A, 1) ? s1 : 0.0;
+}
+
+// (G^T u)_e (GT_prod_d, Solver.c:645-666): the element's free dofs in
+// ascending equation order.
+__device__ __forceinline__ double gtmul_elem(const DevLevel &L, const double2 *__restrict__ u, int e)
+{
+	double s = 0.0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		const int A = L.ienl[a * L.nel + e];
+		double g0, g1;
+		element_g(cS, L.dzh[e], L.dxh[e], a, g0, g1);
+		const double2 ua = u[A];
+		if (vfree(L, A, 0))
+			s += g0 * ua.x;
+		if (vfree(L, A, 1))
+			s += g1 * ua.y;
+	}
+	return s;
+}
 
 // ---- kernel argument blocks (shared by the host launch code) ---------------
 // One level of the hierarchy of the reference's own inner solvers

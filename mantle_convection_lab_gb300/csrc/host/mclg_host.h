@@ -76,6 +76,27 @@ void mclg_mesh_free(mclg_mesh *m);
 int mclg_refmg_interp(const mclg_mesh *m, int lev, int *n, int *src);
 int mclg_refmg_project(const mclg_mesh *m, int lev, int *up_eq);
 int mclg_refmg_waves(const mclg_level *L, int *wave);
+/* Constrained-space structure of one level for the converged solver on
+ * quadtree meshes (mclg_qtmg.c).  Dofs are 2*node + component. */
+typedef struct mclg_qt_level {
+	int nno;
+	unsigned char *kind;              /* [2*nno] 0 fixed, 1 reduced, 2 constrained */
+	int *ex_off, *ex_src;             /* expand: constrained dof = sum ex_w * x[ex_src] */
+	double *ex_w;
+	int *fo_off, *fo_dof;             /* fold: reduced dof <- constrained dofs holding it */
+	double *fo_w;
+	int *dg_off, *dg_node, *dg_slot;  /* diagonal of C^T K C: sum dg_w * K[dg_slot][dg_node] */
+	double *dg_w;
+	int *p_off, *p_src;               /* prolongation from the level below (rows: this level's dofs) */
+	double *p_w;
+	int *r_off, *r_src;               /* restriction from the level above (rows: this level's dofs) */
+	double *r_w;
+	int *node_map;                    /* [nno] the same node on the level above (NULL on the finest) */
+	int n_ex, n_fo, n_dg, n_p, n_r;
+} mclg_qt_level;
+/* levels lo..max_level-1 into q[0..]; lo > min_level-1 and below the finest */
+int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q);
+void mclg_qt_free(mclg_qt_level *q);
 /* Binary search in the sorted node list (node_index, Array_work.c:106-129). */
 int mclg_node_index(const mclg_level *L, int gid);
 

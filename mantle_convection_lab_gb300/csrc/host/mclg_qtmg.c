@@ -1,0 +1,417 @@
+/* Constrained-space structure of the converged solver on quadtree meshes.
+ *
+ * On a mesh with hanging nodes the velocity space is conforming: the value of
+ * a hanging node's free component is the mean of its two parents'
+ * (Connection.c:59-276 finds them; enforce_constrain_veq, Solver.c:1368-1482,
+ * imposes the same relation inside the reference's CG), so the unknowns are
+ * the free components of the other nodes ("reduced" dofs) and the discrete
+ * system is C^T K C d + C^T G p = C^T F, G^T C d = 0 with C the expansion of
+ * reduced dofs to all dofs.  The reference's iteration applies the relation
+ * by overwriting inside CG without folding the hanging rows into their
+ * parents, so its system has no exact solution on such meshes; this one has.
+ *
+ * Per level, dofs are 2*node + component:
+ *   kind      0 fixed (Dirichlet 'V'), 1 reduced, 2 constrained (hanging, free)
+ *   expand    constrained dof = sum w * reduced dof (parents' chains resolved;
+ *             a fixed parent contributes its value, 0 for the homogeneous
+ *             corrections this structure is used for)
+ *   fold      the transpose: for a reduced dof, the constrained dofs whose
+ *             expansion holds it, with the same weights
+ *   diag      terms of the constrained operator's diagonal:
+ *             D_a = sum w * K[row node][slot] (component c,c)
+ *   P         prolongation from the level below to this level's reduced dofs:
+ *             the reference's averaging map (build_interp_conn,
+ *             Connection.c:708-930) applied to the coarse expanded field
+ *   R         restriction to this level from the level above, P^T by rows.
+ * All lists are CSR by dof, built in ascending order so device gathers sum in
+ * a fixed order. */
+#include <stdlib.h>
+#include <string.h>
+
+#include "mclg_host.h"
+
+typedef struct {
+	int *idx;
+	double *w;
+	long n, cap;
+} csr_b;
+
+static int csr_push(csr_b *c, int idx, double w)
+{
+	if (c->n == c->cap) {
+		long cap = c->cap ? 2 * c->cap : 256;
+		int *i2 = (int *)realloc(c->idx, (size_t)cap * sizeof(int));
+		if (i2 == NULL)
+			return -1;
+		c->idx = i2;
+		double *w2 = (double *)realloc(c->w, (size_t)cap * sizeof(double));
+		if (w2 == NULL)
+			return -1;
+		c->w = w2;
+		c->cap = cap;
+	}
+	c->idx[c->n] = idx;
+	c->w[c->n] = w;
+	c->n++;
+	return 0;
+}
+
+/* a term list: (dof, weight) pairs, merged by dof */
+typedef struct {
+	int dof[64];
+	double w[64];
+	int n;
+} terms;
+
+static int terms_add(terms *t, int dof, double w)
+{
+	int i;
+	for (i = 0; i < t->n; i++)
+		if (t->dof[i] == dof) {
+			t->w[i] += w;
+			return 0;
+		}
+	if (t->n == 64)
+		return -1;
+	t->dof[t->n] = dof;
+	t->w[t->n] = w;
+	t->n++;
+	return 0;
+}
+
+static void terms_sort(terms *t)
+{
+	int i, j;
+	for (i = 1; i < t->n; i++)
+		for (j = i; j > 0 && t->dof[j - 1] > t->dof[j]; j--) {
+			int d = t->dof[j];
+			double w = t->w[j];
+			t->dof[j] = t->dof[j - 1];
+			t->w[j] = t->w[j - 1];
+			t->dof[j - 1] = d;
+			t->w[j - 1] = w;
+		}
+}
+
+/* expansion of dof (2*A + c) of level L into reduced dofs, through chains of
+ * hanging parents; hang_of[A] = index in the hanging list or -1 */
+static int expand_dof(const mclg_level *L, const int *hang_of, int dof, double w, int depth, terms *out)
+{
+	const int A = dof >> 1, c = dof & 1;
+	if (L->v_bc[(size_t)c * L->nno + A] == 'V')
+		return 0;   /* fixed: value 0 in the homogeneous space */
+	const int h = hang_of[A];
+	if (h < 0)
+		return terms_add(out, dof, w);
+	if (depth > 16)
+		return -1;   /* a cycle of hanging parents: not a quadtree */
+	if (expand_dof(L, hang_of, 2 * L->hang_ci0[h] + c, 0.5 * w, depth + 1, out))
+		return -1;
+	return expand_dof(L, hang_of, 2 * L->hang_ci1[h] + c, 0.5 * w, depth + 1, out);
+}
+
+static int slot_of(const mclg_level *L, int row, int col)
+{
+	int k;
+	for (k = 0; k < L->nb_cnt[row]; k++)
+		if (L->nb[(size_t)k * L->nno + row] == col)
+			return k;
+	return -1;
+}
+
+static void free_csr(int **off, int **idx, double **w)
+{
+	free(*off);
+	free(*idx);
+	free(*w);
+	*off = NULL;
+	*idx = NULL;
+	*w = NULL;
+}
+
+void mclg_qt_free(mclg_qt_level *q)
+{
+	free(q->kind);
+	free_csr(&q->ex_off, &q->ex_src, &q->ex_w);
+	free_csr(&q->fo_off, &q->fo_dof, &q->fo_w);
+	free_csr(&q->dg_off, &q->dg_slot, &q->dg_w);
+	free(q->dg_node);
+	free_csr(&q->p_off, &q->p_src, &q->p_w);
+	free_csr(&q->r_off, &q->r_src, &q->r_w);
+	free(q->node_map);
+	memset(q, 0, sizeof *q);
+}
+
+/* hand a built list's arrays over (never NULL) */
+static int take(csr_b *b, int **idx, double **w)
+{
+	*idx = b->idx ? b->idx : (int *)malloc(sizeof(int));
+	*w = b->w ? b->w : (double *)malloc(sizeof(double));
+	return (*idx && *w) ? 0 : -1;
+}
+
+/* kind, expand, fold and diag terms of one level */
+static int build_constraints(const mclg_level *L, mclg_qt_level *q)
+{
+	const int nno = L->nno, nd = 2 * nno;
+	int *hang_of = (int *)malloc((size_t)nno * sizeof(int));
+	csr_b ex = {0}, fo = {0}, dg = {0};
+	int *dg_node_tmp = NULL;
+	long dgn = 0, dgcap = 0;
+	int rc = MCLG_BAD_INPUT, h, d, i;
+	q->nno = nno;
+	q->kind = (unsigned char *)calloc((size_t)nd + 1, 1);
+	q->ex_off = (int *)calloc((size_t)nd + 1, sizeof(int));
+	q->fo_off = (int *)calloc((size_t)nd + 1, sizeof(int));
+	q->dg_off = (int *)calloc((size_t)nd + 1, sizeof(int));
+	if (!hang_of || !q->kind || !q->ex_off || !q->fo_off || !q->dg_off)
+		goto out;
+	for (i = 0; i < nno; i++)
+		hang_of[i] = -1;
+	for (h = 0; h < L->nh; h++)
+		hang_of[L->hang_ni[h]] = h;
+	for (d = 0; d < nd; d++) {
+		const int A = d >> 1, c = d & 1;
+		q->kind[d] = L->v_bc[(size_t)c * nno + A] == 'V' ? 0 : hang_of[A] >= 0 ? 2 : 1;
+	}
+	/* expand lists of constrained dofs */
+	for (d = 0; d < nd; d++) {
+		q->ex_off[d] = (int)ex.n;
+		if (q->kind[d] != 2)
+			continue;
+		const int A = d >> 1, c = d & 1, hh = hang_of[A];
+		terms t;
+		t.n = 0;
+		if (expand_dof(L, hang_of, 2 * L->hang_ci0[hh] + c, 0.5, 1, &t) ||
+		    expand_dof(L, hang_of, 2 * L->hang_ci1[hh] + c, 0.5, 1, &t)) {
+			mclg_set_error("hanging node %d: its parents' chain does not end", A);
+			goto out;
+		}
+		terms_sort(&t);
+		for (i = 0; i < t.n; i++)
+			if (csr_push(&ex, t.dof[i], t.w[i]))
+				goto out;
+	}
+	q->ex_off[nd] = (int)ex.n;
+	/* fold: transpose of expand, by reduced dof, constrained dofs ascending */
+	{
+		int *cnt = (int *)calloc((size_t)nd + 1, sizeof(int));
+		if (cnt == NULL)
+			goto out;
+		for (long k = 0; k < ex.n; k++)
+			cnt[ex.idx[k]]++;
+		q->fo_off[0] = 0;
+		for (d = 0; d < nd; d++)
+			q->fo_off[d + 1] = q->fo_off[d] + cnt[d];
+		fo.n = fo.cap = ex.n;
+		fo.idx = (int *)malloc((size_t)(ex.n + 1) * sizeof(int));
+		fo.w = (double *)malloc((size_t)(ex.n + 1) * sizeof(double));
+		if (!fo.idx || !fo.w) {
+			free(cnt);
+			goto out;
+		}
+		memcpy(cnt, q->fo_off, (size_t)nd * sizeof(int));
+		for (d = 0; d < nd; d++)   /* constrained dofs in ascending order */
+			for (int k = q->ex_off[d]; k < q->ex_off[d + 1]; k++) {
+				const int a = ex.idx[k];
+				fo.idx[cnt[a]] = d;
+				fo.w[cnt[a]] = ex.w[k];
+				cnt[a]++;
+			}
+		free(cnt);
+	}
+	/* diagonal terms of C^T K C at each reduced dof: (row node, slot, weight) */
+	for (d = 0; d < nd; d++) {
+		q->dg_off[d] = (int)dg.n;
+		if (q->kind[d] != 1)
+			continue;
+		int sup[65];
+		double sw[65];
+		int ns = 1;
+		sup[0] = d;
+		sw[0] = 1.0;
+		for (int k = q->fo_off[d]; k < q->fo_off[d + 1] && ns < 65; k++) {
+			sup[ns] = fo.idx[k];
+			sw[ns] = fo.w[k];
+			ns++;
+		}
+		for (int a = 0; a < ns; a++)
+			for (int b = 0; b < ns; b++) {
+				const int row = sup[a] >> 1, col = sup[b] >> 1;
+				const int k = slot_of(L, row, col);
+				if (k < 0)
+					continue;
+				if (csr_push(&dg, k, sw[a] * sw[b]))
+					goto out;
+				if (dgn == dgcap) {
+					long cap = dgcap ? 2 * dgcap : 256;
+					int *t2 = (int *)realloc(dg_node_tmp, (size_t)cap * sizeof(int));
+					if (t2 == NULL)
+						goto out;
+					dg_node_tmp = t2;
+					dgcap = cap;
+				}
+				dg_node_tmp[dgn++] = row;
+			}
+	}
+	q->dg_off[nd] = (int)dg.n;
+	if (take(&ex, &q->ex_src, &q->ex_w) || take(&fo, &q->fo_dof, &q->fo_w) ||
+	    take(&dg, &q->dg_slot, &q->dg_w))
+		goto out;
+	ex.idx = NULL;
+	ex.w = NULL;
+	fo.idx = NULL;
+	fo.w = NULL;
+	dg.idx = NULL;
+	dg.w = NULL;
+	q->dg_node = dg_node_tmp ? dg_node_tmp : (int *)malloc(sizeof(int));
+	dg_node_tmp = NULL;
+	q->n_ex = q->ex_off[nd];
+	q->n_fo = q->fo_off[nd];
+	q->n_dg = q->dg_off[nd];
+	rc = q->dg_node ? MCLG_OK : MCLG_BAD_INPUT;
+out:
+	free(hang_of);
+	free(ex.idx);
+	free(ex.w);
+	free(fo.idx);
+	free(fo.w);
+	free(dg.idx);
+	free(dg.w);
+	free(dg_node_tmp);
+	return rc;
+}
+
+/* P of level `lev` (rows: its reduced dofs; columns: reduced dofs of lev-1) */
+static int build_prolongation(const mclg_mesh *m, int lev, const mclg_qt_level *lo, mclg_qt_level *up)
+{
+	const mclg_level *U = &m->lev[lev], *D = &m->lev[lev - 1];
+	const int neq = U->neq, nd = 2 * U->nno;
+	int *n = (int *)malloc((size_t)(neq > 0 ? neq : 1) * sizeof(int));
+	int *src = (int *)malloc(4 * (size_t)(neq > 0 ? neq : 1) * sizeof(int));
+	int *dof_lo = (int *)malloc((size_t)(D->neq > 0 ? D->neq : 1) * sizeof(int));
+	csr_b p = {0};
+	int rc = MCLG_BAD_INPUT, d, A, c;
+	up->p_off = (int *)calloc((size_t)nd + 1, sizeof(int));
+	if (!n || !src || !dof_lo || !up->p_off)
+		goto out;
+	if (mclg_refmg_interp(m, lev, n, src) != MCLG_OK)
+		goto out;
+	for (A = 0; A < D->nno; A++)
+		for (c = 0; c < 2; c++) {
+			const int eq = D->id[(size_t)c * D->nno + A];
+			if (eq >= 0)
+				dof_lo[eq] = 2 * A + c;
+		}
+	for (d = 0; d < nd; d++) {
+		up->p_off[d] = (int)p.n;
+		if (up->kind[d] != 1)
+			continue;
+		A = d >> 1;
+		c = d & 1;
+		const int eu = U->id[(size_t)c * U->nno + A];
+		if (eu < 0 || n[eu] <= 0) {
+			mclg_set_error("level %d: reduced dof %d has no interpolation from level %d", lev, d, lev - 1);
+			goto out;
+		}
+		terms t;
+		t.n = 0;
+		for (int i = 0; i < n[eu]; i++) {
+			const int el = src[(size_t)i * neq + eu];
+			if (el < 0)
+				continue;   /* a fixed coarse dof: 0, still counted in the mean (Solver.c:1036-1043) */
+			const int dl = dof_lo[el];
+			if (lo->kind[dl] == 1) {
+				if (terms_add(&t, dl, 1.0 / n[eu]))
+					goto out;
+			} else if (lo->kind[dl] == 2) {
+				for (int k = lo->ex_off[dl]; k < lo->ex_off[dl + 1]; k++)
+					if (terms_add(&t, lo->ex_src[k], lo->ex_w[k] / n[eu]))
+						goto out;
+			}
+		}
+		terms_sort(&t);
+		for (int i = 0; i < t.n; i++)
+			if (csr_push(&p, t.dof[i], t.w[i]))
+				goto out;
+	}
+	up->p_off[nd] = (int)p.n;
+	up->n_p = (int)p.n;
+	if (take(&p, &up->p_src, &up->p_w))
+		goto out;
+	p.idx = NULL;
+	p.w = NULL;
+	rc = MCLG_OK;
+out:
+	free(n);
+	free(src);
+	free(dof_lo);
+	free(p.idx);
+	free(p.w);
+	return rc;
+}
+
+/* R of level lev-1 = P(lev)^T, rows by coarse dof, fine dofs ascending */
+static int build_restriction(const mclg_qt_level *up, mclg_qt_level *lo)
+{
+	const int ndl = 2 * lo->nno, ndu = 2 * up->nno;
+	int *cnt = (int *)calloc((size_t)ndl + 1, sizeof(int));
+	lo->r_off = (int *)calloc((size_t)ndl + 1, sizeof(int));
+	lo->r_src = (int *)malloc((size_t)(up->n_p + 1) * sizeof(int));
+	lo->r_w = (double *)malloc((size_t)(up->n_p + 1) * sizeof(double));
+	if (!cnt || !lo->r_off || !lo->r_src || !lo->r_w) {
+		free(cnt);
+		return MCLG_BAD_INPUT;
+	}
+	for (int k = 0; k < up->n_p; k++)
+		cnt[up->p_src[k]]++;
+	for (int d = 0; d < ndl; d++)
+		lo->r_off[d + 1] = lo->r_off[d] + cnt[d];
+	memcpy(cnt, lo->r_off, (size_t)ndl * sizeof(int));
+	for (int u = 0; u < ndu; u++)
+		for (int k = up->p_off[u]; k < up->p_off[u + 1]; k++) {
+			const int a = up->p_src[k];
+			lo->r_src[cnt[a]] = u;
+			lo->r_w[cnt[a]] = up->p_w[k];
+			cnt[a]++;
+		}
+	lo->n_r = up->n_p;
+	free(cnt);
+	return MCLG_OK;
+}
+
+int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q)
+{
+	const int top = m->max_level - 1;
+	int lev, rc;
+	if (lo < m->min_level || lo >= top)
+		return MCLG_BAD_INPUT;
+	for (lev = lo; lev <= top; lev++) {
+		mclg_qt_level *Q = &q[lev - lo];
+		memset(Q, 0, sizeof *Q);
+		if ((rc = build_constraints(&m->lev[lev], Q)) != MCLG_OK)
+			return rc;
+		/* node_map: this level's node -> the same node one level up (every node of a
+		 * level exists on the finer levels) */
+		if (lev < top) {
+			const mclg_level *L = &m->lev[lev], *U = &m->lev[lev + 1];
+			Q->node_map = (int *)malloc((size_t)L->nno * sizeof(int));
+			if (Q->node_map == NULL)
+				return MCLG_BAD_INPUT;
+			for (int A = 0; A < L->nno; A++) {
+				Q->node_map[A] = mclg_node_index(U, L->node[A]);
+				if (Q->node_map[A] < 0) {
+					mclg_set_error("level %d: node %d is missing on level %d", lev, L->node[A], lev + 1);
+					return MCLG_BAD_INPUT;
+				}
+			}
+		}
+		if (lev > lo) {
+			if ((rc = build_prolongation(m, lev, &q[lev - lo - 1], Q)) != MCLG_OK)
+				return rc;
+			if ((rc = build_restriction(Q, &q[lev - lo - 1])) != MCLG_OK)
+				return rc;
+		}
+	}
+	return MCLG_OK;
+}
