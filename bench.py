@@ -75,8 +75,9 @@ WORKLOADS["cfg2_amr_128"] = {
     "input": "mantle_convection_lab_gb300/configs/cfg2_amr_128.input",
     "kind": "amr",
     "desc": "configuration 2: 128x128 base, |grad T| > 0.2 max refined up to 3 levels (2:1 balanced, hanging "
-            "nodes), remeshing every 10 steps, eta=exp(-ln(1e4) T), Ra=1e7; FP64 replica of the reference's "
-            "Uzawa/Jacobi-PCG iteration with bounded caps (200 Uzawa x 500 CG cycles)",
+            "nodes), remeshing every 10 steps, eta=exp(-ln(1e4) T), Ra=1e7; FP32 V-cycle inside FP64 refinement "
+            "(MINRES on the conforming hanging-node system) to Stokes residual 1e-8 every step; the FP64 replica "
+            "of the reference's Uzawa/Jacobi-PCG iteration beside it",
     "mesh": "128^2 base + 3 levels",
 }
 ENSEMBLE_METRIC = "aggregate model-steps/s at Stokes residual 1e-8"
@@ -435,55 +436,89 @@ def run_ensemble(args, wl):
     return 0
 
 
-def run_amr(args, wl):
-    """Configuration 2: steps including the remeshing every 10 steps (host tree
-    and transfer, device flags), timed on the wall clock because remeshing is
-    host work; the device time of the steps is reported beside it."""
-    import torch
-    from mantle_convection_lab_gb300 import Config, amr
-
-    rank, world, local_rank = dist_env()
-    dist = init_dist(world, local_rank)
-    torch.cuda.set_device(local_rank)
-    cfg = Config.from_input(os.path.join(ROOT, wl["input"]))
-    cfg.max_citcom_cycle, cfg.max_cg_cycle = 200, 500
+def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch):
+    from mantle_convection_lab_gb300 import amr
     run = amr.AmrRun(cfg)
-    for _ in range(max(args.warmup, 0)):
+    for _ in range(max(warmup, 0)):
         run.step()
-    sampler = ClockSampler() if rank == 0 else None
+    sampler = ClockSampler() if sampler_on else None
     if sampler:
         sampler.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ms, res, nel, launches, capped, rem0 = 0.0, 0.0, [], 0, 0, run.remeshes
-    for _ in range(args.steps):
+    acc = {"ms": 0.0, "ms_solver": 0.0, "res": 0.0, "nel": [], "launches": 0, "capped": 0, "passes": 0,
+           "minres": 0, "vcycles": 0, "rem0": run.remeshes}
+    for _ in range(steps):
         st = run.step()
-        ms += st.ms_total
-        launches += st.kernel_launches
-        res = max(res, st.res_momentum, st.res_continuity)
-        capped += st.status == 1
-        nel.append(run.model.nel)
+        acc["ms"] += st.ms_total
+        acc["ms_solver"] += st.solver_kernel_ms
+        acc["launches"] += st.kernel_launches
+        acc["res"] = max(acc["res"], st.res_momentum, st.res_continuity)
+        acc["capped"] += st.status == 1
+        acc["passes"] += st.refine_passes
+        acc["minres"] += st.uzawa_cycles
+        acc["vcycles"] += st.cg_cycles
+        acc["nel"].append(run.model.nel)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    acc["wall"] = time.perf_counter() - t0
     if dist:
         dist.barrier()
-    clocks = sampler.stop() if sampler else None
-    value = job_throughput(dist, args.steps, wall)
-    line = {
-        "metric": "time steps/s including remeshing (configuration 2)", "value": value, "unit": "steps/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded .input)",
-        "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"], "elements_per_step": nel,
-                   "remeshes_timed": run.remeshes - rem0, "device_ms_per_step": ms / args.steps,
-                   "steps_at_iteration_cap": capped, "max_stokes_residual": res,
-                   "residual_1e-8_met": bool(res < 1e-8), "parallelism": f"replicas x{world}"},
-        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "gpu_launches": launches, "roofline": None, "clocks": clocks,
-    }
+    acc["clocks"] = sampler.stop() if sampler else None
+    acc["remeshes"] = run.remeshes - acc["rem0"]
+    acc["nh"] = run.model.nh
     run.close()
+    return acc
+
+
+def run_amr(args, wl):
+    """Configuration 2: steps including the remeshing every 10 steps (host tree
+    and transfer, device flags), timed on the wall clock because remeshing is
+    host work; the device time of the steps is reported beside it.  value: the
+    mixed-precision converged solver (FP64 refinement around MINRES with an FP32
+    V-cycle on the mesh's own levels, conforming hanging-node space) to Stokes
+    residual 1e-8; fp64_replica: the reference's iteration (Uzawa + Jacobi-PCG)
+    on the same run with bounded caps, which does not converge here."""
+    import torch
+    from mantle_convection_lab_gb300 import Config
+
+    rank, world, local_rank = dist_env()
+    dist = init_dist(world, local_rank)
+    torch.cuda.set_device(local_rank)
+    cfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+    cfg.precision, cfg.warm_start, cfg.stokes_method, cfg.stokes_rtol = 1, 3, 1, 1e-8
+    cfg.outer_rtol, cfg.max_outer, cfg.max_refine = 3e-3, 1000, 20
+    acc = _amr_arm(cfg, args.steps, args.warmup, rank == 0, dist, torch)
+    value = job_throughput(dist, args.steps, acc["wall"])
+    line = {
+        "metric": "time steps/s including remeshing at Stokes residual 1e-8 (configuration 2)", "value": value,
+        "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * acc["wall"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic (seeded .input)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
+                   "elements_per_step": acc["nel"], "hanging_nodes_last": acc["nh"],
+                   "remeshes_timed": acc["remeshes"], "device_ms_per_step": acc["ms"] / args.steps,
+                   "solver_kernel_ms_per_step": acc["ms_solver"] / args.steps,
+                   "refine_passes_per_step": acc["passes"] / args.steps,
+                   "minres_iterations_per_step": acc["minres"] / args.steps,
+                   "steps_at_iteration_cap": acc["capped"], "max_stokes_residual": acc["res"],
+                   "residual": "conforming: |[C^T(F - K d - G p); G^T C d]| / |C^T F|, C the hanging-node expansion",
+                   "residual_1e-8_met": bool(acc["res"] < 1e-8), "parallelism": f"replicas x{world}",
+                   "roofline": "not reported: assembled-ELL operators on 5 levels, latency-bound at this size"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": acc["launches"], "roofline": None, "clocks": acc["clocks"],
+    }
+    if not args.no_plain:
+        rcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+        rcfg.max_citcom_cycle, rcfg.max_cg_cycle = 200, 500
+        n = min(args.plain_steps, args.steps)
+        racc = _amr_arm(rcfg, n, 1, False, dist, torch)
+        line["fp64_replica"] = {
+            "value": job_throughput(dist, n, racc["wall"]), "unit": "steps/s", "steps": n,
+            "max_stokes_residual": racc["res"], "steps_at_iteration_cap": racc["capped"],
+            "desc": "the reference's iteration (BAB-multiply Uzawa, Jacobi-PCG, hanging nodes overwritten in CG) "
+                    "in FP64 with caps 200 x 500; it does not reach the residual on this mesh"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -64,6 +64,7 @@ def test_step_output_is_the_text_of_the_models_fields(tmp_path):
 
 def test_outputs_in_flight_while_stepping(tmp_path):
     cfg = Config.from_input(golden_input("hang11_l6"))
+    cfg.max_citcom_cycle, cfg.max_cg_cycle = 20, 100    # a capped, quick replica step
     mesh = Mesh(cfg)
     d = tmp_path / "o"
     with Model(cfg) as m:
