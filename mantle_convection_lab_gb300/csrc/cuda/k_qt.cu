@@ -26,19 +26,49 @@ __device__ __forceinline__ X qt_val(const QtLevel<T> &L, const X *__restrict__ x
 	return s;
 }
 
+// Both components of node B of a primal vector through the constraints (the
+// rare path of a row: a column with a constrained component).
+template <class T, class X>
+__device__ __noinline__ typename Q2T<X>::t qt_val2(const QtLevel<T> &L, const X *__restrict__ xf, int B)
+{
+	typename Q2T<X>::t v;
+	v.x = qt_val(L, xf, 2 * B);
+	v.y = qt_val(L, xf, 2 * B + 1);
+	return v;
+}
+
 // Both rows of node j of K x~ (x~ the expanded x), with K in the level's TI
-// blocks or its FP64 blocks.
+// blocks or its FP64 blocks.  Columns go in chunks of four: the chunk's index
+// and block loads, then its gathers, are issued before any is used (a short
+// chunk is padded with the node itself and a zero block).
 template <class T, class K4, class X>
 __device__ __forceinline__ void qt_rows(const QtLevel<T> &L, const K4 *__restrict__ K, const X *__restrict__ xf, int j,
                                         X &y0, X &y1)
 {
+	typedef typename Q2T<X>::t X2;
+	const X2 *x2 = reinterpret_cast<const X2 *>(xf);
 	X s0 = X(0), s1 = X(0);
-	for (int k = 0; k < L.nbw; k++) {
-		const int B = L.nb[(size_t)k * L.nno + j];
-		const K4 kb = K[(size_t)k * L.nno + j];
-		const X x0 = qt_val(L, xf, 2 * B), x1 = qt_val(L, xf, 2 * B + 1);
-		s0 += (X)kb.x * x0 + (X)kb.y * x1;
-		s1 += (X)kb.z * x0 + (X)kb.w * x1;
+	const int n = L.cnt[j];
+	for (int k0 = 0; k0 < n; k0 += 4) {
+		int Bf[4];
+		K4 kb[4];
+		X2 xv[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			const bool in = k0 + u < n;
+			Bf[u] = in ? L.nb[(size_t)(k0 + u) * L.nno + j] : j;
+			kb[u] = in ? K[(size_t)(k0 + u) * L.nno + j] : K4{};
+		}
+#pragma unroll
+		for (int u = 0; u < 4; u++)
+			xv[u] = x2[Bf[u] & ~kQtCon];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			if (Bf[u] & kQtCon)
+				xv[u] = qt_val2(L, xf, Bf[u] & ~kQtCon);
+			s0 += (X)kb[u].x * xv[u].x + (X)kb[u].y * xv[u].y;
+			s1 += (X)kb[u].z * xv[u].x + (X)kb[u].w * xv[u].y;
+		}
 	}
 	y0 = s0;
 	y1 = s1;
@@ -131,85 +161,138 @@ __device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const t
 	}
 }
 
+// The team running a part of the V-cycle: the whole grid, or block 0 alone
+// for the smallest levels (block barriers instead of grid barriers).
+struct QtTeam {
+	cg::grid_group *g;
+	bool grid;
+	int tid, nth;
+	__device__ void sync()
+	{
+		if (grid)
+			g->sync();
+		else
+			__syncthreads();
+	}
+};
+
+// Buffer index holding a level's result: the coarsest solve writes x[0]; a
+// finer level runs smooth-1 sweeps from the first one, then smooth after the
+// correction, so it ends in x[(2 smooth - 1) & 1].
+template <class TI>
+__device__ __forceinline__ int qt_final(const QtHier<TI> &H, int l)
+{
+	return l == 0 ? 0 : (2 * H.smooth - 1) & 1;
+}
+
+// Level l on the way down: smoothing from zero, residual, restriction into l-1.
+template <class TI>
+__device__ void qt_down(const QtHier<TI> &H, int l, QtTeam &t)
+{
+	typedef typename Q2T<TI>::t V;
+	const QtLevel<TI> &L = H.lv[l];
+	V *x0 = L.x[0];
+	for (int A = t.tid; A < L.nno; A += t.nth) {   // first sweep from zero: w D^-1 b
+		const V b = L.b[A];
+		V o;
+		o.x = H.omega * L.invD[2 * A] * b.x;
+		o.y = H.omega * L.invD[2 * A + 1] * b.y;
+		x0[A] = o;
+	}
+	int cur = 0;
+	t.sync();
+	for (int s = 1; s < H.smooth; s++) {
+		qt_sweep(L, H.omega, L.x[cur], L.x[1 - cur], t.tid, t.nth);
+		cur = 1 - cur;
+		t.sync();
+	}
+	const TI *xf = reinterpret_cast<const TI *>(L.x[cur]);
+	for (int A = t.tid; A < L.nno; A += t.nth) {
+		TI y0, y1;
+		qt_op_node(L, L.K, xf, A, y0, y1);
+		const V b = L.b[A];
+		V r;
+		r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
+		r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
+		L.r[A] = r;
+	}
+	t.sync();
+	const QtLevel<TI> &C = H.lv[l - 1];
+	const TI *rf = reinterpret_cast<const TI *>(L.r);
+	TI *cb = reinterpret_cast<TI *>(C.b);
+	for (int d = t.tid; d < 2 * C.nno; d += t.nth) {   // restriction: P^T by rows
+		TI s = TI(0);
+		for (int i = C.r_off[d]; i < C.r_off[d + 1]; i++)
+			s += C.r_w[i] * rf[C.r_src[i]];
+		cb[d] = s;
+	}
+	t.sync();
+}
+
+// Level l on the way up: prolongation of level l-1's result added, smoothing.
+template <class TI>
+__device__ void qt_up(const QtHier<TI> &H, int l, QtTeam &t)
+{
+	const QtLevel<TI> &L = H.lv[l];
+	int cur = (H.smooth - 1) & 1;
+	const TI *xc = reinterpret_cast<const TI *>(H.lv[l - 1].x[qt_final(H, l - 1)]);
+	TI *xf = reinterpret_cast<TI *>(L.x[cur]);
+	for (int d = t.tid; d < 2 * L.nno; d += t.nth) {
+		if (L.p_off[d] == L.p_off[d + 1])
+			continue;
+		TI s = TI(0);
+		for (int i = L.p_off[d]; i < L.p_off[d + 1]; i++)
+			s += L.p_w[i] * xc[L.p_src[i]];
+		xf[d] += s;
+	}
+	t.sync();
+	for (int s = 0; s < H.smooth; s++) {
+		qt_sweep(L, H.omega, L.x[cur], L.x[1 - cur], t.tid, t.nth);
+		cur = 1 - cur;
+		t.sync();
+	}
+}
+
+// coarsest level: the dense inverse on its reduced dofs
+template <class TI>
+__device__ void qt_coarse_solve(const QtHier<TI> &H, QtTeam &t)
+{
+	const QtLevel<TI> &C = H.lv[0];
+	const TI *bf = reinterpret_cast<const TI *>(C.b);
+	TI *xf = reinterpret_cast<TI *>(C.x[0]);
+	for (int i = t.tid; i < H.nc; i += t.nth) {
+		TI s = TI(0);
+		for (int j = 0; j < H.nc; j++)
+			s += H.cinv[(size_t)i * H.nc + j] * bf[H.cdof[j]];
+		xf[H.cdof[i]] = s;
+	}
+	t.sync();
+}
+
 // z = V-cycle(b) with b in the finest level's b; returns the buffer holding z.
 template <class TI>
 __device__ const typename Q2T<TI>::t *qt_vcycle(cg::grid_group &g, const QtHier<TI> &H, int tid, int nth)
 {
-	typedef typename Q2T<TI>::t V;
-	const int top = H.nlev - 1;
-	int cur[16];
-	for (int l = top; l >= 1; l--) {
-		const QtLevel<TI> &L = H.lv[l];
-		V *x0 = L.x[0];
-		for (int A = tid; A < L.nno; A += nth) {   // first sweep from zero: w D^-1 b
-			const V b = L.b[A];
-			V o;
-			o.x = H.omega * L.invD[2 * A] * b.x;
-			o.y = H.omega * L.invD[2 * A + 1] * b.y;
-			x0[A] = o;
-		}
-		cur[l] = 0;
-		g.sync();
-		for (int s = 1; s < H.smooth; s++) {
-			qt_sweep(L, H.omega, L.x[cur[l]], L.x[1 - cur[l]], tid, nth);
-			cur[l] = 1 - cur[l];
-			g.sync();
-		}
-		const TI *xf = reinterpret_cast<const TI *>(L.x[cur[l]]);
-		for (int A = tid; A < L.nno; A += nth) {
-			TI y0, y1;
-			qt_op_node(L, L.K, xf, A, y0, y1);
-			const V b = L.b[A];
-			V r;
-			r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
-			r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
-			L.r[A] = r;
+	const int top = H.nlev - 1, nb = H.nblk < top ? H.nblk : top;   // the finest level always runs on the grid
+	QtTeam grid{&g, true, tid, nth};
+	for (int l = top; l >= (nb > 1 ? nb : 1); l--)
+		qt_down(H, l, grid);
+	if (nb > 0) {
+		if (blockIdx.x == 0) {
+			QtTeam blk{&g, false, (int)threadIdx.x, (int)blockDim.x};
+			for (int l = nb - 1; l >= 1; l--)
+				qt_down(H, l, blk);
+			qt_coarse_solve(H, blk);
+			for (int l = 1; l < nb; l++)
+				qt_up(H, l, blk);
 		}
 		g.sync();
-		const QtLevel<TI> &C = H.lv[l - 1];
-		const TI *rf = reinterpret_cast<const TI *>(L.r);
-		TI *cb = reinterpret_cast<TI *>(C.b);
-		for (int d = tid; d < 2 * C.nno; d += nth) {   // restriction: P^T by rows
-			TI s = TI(0);
-			for (int i = C.r_off[d]; i < C.r_off[d + 1]; i++)
-				s += C.r_w[i] * rf[C.r_src[i]];
-			cb[d] = s;
-		}
-		g.sync();
+	} else {
+		qt_coarse_solve(H, grid);
 	}
-	{   // coarsest level: the dense inverse on its reduced dofs
-		const QtLevel<TI> &C = H.lv[0];
-		const TI *bf = reinterpret_cast<const TI *>(C.b);
-		TI *xf = reinterpret_cast<TI *>(C.x[0]);
-		for (int i = tid; i < H.nc; i += nth) {
-			TI s = TI(0);
-			for (int j = 0; j < H.nc; j++)
-				s += H.cinv[(size_t)i * H.nc + j] * bf[H.cdof[j]];
-			xf[H.cdof[i]] = s;
-		}
-		cur[0] = 0;
-		g.sync();
-	}
-	for (int l = 1; l <= top; l++) {
-		const QtLevel<TI> &L = H.lv[l];
-		const TI *xc = reinterpret_cast<const TI *>(H.lv[l - 1].x[cur[l - 1]]);
-		TI *xf = reinterpret_cast<TI *>(L.x[cur[l]]);
-		for (int d = tid; d < 2 * L.nno; d += nth) {   // prolongation, added
-			if (L.p_off[d] == L.p_off[d + 1])
-				continue;
-			TI s = TI(0);
-			for (int i = L.p_off[d]; i < L.p_off[d + 1]; i++)
-				s += L.p_w[i] * xc[L.p_src[i]];
-			xf[d] += s;
-		}
-		g.sync();
-		for (int s = 0; s < H.smooth; s++) {
-			qt_sweep(L, H.omega, L.x[cur[l]], L.x[1 - cur[l]], tid, nth);
-			cur[l] = 1 - cur[l];
-			g.sync();
-		}
-	}
-	return H.lv[top].x[cur[top]];
+	for (int l = nb > 1 ? nb : 1; l <= top; l++)
+		qt_up(H, l, grid);
+	return H.lv[top].x[qt_final(H, top)];
 }
 
 // Dense inverse of the coarsest level's constrained operator on its reduced

@@ -19,10 +19,16 @@ template <> struct Q2T<float> { typedef float2 t; };
 template <> struct Q2T<double> { typedef double2 t; };
 
 // One level; dofs are 2*node + component, vectors node layout (T2 per node).
+// A column entry of nbf: the neighbour node, with kQtCon set when one of its
+// components is constrained (read through the expansion; the others are read
+// as stored, fixed entries being kept at 0).
+constexpr int kQtCon = 1 << 30;
+
 template <class T>
 struct QtLevel {
 	int nno, nbw;
-	const int *nb;                          // [nbw*nno] matrix neighbours
+	const int *nb;                          // [nbw*nno] matrix neighbours (flagged, see kQtCon)
+	const unsigned char *cnt;               // [nno] neighbours of each node
 	const double4 *K64;                     // [nbw*nno] FP64 blocks assembled this step
 	typename V4T<T>::t *K;                  // [nbw*nno] the same in T
 	const unsigned char *kind;              // [2*nno] 0 fixed, 1 reduced, 2 constrained
@@ -46,6 +52,7 @@ struct QtHier {
 	QtLevel<T> lv[16];
 	int smooth;                             // Jacobi sweeps before and after the coarse correction
 	T omega;
+	int nblk;                               // levels lv[0..nblk-1] are small: block 0 alone runs them
 	int nc;                                 // reduced dofs of the coarsest level
 	const int *cdof;                        // [nc] their dof numbers
 	double *cwork;                          // [nc * 2nc] Gauss-Jordan workspace

@@ -717,6 +717,9 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 	H.nlev = nlev;
 	H.smooth = f.mg_smooth > 0 ? f.mg_smooth : 1;
 	H.omega = (TI)f.mg_omega;
+	H.nblk = 0;   // the smallest levels run in one block
+	while (H.nblk < nlev - 1 && m.lev[lo + H.nblk].nno <= 2048)
+		H.nblk++;
 	for (int l = lo; l <= top; l++) {
 		const int k = l - lo;
 		const mclg_level &ML = m.lev[l];
@@ -724,7 +727,6 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 		QtLevel<TI> &Q = H.lv[k];
 		const size_t nn = ML.nno, nk = (size_t)ML.nbw * nn;
 		if (l == top) {
-			Q.nb = c->L.nb;
 			Q.K64 = c->K;
 		} else {
 			DevLevel &L = c->lvl_L[k];
@@ -737,11 +739,24 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 			CK(dev_zeros(c, &c->lvl_F[k], nn));
 			CK(dev_zeros(c, &c->lvl_Kd[k], nn));
 			CK(dev_upload_n(c, &c->lvl_map[k], S.node_map, nn));
-			Q.nb = L.nb;
 			Q.K64 = c->lvl_K[k];
 		}
 		Q.nno = (int)nn;
 		Q.nbw = ML.nbw;
+		{   // neighbour columns flagged where a component is constrained, and counts
+			std::vector<int> nbf(nk);
+			std::vector<unsigned char> cnt(nn);
+			for (size_t A = 0; A < nn; A++) {
+				cnt[A] = (unsigned char)ML.nb_cnt[A];
+				for (int kk = 0; kk < ML.nbw; kk++) {
+					const int B = ML.nb[(size_t)kk * nn + A];
+					const bool con = S.kind[2 * B] == 2 || S.kind[2 * B + 1] == 2;
+					nbf[(size_t)kk * nn + A] = con ? (B | kQtCon) : B;
+				}
+			}
+			CK(dev_upload(c, (int **)&Q.nb, nbf));
+			CK(dev_upload(c, (unsigned char **)&Q.cnt, cnt));
+		}
 		K4 *Kt = NULL;
 		TI *invD = NULL;
 		CK(dev_zeros(c, &Kt, nk));
