@@ -100,6 +100,40 @@ __device__ __forceinline__ void qt_op_node(const QtLevel<T> &L, const K4 *__rest
 	y1 = y[1];
 }
 
+// (C^T K C x) at both dofs of node A from the assembled reduced operator: a
+// plain node-block ELL row (x's constrained and fixed entries are stored as 0
+// and the reduced columns hold every coupling).
+template <class TI>
+__device__ __forceinline__ void qt_kr_node(const QtLevel<TI> &L, const TI *__restrict__ xf, int A, TI &y0, TI &y1)
+{
+	typedef typename Q2T<TI>::t X2;
+	typedef typename V4T<TI>::t K4;
+	const X2 *x2 = reinterpret_cast<const X2 *>(xf);
+	TI s0 = TI(0), s1 = TI(0);
+	const int n = L.rcnt[A];
+	for (int k0 = 0; k0 < n; k0 += 4) {
+		int B[4];
+		K4 kb[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			const bool in = k0 + u < n;
+			B[u] = in ? L.rnb[(size_t)(k0 + u) * L.nno + A] : A;
+			kb[u] = in ? L.Kr[(size_t)(k0 + u) * L.nno + A] : K4{};
+		}
+		X2 xv[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++)
+			xv[u] = x2[B[u]];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			s0 += kb[u].x * xv[u].x + kb[u].y * xv[u].y;
+			s1 += kb[u].z * xv[u].x + kb[u].w * xv[u].y;
+		}
+	}
+	y0 = s0;
+	y1 = s1;
+}
+
 // (C^T G p) at both dofs of node A (FP64, the finest level)
 template <class T>
 __device__ __forceinline__ void qt_g_node(const QtLevel<T> &Q, const DevLevel &L, const double *__restrict__ p, int A,
@@ -152,7 +186,7 @@ __device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const t
 	const TI *xf = reinterpret_cast<const TI *>(xi);
 	for (int A = tid; A < L.nno; A += nth) {
 		TI y0, y1;
-		qt_op_node(L, L.K, xf, A, y0, y1);
+		qt_kr_node(L, xf, A, y0, y1);
 		const V x = xi[A], b = L.b[A];
 		V o;
 		o.x = L.kind[2 * A] == 1 ? x.x + omega * L.invD[2 * A] * (b.x - y0) : TI(0);
@@ -209,7 +243,7 @@ __device__ void qt_down(const QtHier<TI> &H, int l, QtTeam &t)
 	const TI *xf = reinterpret_cast<const TI *>(L.x[cur]);
 	for (int A = t.tid; A < L.nno; A += t.nth) {
 		TI y0, y1;
-		qt_op_node(L, L.K, xf, A, y0, y1);
+		qt_kr_node(L, xf, A, y0, y1);
 		const V b = L.b[A];
 		V r;
 		r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
@@ -464,7 +498,7 @@ __device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, d
 		for (int A = tid; A < nn; A += nth) {
 			TI k0, k1;
 			double g0, g1;
-			qt_op_node(Q, Q.K, zf, A, k0, k1);
+			qt_kr_node(Q, zf, A, k0, k1);
 			qt_g_node(Q, L, zp[cv], A, g0, g1);
 			const double2 az = make_double2((double)k0 + g0, (double)k1 + g1);
 			a.Kd[A] = az;
@@ -549,26 +583,34 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 	GridRed red = a.red;
 	int *status = &a.sc->status;
 
-	// -- per step: every level's operator in TI and its constrained diagonal
+	// -- per step: every level's reduced operator C^T K C in TI, and its diagonal
 	for (int l = 0; l < H.nlev; l++) {
 		const QtLevel<TI> &Q = H.lv[l];
-		const size_t nk = (size_t)Q.nbw * Q.nno;
-		for (size_t k = tid; k < nk; k += nth) {
-			const double4 v = Q.K64[k];
-			K4 t;
-			t.x = (TI)v.x;
-			t.y = (TI)v.y;
-			t.z = (TI)v.z;
-			t.w = (TI)v.w;
-			Q.K[k] = t;
-		}
-		for (int dof = tid; dof < 2 * Q.nno; dof += nth) {
-			double D = 0.0;
-			for (int i = Q.dg_off[dof]; i < Q.dg_off[dof + 1]; i++) {
-				const double4 kb = Q.K64[(size_t)Q.dg_slot[i] * Q.nno + Q.dg_node[i]];
-				D += Q.dg_w[i] * ((dof & 1) ? kb.w : kb.x);
+		const double *K64f = reinterpret_cast<const double *>(Q.K64);
+		TI *Krf = reinterpret_cast<TI *>(Q.Kr);
+		for (int A = tid; A < Q.nno; A += nth) {
+			for (int u = 0; u < Q.rnbw; u++) {
+				const size_t b = ((size_t)u * Q.nno + A) * 4;
+				Krf[b] = Krf[b + 1] = Krf[b + 2] = Krf[b + 3] = TI(0);
 			}
-			Q.invD[dof] = Q.kind[dof] == 1 && D > 0.0 ? (TI)(1.0 / D) : TI(0);
+			int self = -1;
+			for (int u = 0; u < Q.rcnt[A]; u++)
+				if (Q.rnb[(size_t)u * Q.nno + A] == A)
+					self = u;
+			double dgl[2] = {0.0, 0.0};
+			const int i1 = Q.rc_off[A + 1];
+			for (int i = Q.rc_off[A]; i < i1;) {
+				const int t = Q.rc_tgt[i];
+				double v = 0.0;
+				for (; i < i1 && Q.rc_tgt[i] == t; i++)
+					v += (double)Q.rc_w[i] * K64f[Q.rc_src[i]];
+				const int slot = t >> 2, cc = t & 3;
+				Krf[((size_t)slot * Q.nno + A) * 4 + cc] = (TI)v;
+				if (slot == self && (cc == 0 || cc == 3))
+					dgl[cc == 3] = v;
+			}
+			for (int c = 0; c < 2; c++)
+				Q.invD[2 * A + c] = Q.kind[2 * A + c] == 1 && dgl[c] > 0.0 ? (TI)(1.0 / dgl[c]) : TI(0);
 		}
 	}
 	g.sync();

@@ -30,14 +30,17 @@ struct QtLevel {
 	const int *nb;                          // [nbw*nno] matrix neighbours (flagged, see kQtCon)
 	const unsigned char *cnt;               // [nno] neighbours of each node
 	const double4 *K64;                     // [nbw*nno] FP64 blocks assembled this step
-	typename V4T<T>::t *K;                  // [nbw*nno] the same in T
 	const unsigned char *kind;              // [2*nno] 0 fixed, 1 reduced, 2 constrained
 	const int *ex_off, *ex_src;             // [2*nno+1] constrained dof = sum ex_w * x[ex_src]
 	const T *ex_w;
 	const int *fo_off, *fo_dof;             // [2*nno+1] reduced dof <- constrained dofs holding it
 	const T *fo_w;
-	const int *dg_off, *dg_node, *dg_slot;  // diagonal of C^T K C
-	const double *dg_w;
+	int rnbw;                               // C^T K C as node-block ELL over reduced columns:
+	const int *rnb;                         // [rnbw*nno] columns (padded with the row node)
+	const unsigned char *rcnt;              // [nno] columns per row
+	const int *rc_off, *rc_tgt, *rc_src;    // its assembly from K64 (see mclg_qt_level)
+	const float *rc_w;
+	typename V4T<T>::t *Kr;                 // [rnbw*nno] the assembled blocks in T
 	const int *p_off, *p_src;               // prolongation from the level below (rows: this level)
 	const T *p_w;
 	const int *r_off, *r_src;               // restriction from the level above (rows: this level)

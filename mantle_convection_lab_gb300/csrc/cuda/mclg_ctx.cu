@@ -757,12 +757,19 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 			CK(dev_upload(c, (int **)&Q.nb, nbf));
 			CK(dev_upload(c, (unsigned char **)&Q.cnt, cnt));
 		}
-		K4 *Kt = NULL;
+		K4 *Kr = NULL;
 		TI *invD = NULL;
-		CK(dev_zeros(c, &Kt, nk));
+		CK(dev_zeros(c, &Kr, (size_t)S.rnbw * nn));
 		CK(dev_zeros(c, &invD, 2 * nn));
-		Q.K = Kt;
+		Q.Kr = Kr;
 		Q.invD = invD;
+		Q.rnbw = S.rnbw;
+		CK(dev_upload_n(c, (int **)&Q.rnb, S.rnb, (size_t)S.rnbw * nn));
+		CK(dev_upload_n(c, (unsigned char **)&Q.rcnt, S.rcnt, nn));
+		CK(dev_upload_n(c, (int **)&Q.rc_off, S.rc_off, nn + 1));
+		CK(dev_upload_n(c, (int **)&Q.rc_tgt, S.rc_tgt, (size_t)S.n_rc));
+		CK(dev_upload_n(c, (int **)&Q.rc_src, S.rc_src, (size_t)S.n_rc));
+		CK(dev_upload_cast(c, (float **)&Q.rc_w, S.rc_w, (size_t)S.n_rc));
 		const size_t nd = 2 * nn;
 		CK(dev_upload_n(c, (unsigned char **)&Q.kind, S.kind, nd));
 		CK(dev_upload_n(c, (int **)&Q.ex_off, S.ex_off, nd + 1));
@@ -771,10 +778,6 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 		CK(dev_upload_n(c, (int **)&Q.fo_off, S.fo_off, nd + 1));
 		CK(dev_upload_n(c, (int **)&Q.fo_dof, S.fo_dof, (size_t)S.n_fo));
 		CK(dev_upload_cast(c, (TI **)&Q.fo_w, S.fo_w, (size_t)S.n_fo));
-		CK(dev_upload_n(c, (int **)&Q.dg_off, S.dg_off, nd + 1));
-		CK(dev_upload_n(c, (int **)&Q.dg_node, S.dg_node, (size_t)S.n_dg));
-		CK(dev_upload_n(c, (int **)&Q.dg_slot, S.dg_slot, (size_t)S.n_dg));
-		CK(dev_upload_n(c, (double **)&Q.dg_w, S.dg_w, (size_t)S.n_dg));
 		if (k > 0) {
 			CK(dev_upload_n(c, (int **)&Q.p_off, S.p_off, nd + 1));
 			CK(dev_upload_n(c, (int **)&Q.p_src, S.p_src, (size_t)S.n_p));
@@ -2528,6 +2531,47 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 		rc = mclg_amr_transfer(&c->mesh, T_old.data(), &n->mesh, T_new.data());
 	if (rc == MCLG_OK)
 		rc = mclg_set_field(n, MCLG_F_T, -1, T_new.data(), T_new.size());
+	// converged solvers: the velocity (bilinear, as T) and the pressure (the old element
+	// holding the new element's centre) start the first solve on the new mesh; the FP64
+	// replica starts as the reference does (d = 0, p = 0 on a new mesh)
+	const bool carry = cfg.precision != 0;
+	const mclg_level &HN = n->mesh.lev[n->fl], &HO = c->mesh.lev[c->fl];
+	const size_t nn2 = (size_t)HN.nno, ne2 = (size_t)HN.nel;
+	std::vector<double> V_old(nn), V_new(nn2), d_new((size_t)(HN.neq > 0 ? HN.neq : 1), 0.0);
+	for (int comp = 0; comp < 2 && rc == MCLG_OK && carry; comp++) {
+		rc = mclg_get_field(c, comp ? MCLG_F_V1 : MCLG_F_V0, -1, V_old.data(), nn);
+		if (rc == MCLG_OK)
+			rc = mclg_amr_transfer(&c->mesh, V_old.data(), &n->mesh, V_new.data());
+		if (rc == MCLG_OK)
+			rc = mclg_set_field(n, comp ? MCLG_F_V1 : MCLG_F_V0, -1, V_new.data(), nn2);
+		for (size_t A = 0; A < nn2 && rc == MCLG_OK; A++) {
+			const int eq = HN.id[(size_t)comp * nn2 + A];
+			if (eq >= 0)
+				d_new[eq] = V_new[A];
+		}
+	}
+	if (rc == MCLG_OK && carry && HN.neq > 0)
+		rc = mclg_set_field(n, MCLG_F_D, -1, d_new.data(), (size_t)HN.neq);
+	if (rc == MCLG_OK && carry) {
+		std::vector<double> P_old(ne), P_new(ne2);
+		rc = mclg_get_field(c, MCLG_F_P, -1, P_old.data(), ne);
+		const int ncell = c->mesh.gnox - 1;
+		const double dxc = c->mesh.length / ncell, dzc = c->mesh.height / ncell;
+		for (size_t e = 0; e < ne2 && rc == MCLG_OK; e++) {
+			double x = 0.0, z = 0.0;
+			for (int a = 0; a < 4; a++) {
+				const int A = HN.ienl[(size_t)a * ne2 + e];
+				x += 0.25 * HN.X[A];
+				z += 0.25 * HN.X[nn2 + A];
+			}
+			int cx = (int)(x / dxc), cz = (int)(z / dzc);
+			cx = cx < 0 ? 0 : cx >= ncell ? ncell - 1 : cx;
+			cz = cz < 0 ? 0 : cz >= ncell ? ncell - 1 : cz;
+			P_new[e] = P_old[HO.cell_elem[(size_t)cx * ncell + cz]];
+		}
+		if (rc == MCLG_OK)
+			rc = mclg_set_field(n, MCLG_F_P, -1, P_new.data(), ne2);
+	}
 	if (rc == MCLG_OK) {
 		cudaError_t e = cudaMemcpyAsync(n->sc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToDevice, n->st);
 		if (e == cudaSuccess)

@@ -92,7 +92,12 @@ typedef struct mclg_qt_level {
 	int *r_off, *r_src;               /* restriction from the level above (rows: this level's dofs) */
 	double *r_w;
 	int *node_map;                    /* [nno] the same node on the level above (NULL on the finest) */
-	int n_ex, n_fo, n_dg, n_p, n_r;
+	int rnbw;                         /* C^T K C as node-block ELL over reduced columns: width, */
+	int *rnb;                         /* [rnbw*nno] columns (padded with the row node), */
+	unsigned char *rcnt;              /* [nno] columns per row, */
+	int *rc_off, *rc_tgt, *rc_src;    /* per row: entry (4*slot + 2c + c') += rc_w * K[rc_src] (K as */
+	double *rc_w;                     /* flat doubles, 4 per block) */
+	int n_ex, n_fo, n_dg, n_p, n_r, n_rc;
 } mclg_qt_level;
 /* levels lo..max_level-1 into q[0..]; lo > min_level-1 and below the finest */
 int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q);

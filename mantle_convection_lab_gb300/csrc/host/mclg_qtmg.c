@@ -139,6 +139,12 @@ void mclg_qt_free(mclg_qt_level *q)
 	free_csr(&q->p_off, &q->p_src, &q->p_w);
 	free_csr(&q->r_off, &q->r_src, &q->r_w);
 	free(q->node_map);
+	free(q->rnb);
+	free(q->rcnt);
+	free(q->rc_off);
+	free(q->rc_tgt);
+	free(q->rc_src);
+	free(q->rc_w);
 	memset(q, 0, sizeof *q);
 }
 
@@ -380,6 +386,171 @@ static int build_restriction(const mclg_qt_level *up, mclg_qt_level *lo)
 	return MCLG_OK;
 }
 
+/* The reduced operator C^T K C of a level as node-block ELL rows over reduced
+ * columns, assembled on the device each step from K by a per-row list of
+ * contributions: entry (slot s, component pair cc) of row A accumulates
+ * w * K[k][j].cc for every row j holding A (A itself, weight 1, and the
+ * constrained dofs folded into A) and every column of row j expanded into
+ * reduced dofs. */
+typedef struct {
+	int B, tgt, src;
+	double w;
+} contrib;
+
+static int cmp_contrib(const void *a, const void *b)
+{
+	const contrib *x = (const contrib *)a, *y = (const contrib *)b;
+	if (x->tgt != y->tgt)
+		return x->tgt < y->tgt ? -1 : 1;
+	return x->src < y->src ? -1 : x->src > y->src;
+}
+
+static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
+{
+	const int nno = L->nno;
+	contrib *row = NULL;
+	long rn = 0, rcap = 0, tot = 0, tcap = 0;
+	int *cols = NULL, ncols, maxw = 1, rc = MCLG_BAD_INPUT;
+	int **rnb_rows = NULL, *rcnt = NULL;
+	q->rc_off = (int *)calloc((size_t)nno + 1, sizeof(int));
+	rnb_rows = (int **)calloc((size_t)nno, sizeof(int *));
+	rcnt = (int *)calloc((size_t)nno, sizeof(int));
+	cols = (int *)malloc(512 * sizeof(int));
+	if (!q->rc_off || !rnb_rows || !rcnt || !cols)
+		goto out;
+	for (int A = 0; A < nno; A++) {
+		rn = 0;
+		for (int c = 0; c < 2; c++) {
+			const int da = 2 * A + c;
+			if (q->kind[da] != 1)
+				continue;
+			/* rows holding dof (A,c): itself and the constrained dofs folded into it */
+			for (int t = -1; t < q->fo_off[da + 1] - q->fo_off[da]; t++) {
+				const int jd = t < 0 ? da : q->fo_dof[q->fo_off[da] + t];
+				const double wj = t < 0 ? 1.0 : q->fo_w[q->fo_off[da] + t];
+				const int j = jd >> 1;
+				for (int k = 0; k < L->nb_cnt[j]; k++) {
+					const int B = L->nb[(size_t)k * nno + j];
+					for (int c2 = 0; c2 < 2; c2++) {
+						const int db = 2 * B + c2;
+						const int src = (int)(((size_t)k * nno + j) * 4 + (size_t)(c * 2 + c2));
+						int ni = 1, first = 0;
+						if (q->kind[db] == 0)
+							continue;
+						if (q->kind[db] == 2) {
+							first = q->ex_off[db];
+							ni = q->ex_off[db + 1] - first;
+						}
+						for (int i = 0; i < ni; i++) {
+							const int Bp = q->kind[db] == 2 ? q->ex_src[first + i] >> 1 : B;
+							const double wb = q->kind[db] == 2 ? q->ex_w[first + i] : 1.0;
+							if (rn == rcap) {
+								long cap = rcap ? 2 * rcap : 256;
+								contrib *r2 = (contrib *)realloc(row, (size_t)cap * sizeof(contrib));
+								if (r2 == NULL)
+									goto out;
+								row = r2;
+								rcap = cap;
+							}
+							row[rn].B = Bp;
+							row[rn].tgt = c * 2 + c2;   /* slot added below */
+							row[rn].src = src;
+							row[rn].w = wj * wb;
+							rn++;
+						}
+					}
+				}
+			}
+		}
+		/* the row's reduced columns, sorted; the node itself first when present */
+		ncols = 0;
+		for (long i = 0; i < rn; i++) {
+			int f = 0;
+			for (int u = 0; u < ncols; u++)
+				if (cols[u] == row[i].B) {
+					f = 1;
+					break;
+				}
+			if (!f) {
+				if (ncols == 512)
+					goto out;
+				cols[ncols++] = row[i].B;
+			}
+		}
+		for (int u = 1; u < ncols; u++)
+			for (int v = u; v > 0 && cols[v - 1] > cols[v]; v--) {
+				int t = cols[v];
+				cols[v] = cols[v - 1];
+				cols[v - 1] = t;
+			}
+		for (long i = 0; i < rn; i++) {
+			int slot = 0;
+			while (cols[slot] != row[i].B)
+				slot++;
+			row[i].tgt += 4 * slot;
+		}
+		qsort(row, (size_t)rn, sizeof(contrib), cmp_contrib);
+		if (ncols > maxw)
+			maxw = ncols;
+		rcnt[A] = ncols;
+		rnb_rows[A] = (int *)malloc((size_t)(ncols > 0 ? ncols : 1) * sizeof(int));
+		if (rnb_rows[A] == NULL)
+			goto out;
+		memcpy(rnb_rows[A], cols, (size_t)ncols * sizeof(int));
+		q->rc_off[A] = (int)tot;
+		if (tot + rn > tcap) {
+			long cap = tcap ? 2 * tcap : 4096;
+			while (cap < tot + rn)
+				cap *= 2;
+			int *t1 = (int *)realloc(q->rc_tgt, (size_t)cap * sizeof(int));
+			if (t1)
+				q->rc_tgt = t1;
+			int *t2 = (int *)realloc(q->rc_src, (size_t)cap * sizeof(int));
+			if (t2)
+				q->rc_src = t2;
+			double *t3 = (double *)realloc(q->rc_w, (size_t)cap * sizeof(double));
+			if (t3)
+				q->rc_w = t3;
+			if (!t1 || !t2 || !t3)
+				goto out;
+			tcap = cap;
+		}
+		for (long i = 0; i < rn; i++) {
+			q->rc_tgt[tot] = row[i].tgt;
+			q->rc_src[tot] = row[i].src;
+			q->rc_w[tot] = row[i].w;
+			tot++;
+		}
+	}
+	q->rc_off[nno] = (int)tot;
+	q->n_rc = (int)tot;
+	q->rnbw = maxw;
+	q->rnb = (int *)malloc((size_t)maxw * nno * sizeof(int));
+	q->rcnt = (unsigned char *)malloc((size_t)nno);
+	if (!q->rnb || !q->rcnt || maxw > 255)
+		goto out;
+	for (int A = 0; A < nno; A++) {
+		q->rcnt[A] = (unsigned char)rcnt[A];
+		for (int u = 0; u < maxw; u++)
+			q->rnb[(size_t)u * nno + A] = u < rcnt[A] ? rnb_rows[A][u] : A;
+	}
+	if (q->rc_tgt == NULL) {   /* no reduced dof at all */
+		q->rc_tgt = (int *)malloc(sizeof(int));
+		q->rc_src = (int *)malloc(sizeof(int));
+		q->rc_w = (double *)malloc(sizeof(double));
+	}
+	rc = MCLG_OK;
+out:
+	if (rnb_rows)
+		for (int A = 0; A < nno; A++)
+			free(rnb_rows[A]);
+	free(rnb_rows);
+	free(rcnt);
+	free(cols);
+	free(row);
+	return rc;
+}
+
 int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q)
 {
 	const int top = m->max_level - 1;
@@ -390,6 +561,8 @@ int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q)
 		mclg_qt_level *Q = &q[lev - lo];
 		memset(Q, 0, sizeof *Q);
 		if ((rc = build_constraints(&m->lev[lev], Q)) != MCLG_OK)
+			return rc;
+		if ((rc = build_reduced_operator(&m->lev[lev], Q)) != MCLG_OK)
 			return rc;
 		/* node_map: this level's node -> the same node one level up (every node of a
 		 * level exists on the finer levels) */
