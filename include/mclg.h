@@ -88,7 +88,9 @@ typedef struct mclg_config {
 	/* GB300 solver options (not in the reference) */
 	int precision;           /* 0 "fp64": FP64 replica of the reference's iteration;
 	                            1 "mixed": FP32 multigrid-preconditioned inner CG inside the
-	                                FP64 Uzawa loop and FP64 iterative refinement (uniform meshes);
+	                                FP64 Uzawa loop and FP64 iterative refinement (on a refined mesh:
+	                                MINRES with an FP32 V-cycle on the mesh's levels, conforming
+	                                hanging-node space);
 	                            2 "fp64mg": the same converged solver with FP64 inner solves */
 	double stokes_rtol;      /* converged solvers: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
 	int warm_start;          /* converged solvers: 0 zero, 1 the previous step's (d,p), 2 d=0 and p kept
