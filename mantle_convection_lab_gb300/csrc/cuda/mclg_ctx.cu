@@ -213,7 +213,10 @@ static int upload_level_into(mclg_ctx *c, int lev, DevLevelBuf &b, DevLevel &L)
 	CK(upload(&b.hang_ni, H.hang_ni, nh, st));
 	CK(upload(&b.hang_ci0, H.hang_ci0, nh, st));
 	CK(upload(&b.hang_ci1, H.hang_ci1, nh, st));
-	CK(upload(&b.cell_elem, H.cell_elem, (size_t)(m.gnox - 1) * (m.gnoz - 1), st));
+	if (H.cell_elem != NULL)
+		CK(upload(&b.cell_elem, H.cell_elem, (size_t)(m.gnox - 1) * (m.gnoz - 1), st));
+	else
+		CK(dalloc(&b.cell_elem, 1));
 	CK(upload(&b.dxh, H.dx_dxi, ne, st));
 	CK(upload(&b.dzh, H.dz_deta, ne, st));
 	CK(upload(&b.jac, H.jacobi, ne, st));

@@ -23,6 +23,8 @@ typedef struct mclg_level {
 	int nel, nno;
 	int *Mcode;            /* [nel]  (morton << 4) | element level             Tree.c:340-358 */
 	int *node;             /* [nno]  sorted global node ids                    Construct_ien_id_lm.c:43-66 */
+	int *node_lut;         /* [lut_n] global id -> index or -1 (grids of up to 4M ids; else NULL) */
+	long lut_n;
 	int *ien;              /* [4*nel] global node ids, ien[a*nel + e]          Construct_ien_id_lm.c:3-41 */
 	int *ienl;             /* [4*nel] local node indices (node_index(ien))     */
 	int *elev;             /* [nel]  element level (Mcode_lev)                 */
@@ -85,8 +87,6 @@ typedef struct mclg_qt_level {
 	double *ex_w;
 	int *fo_off, *fo_dof;             /* fold: reduced dof <- constrained dofs holding it */
 	double *fo_w;
-	int *dg_off, *dg_node, *dg_slot;  /* diagonal of C^T K C: sum dg_w * K[dg_slot][dg_node] */
-	double *dg_w;
 	int *p_off, *p_src;               /* prolongation from the level below (rows: this level's dofs) */
 	double *p_w;
 	int *r_off, *r_src;               /* restriction from the level above (rows: this level's dofs) */
@@ -97,7 +97,7 @@ typedef struct mclg_qt_level {
 	unsigned char *rcnt;              /* [nno] columns per row, */
 	int *rc_off, *rc_tgt, *rc_src;    /* per row: entry (4*slot + 2c + c') += rc_w * K[rc_src] (K as */
 	double *rc_w;                     /* flat doubles, 4 per block) */
-	int n_ex, n_fo, n_dg, n_p, n_r, n_rc;
+	int n_ex, n_fo, n_p, n_r, n_rc;
 } mclg_qt_level;
 /* levels lo..max_level-1 into q[0..]; lo > min_level-1 and below the finest */
 int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q);

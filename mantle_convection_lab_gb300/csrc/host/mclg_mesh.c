@@ -20,6 +20,7 @@
 #include <string.h>
 #include <stdarg.h>
 #include <math.h>
+#include <pthread.h>
 #include "mclg_host.h"
 #include "mclg_ic.h"
 
@@ -240,6 +241,8 @@ static int initial_refine(tree_ctx *t, ivec *head, int dev_mode, int max_level)
 
 int mclg_node_index(const mclg_level *L, int gid)
 {
+	if (L->node_lut != NULL)
+		return gid >= 0 && gid < L->lut_n ? L->node_lut[gid] : -1;
 	int lo = 0, hi = L->nno - 1;
 	while (lo <= hi) {
 		int mid = lo + ((hi - lo) >> 1);
@@ -277,11 +280,35 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 		L->ien[2L * ne + e] = node + step + step * gnoz;
 		L->ien[3L * ne + e] = node + step * gnoz;
 	}
-	/* node list (Construct_ien_id_lm.c:43-66) */
-	for (k = 0; k < 4L * ne; k++)
-		if (ivec_push(&nodes, L->ien[k]) != 0)
+	/* node list (Construct_ien_id_lm.c:43-66): the sorted distinct ids of ien.
+	 * Grids of up to 4M node ids keep a direct id -> index table, which also
+	 * serves node_index; larger ones sort and binary-search. */
+	if ((long)gnox * gnoz <= (1L << 22)) {
+		const long ng = (long)gnox * gnoz;
+		L->lut_n = ng;
+		L->node_lut = (int *)malloc((size_t)ng * sizeof(int));
+		if (L->node_lut == NULL)
 			goto oom;
-	nn = sort_unique(nodes.a, nodes.n);
+		memset(L->node_lut, 0xff, (size_t)ng * sizeof(int));
+		for (k = 0; k < 4L * ne; k++)
+			L->node_lut[L->ien[k]] = 0;
+		nn = 0;
+		for (long g = 0; g < ng; g++)
+			if (L->node_lut[g] == 0)
+				nn++;
+		ALLOC(nodes.a, nn);
+		nn = 0;
+		for (long g = 0; g < ng; g++)
+			if (L->node_lut[g] == 0) {
+				nodes.a[nn] = (int)g;
+				L->node_lut[g] = (int)nn++;
+			}
+	} else {
+		for (k = 0; k < 4L * ne; k++)
+			if (ivec_push(&nodes, L->ien[k]) != 0)
+				goto oom;
+		nn = sort_unique(nodes.a, nodes.n);
+	}
 	L->nno = (int)nn;
 	L->node = nodes.a;
 	ALLOC(L->ienl, 4L * ne);
@@ -487,8 +514,9 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 				}
 			}
 	}
-	/* fine cell -> covering element (used by the horizontal average) */
-	{
+	/* fine cell -> covering element (the horizontal average and the field
+	 * transfers of the finest level; coarser levels do not need it) */
+	if (lev == fl) {
 		long ncx = gnox - 1, ncz = gnoz - 1;
 		ALLOC(L->cell_elem, ncx * ncz);
 		for (e = 0; e < ne; e++) {
@@ -507,6 +535,22 @@ oom:
 /* leaves != NULL: the finest-level Morton start codes of a given leaf set
  * (sorted, covering the domain) replace initial_refine; the last leaf's level
  * then comes from the codes left to the end of the domain. */
+typedef struct {
+	mclg_mesh *m;
+	const mclg_config *c;
+	int lev, rc;
+	char err[512];
+} lvl_job;
+
+static void *level_worker(void *p)
+{
+	lvl_job *j = (lvl_job *)p;
+	j->rc = build_level_arrays(j->m, j->c, j->lev);
+	if (j->rc != MCLG_OK)
+		snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+	return NULL;
+}
+
 static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves, long nleaves)
 {
 	int lev, fl, rc;
@@ -603,10 +647,28 @@ static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves
 			D->Mcode[D->nel++] = (loc << MCLG_LEVEL_BITS) | level;
 		}
 	}
-	for (lev = m->min_level; lev < m->max_level; lev++) {
-		rc = build_level_arrays(m, c, lev);
-		if (rc != MCLG_OK)
-			return rc;
+	{   /* the levels' arrays are independent of one another: one thread per level */
+		lvl_job jobs[MCLG_MAX_LEVEL];
+		pthread_t th[MCLG_MAX_LEVEL];
+		int started[MCLG_MAX_LEVEL], i, nl = m->max_level - m->min_level;
+		for (i = 0; i < nl; i++) {
+			jobs[i].m = m;
+			jobs[i].c = c;
+			jobs[i].lev = m->min_level + i;
+			jobs[i].rc = MCLG_OK;
+			jobs[i].err[0] = 0;
+			started[i] = pthread_create(&th[i], NULL, level_worker, &jobs[i]) == 0;
+			if (!started[i])
+				level_worker(&jobs[i]);
+		}
+		for (i = 0; i < nl; i++)
+			if (started[i])
+				pthread_join(th[i], NULL);
+		for (i = 0; i < nl; i++)
+			if (jobs[i].rc != MCLG_OK) {
+				mclg_set_error("%s", jobs[i].err);
+				return jobs[i].rc;
+			}
 	}
 	{
 		mclg_level *L = &m->lev[fl];
@@ -640,7 +702,7 @@ void mclg_mesh_free(mclg_mesh *m)
 		free(L->T_bc_val); free(L->X); free(L->dx_dxi); free(L->dz_deta); free(L->jacobi);
 		free(L->area); free(L->hang_node); free(L->hang_c0); free(L->hang_c1); free(L->hang_ni);
 		free(L->hang_ci0); free(L->hang_ci1); free(L->p2n_cnt); free(L->p2n_el); free(L->p2n_a);
-		free(L->nb); free(L->nb_cnt); free(L->kslot); free(L->cell_elem);
+		free(L->nb); free(L->nb_cnt); free(L->kslot); free(L->cell_elem); free(L->node_lut);
 	}
 	memset(m, 0, sizeof *m);
 }

@@ -17,14 +17,16 @@
  *             corrections this structure is used for)
  *   fold      the transpose: for a reduced dof, the constrained dofs whose
  *             expansion holds it, with the same weights
- *   diag      terms of the constrained operator's diagonal:
- *             D_a = sum w * K[row node][slot] (component c,c)
+ *   C^T K C   the reduced operator as node-block ELL rows, assembled on the
+ *             device each step from per-row contribution lists
  *   P         prolongation from the level below to this level's reduced dofs:
  *             the reference's averaging map (build_interp_conn,
  *             Connection.c:708-930) applied to the coarse expanded field
  *   R         restriction to this level from the level above, P^T by rows.
  * All lists are CSR by dof, built in ascending order so device gathers sum in
  * a fixed order. */
+#include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -110,15 +112,6 @@ static int expand_dof(const mclg_level *L, const int *hang_of, int dof, double w
 	return expand_dof(L, hang_of, 2 * L->hang_ci1[h] + c, 0.5 * w, depth + 1, out);
 }
 
-static int slot_of(const mclg_level *L, int row, int col)
-{
-	int k;
-	for (k = 0; k < L->nb_cnt[row]; k++)
-		if (L->nb[(size_t)k * L->nno + row] == col)
-			return k;
-	return -1;
-}
-
 static void free_csr(int **off, int **idx, double **w)
 {
 	free(*off);
@@ -134,8 +127,6 @@ void mclg_qt_free(mclg_qt_level *q)
 	free(q->kind);
 	free_csr(&q->ex_off, &q->ex_src, &q->ex_w);
 	free_csr(&q->fo_off, &q->fo_dof, &q->fo_w);
-	free_csr(&q->dg_off, &q->dg_slot, &q->dg_w);
-	free(q->dg_node);
 	free_csr(&q->p_off, &q->p_src, &q->p_w);
 	free_csr(&q->r_off, &q->r_src, &q->r_w);
 	free(q->node_map);
@@ -156,21 +147,18 @@ static int take(csr_b *b, int **idx, double **w)
 	return (*idx && *w) ? 0 : -1;
 }
 
-/* kind, expand, fold and diag terms of one level */
+/* kind, expand and fold lists of one level */
 static int build_constraints(const mclg_level *L, mclg_qt_level *q)
 {
 	const int nno = L->nno, nd = 2 * nno;
 	int *hang_of = (int *)malloc((size_t)nno * sizeof(int));
-	csr_b ex = {0}, fo = {0}, dg = {0};
-	int *dg_node_tmp = NULL;
-	long dgn = 0, dgcap = 0;
+	csr_b ex = {0}, fo = {0};
 	int rc = MCLG_BAD_INPUT, h, d, i;
 	q->nno = nno;
 	q->kind = (unsigned char *)calloc((size_t)nd + 1, 1);
 	q->ex_off = (int *)calloc((size_t)nd + 1, sizeof(int));
 	q->fo_off = (int *)calloc((size_t)nd + 1, sizeof(int));
-	q->dg_off = (int *)calloc((size_t)nd + 1, sizeof(int));
-	if (!hang_of || !q->kind || !q->ex_off || !q->fo_off || !q->dg_off)
+	if (!hang_of || !q->kind || !q->ex_off || !q->fo_off)
 		goto out;
 	for (i = 0; i < nno; i++)
 		hang_of[i] = -1;
@@ -226,65 +214,21 @@ static int build_constraints(const mclg_level *L, mclg_qt_level *q)
 			}
 		free(cnt);
 	}
-	/* diagonal terms of C^T K C at each reduced dof: (row node, slot, weight) */
-	for (d = 0; d < nd; d++) {
-		q->dg_off[d] = (int)dg.n;
-		if (q->kind[d] != 1)
-			continue;
-		int sup[65];
-		double sw[65];
-		int ns = 1;
-		sup[0] = d;
-		sw[0] = 1.0;
-		for (int k = q->fo_off[d]; k < q->fo_off[d + 1] && ns < 65; k++) {
-			sup[ns] = fo.idx[k];
-			sw[ns] = fo.w[k];
-			ns++;
-		}
-		for (int a = 0; a < ns; a++)
-			for (int b = 0; b < ns; b++) {
-				const int row = sup[a] >> 1, col = sup[b] >> 1;
-				const int k = slot_of(L, row, col);
-				if (k < 0)
-					continue;
-				if (csr_push(&dg, k, sw[a] * sw[b]))
-					goto out;
-				if (dgn == dgcap) {
-					long cap = dgcap ? 2 * dgcap : 256;
-					int *t2 = (int *)realloc(dg_node_tmp, (size_t)cap * sizeof(int));
-					if (t2 == NULL)
-						goto out;
-					dg_node_tmp = t2;
-					dgcap = cap;
-				}
-				dg_node_tmp[dgn++] = row;
-			}
-	}
-	q->dg_off[nd] = (int)dg.n;
-	if (take(&ex, &q->ex_src, &q->ex_w) || take(&fo, &q->fo_dof, &q->fo_w) ||
-	    take(&dg, &q->dg_slot, &q->dg_w))
+	if (take(&ex, &q->ex_src, &q->ex_w) || take(&fo, &q->fo_dof, &q->fo_w))
 		goto out;
 	ex.idx = NULL;
 	ex.w = NULL;
 	fo.idx = NULL;
 	fo.w = NULL;
-	dg.idx = NULL;
-	dg.w = NULL;
-	q->dg_node = dg_node_tmp ? dg_node_tmp : (int *)malloc(sizeof(int));
-	dg_node_tmp = NULL;
 	q->n_ex = q->ex_off[nd];
 	q->n_fo = q->fo_off[nd];
-	q->n_dg = q->dg_off[nd];
-	rc = q->dg_node ? MCLG_OK : MCLG_BAD_INPUT;
+	rc = MCLG_OK;
 out:
 	free(hang_of);
 	free(ex.idx);
 	free(ex.w);
 	free(fo.idx);
 	free(fo.w);
-	free(dg.idx);
-	free(dg.w);
-	free(dg_node_tmp);
 	return rc;
 }
 
@@ -420,6 +364,43 @@ static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
 		goto out;
 	for (int A = 0; A < nno; A++) {
 		rn = 0;
+		/* the common row: nothing folded into it and no constrained column, so
+		 * its reduced row is K's row, in K's (sorted) column order */
+		int plain = q->fo_off[2 * A + 2] == q->fo_off[2 * A];
+		for (int k = 0; plain && k < L->nb_cnt[A]; k++) {
+			const int B = L->nb[(size_t)k * nno + A];
+			plain = q->kind[2 * B] != 2 && q->kind[2 * B + 1] != 2;
+		}
+		if (plain) {
+			ncols = 0;
+			for (int k = 0; k < L->nb_cnt[A]; k++) {
+				const int B = L->nb[(size_t)k * nno + A];
+				if (q->kind[2 * B] == 0 && q->kind[2 * B + 1] == 0)
+					continue;
+				for (int cc = 0; cc < 4; cc++) {
+					const int c = cc >> 1, c2 = cc & 1;
+					if (q->kind[2 * A + c] != 1 || q->kind[2 * B + c2] != 1)
+						continue;
+					if (rn == rcap) {
+						long cap = rcap ? 2 * rcap : 256;
+						contrib *r2 = (contrib *)realloc(row, (size_t)cap * sizeof(contrib));
+						if (r2 == NULL)
+							goto out;
+						row = r2;
+						rcap = cap;
+					}
+					row[rn].B = B;
+					row[rn].tgt = 4 * ncols + cc;
+					row[rn].src = (int)(((size_t)k * nno + A) * 4 + (size_t)cc);
+					row[rn].w = 1.0;
+					rn++;
+				}
+				if (ncols == 512)
+					goto out;
+				cols[ncols++] = B;
+			}
+			goto row_done;
+		}
 		for (int c = 0; c < 2; c++) {
 			const int da = 2 * A + c;
 			if (q->kind[da] != 1)
@@ -490,6 +471,7 @@ static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
 			row[i].tgt += 4 * slot;
 		}
 		qsort(row, (size_t)rn, sizeof(contrib), cmp_contrib);
+	row_done:
 		if (ncols > maxw)
 			maxw = ncols;
 		rcnt[A] = ncols;
@@ -551,40 +533,80 @@ out:
 	return rc;
 }
 
-int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q)
+/* one level's lists, run on a thread of its own: phase 0 the constraint lists,
+ * C^T K C and the node map; phase 1 the transfers to the level below */
+typedef struct {
+	const mclg_mesh *m;
+	mclg_qt_level *q;   /* q[0] is level lo */
+	int lo, lev, phase, rc;
+	char err[512];
+} qt_job;
+
+static void *qt_worker(void *p)
 {
-	const int top = m->max_level - 1;
-	int lev, rc;
-	if (lo < m->min_level || lo >= top)
-		return MCLG_BAD_INPUT;
-	for (lev = lo; lev <= top; lev++) {
-		mclg_qt_level *Q = &q[lev - lo];
+	qt_job *j = (qt_job *)p;
+	const mclg_mesh *m = j->m;
+	const int lev = j->lev, top = m->max_level - 1;
+	mclg_qt_level *Q = &j->q[lev - j->lo];
+	j->rc = MCLG_OK;
+	if (j->phase == 0) {
 		memset(Q, 0, sizeof *Q);
-		if ((rc = build_constraints(&m->lev[lev], Q)) != MCLG_OK)
-			return rc;
-		if ((rc = build_reduced_operator(&m->lev[lev], Q)) != MCLG_OK)
-			return rc;
+		if ((j->rc = build_constraints(&m->lev[lev], Q)) == MCLG_OK)
+			j->rc = build_reduced_operator(&m->lev[lev], Q);
 		/* node_map: this level's node -> the same node one level up (every node of a
 		 * level exists on the finer levels) */
-		if (lev < top) {
+		if (j->rc == MCLG_OK && lev < top) {
 			const mclg_level *L = &m->lev[lev], *U = &m->lev[lev + 1];
 			Q->node_map = (int *)malloc((size_t)L->nno * sizeof(int));
 			if (Q->node_map == NULL)
-				return MCLG_BAD_INPUT;
-			for (int A = 0; A < L->nno; A++) {
+				j->rc = MCLG_BAD_INPUT;
+			for (int A = 0; Q->node_map && A < L->nno; A++) {
 				Q->node_map[A] = mclg_node_index(U, L->node[A]);
 				if (Q->node_map[A] < 0) {
 					mclg_set_error("level %d: node %d is missing on level %d", lev, L->node[A], lev + 1);
-					return MCLG_BAD_INPUT;
+					j->rc = MCLG_BAD_INPUT;
+					break;
 				}
 			}
 		}
-		if (lev > lo) {
-			if ((rc = build_prolongation(m, lev, &q[lev - lo - 1], Q)) != MCLG_OK)
-				return rc;
-			if ((rc = build_restriction(Q, &q[lev - lo - 1])) != MCLG_OK)
-				return rc;
+	} else if (lev > j->lo) {
+		if ((j->rc = build_prolongation(m, lev, &j->q[lev - j->lo - 1], Q)) == MCLG_OK)
+			j->rc = build_restriction(Q, &j->q[lev - j->lo - 1]);
+	}
+	if (j->rc != MCLG_OK)
+		snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+	return NULL;
+}
+
+int mclg_qt_build(const mclg_mesh *m, int lo, mclg_qt_level *q)
+{
+	const int top = m->max_level - 1;
+	qt_job jobs[MCLG_MAX_LEVEL];
+	pthread_t th[MCLG_MAX_LEVEL];
+	int started[MCLG_MAX_LEVEL];
+	if (lo < m->min_level || lo >= top)
+		return MCLG_BAD_INPUT;
+	const int nl = top - lo + 1;
+	for (int phase = 0; phase < 2; phase++) {
+		for (int i = 0; i < nl; i++) {
+			jobs[i].m = m;
+			jobs[i].q = q;
+			jobs[i].lo = lo;
+			jobs[i].lev = lo + i;
+			jobs[i].phase = phase;
+			jobs[i].err[0] = 0;
+			started[i] = pthread_create(&th[i], NULL, qt_worker, &jobs[i]) == 0;
+			if (!started[i])
+				qt_worker(&jobs[i]);
 		}
+		for (int i = 0; i < nl; i++)
+			if (started[i])
+				pthread_join(th[i], NULL);
+		for (int i = 0; i < nl; i++)
+			if (jobs[i].rc != MCLG_OK) {
+				mclg_set_error("%s", jobs[i].err);
+				return jobs[i].rc;
+			}
 	}
 	return MCLG_OK;
 }
