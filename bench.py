@@ -71,6 +71,15 @@ WORKLOADS["cfg4_ensemble_256"] = {
             "precision, every model to Stokes residual < 1e-8 every step; one batched solver launch per step",
     "mesh": "256 models, 32^2..256^2",
 }
+WORKLOADS["cfg4_ensemble_amr_256"] = {
+    "input": "mantle_convection_lab_gb300/configs/cfg3_mg_1024.input",
+    "kind": "ensemble", "amr": True,
+    "desc": "configuration 4 with refinement: the 256 members of cfg4_ensemble_256 starting from tanh boundary "
+            "layers with seeded modes, each base grid refined 0-2 levels (seeded) by |grad T| > 0.2 max (2:1, "
+            "hanging nodes); uniform members in one batched launch, refined members by the refined-mesh solver one "
+            "launch each; every member to Stokes residual < 1e-8 every step",
+    "mesh": "256 models, 32^2..256^2 bases + 0-2 levels",
+}
 WORKLOADS["cfg2_amr_128"] = {
     "input": "mantle_convection_lab_gb300/configs/cfg2_amr_128.input",
     "kind": "amr",
@@ -371,8 +380,10 @@ def run_ensemble(args, wl):
     rank, world, local_rank = dist_env()
     dist = init_dist(world, local_rank)
     torch.cuda.set_device(local_rank)
-    e = ensemble.make(256, seed=4)
+    amr_run = wl.get("amr", False)
+    e = ensemble.make_amr(256, seed=4) if amr_run else ensemble.make(256, seed=4)
     n = e.n
+    levels = ensemble.amr_levels(256, 4) if amr_run else None
     # the cluster-size autotuner times one candidate on each of steps 2..6:
     # warm up past it so that the timed steps use its choice
     warmup = max(args.warmup, 7)
@@ -416,6 +427,8 @@ def run_ensemble(args, wl):
         "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic (seeded members)",
         "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
                    "members_by_size": {str(k): sizes.count(k) for k in ensemble.SIZES},
+                   "members_by_refinement_levels": ({str(k): int((levels == k).sum()) for k in (0, 1, 2)}
+                                                    if levels is not None else {"0": n}),
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (256 models)",
                    "solver_ms_per_step": ms_solver / args.steps, "cluster_size_per_step": grids,
                    "inner_per_model_step": inner / (n * args.steps), "max_stokes_residual": res},

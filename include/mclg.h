@@ -335,6 +335,12 @@ int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_
  * stepped alone up to summation order. */
 typedef struct mclg_ensemble mclg_ensemble;
 int mclg_ensemble_create(mclg_ensemble **e, const mclg_config *cfgs, int n);
+/* The same with refined members: member i's configuration gives its base grid
+ * (level-1), refined up to amr_levels[i] levels by |grad T| > 0.2 max of its
+ * initial temperature (2:1 balanced, hanging nodes; 0 = uniform).  Refined
+ * members are solved by the refined-mesh solver, one launch each after the
+ * batched launch of the uniform members. */
+int mclg_ensemble_create_amr(mclg_ensemble **e, const mclg_config *cfgs, const int *amr_levels, int n);
 void mclg_ensemble_destroy(mclg_ensemble *e);
 int mclg_ensemble_size(const mclg_ensemble *e);
 /* Member i as a context (fields, mesh, single operators); owned by the ensemble. */

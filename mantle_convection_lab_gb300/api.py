@@ -153,6 +153,7 @@ def lib():
         "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
+        "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
         "mclg_ensemble_size": (C.c_int, [vp]), "mclg_ensemble_member": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "mclg_ensemble_initial_temperature": (C.c_int, [vp]),
         "mclg_ensemble_step": (C.c_int, [vp, vp, ip]),
@@ -544,12 +545,20 @@ class Model:
 
 class Ensemble:
     """Independent models stepped together: one batched solver launch per step
-    (mclg_ensemble_*).  Members are converged-solver models on uniform meshes."""
+    (mclg_ensemble_*) for the members on uniform meshes; amr_levels[i] > 0 refines
+    member i from its configuration's grid by |grad T| (mclg_ensemble_create_amr)."""
 
-    def __init__(self, configs):
+    def __init__(self, configs, amr_levels=None):
         arr = (Config * len(configs))(*configs)
         self._e = C.c_void_p()
-        _check(lib().mclg_ensemble_create(C.byref(self._e), arr, len(configs)), "ensemble_create")
+        if amr_levels is None:
+            _check(lib().mclg_ensemble_create(C.byref(self._e), arr, len(configs)), "ensemble_create")
+        else:
+            lv = np.ascontiguousarray(amr_levels, np.int32)
+            if lv.size != len(configs):
+                raise MclgError(BAD_INPUT, "amr_levels: one entry per member")
+            _check(lib().mclg_ensemble_create_amr(C.byref(self._e), arr, _iptr(lv), len(configs)),
+                   "ensemble_create_amr")
         self.n = len(configs)
         self.members = []
         for i in range(self.n):

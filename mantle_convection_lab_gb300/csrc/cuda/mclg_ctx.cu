@@ -2192,6 +2192,8 @@ struct mclg_ensemble {
 	float cand_cost[kCand];
 	int cs, grid;          // chosen cluster size and grid
 	long long steps;
+	int nbatch;            // members in the batched launch (uniform meshes)
+	int *amr, namr;        // members on refined meshes, solved one launch each
 };
 
 static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
@@ -2208,7 +2210,7 @@ static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
 	at[0].val.clusterDim.z = 1;
 	lc.attrs = at;
 	lc.numAttrs = 1;
-	void *kargs[] = {&e->dargs, &e->n, &e->queue};
+	void *kargs[] = {&e->dargs, &e->nbatch, &e->queue};
 	return cudaLaunchKernelExC(&lc, stokes_mg_batch_kernel(e->fp64), kargs);
 }
 
@@ -2234,8 +2236,8 @@ static int batch_grid(mclg_ensemble *e, int cs)
 	}
 	if (nc < 1)
 		return 0;
-	if (nc > e->n)
-		nc = e->n;
+	if (nc > e->nbatch)
+		nc = e->nbatch;
 	return (nc < 1 ? 1 : nc) * cs;
 }
 
@@ -2252,6 +2254,7 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 			mclg_destroy(e->m[i]);
 	free(e->m);
 	free(e->order);
+	free(e->amr);
 	if (e->dargs)
 		cudaFree(e->dargs);
 	if (e->queue)
@@ -2264,7 +2267,7 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 	free(e);
 }
 
-int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
+static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const int *amr_levels, int n)
 {
 	if (out == NULL || cfgs == NULL || n < 1)
 		return MCLG_BAD_INPUT;
@@ -2295,23 +2298,59 @@ int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
 		mclg_ensemble_destroy(e);
 		return MCLG_BAD_INPUT;
 	}
+	e->amr = (int *)calloc((size_t)n, sizeof(int));
+	if (e->amr == NULL) {
+		mclg_ensemble_destroy(e);
+		return MCLG_BAD_INPUT;
+	}
 	for (int i = 0; i < n; i++) {
-		int rc = mclg_create(&e->m[i], &cfgs[i]);
+		const int lv = amr_levels ? amr_levels[i] : 0;
+		int rc;
+		if (lv <= 0) {
+			rc = mclg_create(&e->m[i], &cfgs[i]);
+		} else {
+			// a member with refinement: its configuration's grid is the base; the
+			// mesh is refined up to lv levels by |grad T| > 0.2 max of its initial
+			// temperature, as configuration 2's remeshing does
+			mclg_config cf = cfgs[i];
+			const int base = cf.level - 1;
+			cf.level = base + lv + 1;
+			const int F = cf.level - 1;
+			if (lv > 4 || F >= MCLG_MAX_LEVEL - 1 || base < 1) {
+				mclg_set_error("ensemble member %d: %d refinement levels on a %d-level grid", i, lv, base);
+				mclg_ensemble_destroy(e);
+				return MCLG_BAD_INPUT;
+			}
+			std::vector<int> leaves((size_t)1 << (2 * base));
+			for (size_t k = 0; k < leaves.size(); k++)
+				leaves[k] = (int)(k << (2 * (F - base)));
+			rc = create_impl(&e->m[i], &cf, leaves.data(), (long)leaves.size());
+			if (rc == MCLG_OK)
+				rc = mclg_initial_temperature(e->m[i]);
+			if (rc == MCLG_OK)
+				rc = mclg_amr_remesh(e->m[i], 0.2, base, F, NULL);
+		}
 		if (rc != MCLG_OK) {
 			mclg_ensemble_destroy(e);
 			return rc;
 		}
+		if (e->m[i]->qt_on)
+			e->amr[e->namr++] = i;
 	}
 	CKE(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
 	for (int i = 0; i < 4; i++)
 		CKE(cudaEventCreate(&e->ev[i]));
 	// one stream for all members; the solver's element tables are shared
 	// constants, so every member must have the same element aspect ratio
-	const double r0 = e->m[0]->mesh.dz[e->m[0]->fl] / e->m[0]->mesh.dx[e->m[0]->fl];
+	int first = 0;
+	while (first < n && e->m[first]->qt_on)
+		first++;
+	const mclg_ctx *c0 = e->m[first < n ? first : 0];
+	const double r0 = c0->mesh.dz[c0->fl] / c0->mesh.dx[c0->fl];
 	for (int i = 0; i < n; i++) {
 		mclg_ctx *c = e->m[i];
 		const double r = c->mesh.dz[c->fl] / c->mesh.dx[c->fl];
-		if (fabs(r - r0) > 1e-12 * r0) {
+		if (!c->qt_on && fabs(r - r0) > 1e-12 * r0) {
 			mclg_set_error("ensemble member %d: element aspect ratio %g differs from member 0's %g", i, r, r0);
 			mclg_ensemble_destroy(e);
 			return MCLG_BAD_INPUT;
@@ -2321,21 +2360,24 @@ int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
 		c->st = e->st;
 		c->st_borrowed = true;
 	}
+	e->nbatch = 0;
 	for (int i = 0; i < n; i++)
-		e->order[i] = i;
+		if (!e->m[i]->qt_on)
+			e->order[e->nbatch++] = i;
 	auto N0 = [&](int i) { return e->fp64 ? e->m[i]->mgd.N0 : e->m[i]->mgf.N0; };
-	std::stable_sort(e->order, e->order + n, [&](int a, int b) { return N0(a) > N0(b); });
+	std::stable_sort(e->order, e->order + e->nbatch, [&](int a, int b) { return N0(a) > N0(b); });
 	const size_t asz = e->fp64 ? sizeof(MGArgs<double>) : sizeof(MGArgs<float>);
-	std::vector<unsigned char> h(asz * (size_t)n);
-	for (int k = 0; k < n; k++) {
+	std::vector<unsigned char> h(asz * (size_t)(e->nbatch > 0 ? e->nbatch : 1));
+	for (int k = 0; k < e->nbatch; k++) {
 		mclg_ctx *c = e->m[e->order[k]];
 		if (e->fp64)
 			memcpy(&h[asz * k], &c->mgd, asz);
 		else
 			memcpy(&h[asz * k], &c->mgf, asz);
 	}
-	CKE(cudaMalloc(&e->dargs, asz * (size_t)n));
-	CKE(cudaMemcpyAsync(e->dargs, h.data(), asz * (size_t)n, cudaMemcpyHostToDevice, e->st));
+	CKE(cudaMalloc(&e->dargs, asz * (size_t)(e->nbatch > 0 ? e->nbatch : 1)));
+	CKE(cudaMemcpyAsync(e->dargs, h.data(), asz * (size_t)(e->nbatch > 0 ? e->nbatch : 1), cudaMemcpyHostToDevice,
+	                    e->st));
 	CKE(cudaMalloc((void **)&e->queue, sizeof(int)));
 	// 16 blocks per cluster is beyond the portable 8: allowed by an opt-in
 	// attribute, dropped from the candidates where the device refuses it
@@ -2356,6 +2398,18 @@ int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
 #undef CKE
 	*out = e;
 	return MCLG_OK;
+}
+
+int mclg_ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, int n)
+{
+	return ensemble_create(out, cfgs, NULL, n);
+}
+
+int mclg_ensemble_create_amr(mclg_ensemble **out, const mclg_config *cfgs, const int *amr_levels, int n)
+{
+	if (amr_levels == NULL)
+		return MCLG_BAD_INPUT;
+	return ensemble_create(out, cfgs, amr_levels, n);
 }
 
 int mclg_ensemble_size(const mclg_ensemble *e)
@@ -2394,7 +2448,9 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	CK(cudaEventRecord(e->ev[0], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
-		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
+		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)))
+			return rc;
+		if (!c->qt_on && (rc = stokes_mg_prepare(c)))
 			return rc;
 	}
 	// autotuner: steps 2, 3, ... (the warm start settles after two steps) time one
@@ -2405,12 +2461,17 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	const int cs = tune >= 0 ? e->cs_cand[tune] : e->cs;
 	const int grid = tune >= 0 ? e->grid_cand[tune] : e->grid;
 	CK(cudaEventRecord(e->ev[1], e->st));
-	CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
-	CK(launch_batch(e, cs, grid));
+	if (e->nbatch > 0) {
+		CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
+		CK(launch_batch(e, cs, grid));
+	}
+	for (int k = 0; k < e->namr; k++)   // refined members: one solver launch each
+		if ((rc = launch_stokes_qt(e->m[e->amr[k]])))
+			return rc;
 	CK(cudaEventRecord(e->ev[2], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
-		if ((rc = stokes_mg_finish(c)) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
+		if ((!c->qt_on && (rc = stokes_mg_finish(c))) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
 			return rc;
 		CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, e->st));
 	}
@@ -2451,7 +2512,7 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 				s->status = s2;
 			s->ms_total = ms_total;
 			s->solver_kernel_ms = ms_solver;
-			s->solver_kernel_launches = 1;
+			s->solver_kernel_launches = (e->nbatch > 0) + e->namr;
 			s->kernel_launches = (l1 - l0) + 1;
 		}
 		c->timestep++;

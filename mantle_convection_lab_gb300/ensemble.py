@@ -11,8 +11,11 @@ All members use the mixed-precision converged solver (FP32 multigrid inside
 FP64 refinement, MINRES correction, extrapolated warm start) and are stepped
 together by mclg_ensemble_step: one batched solver launch per step.
 
-Members are uniform meshes (no AMR levels): the batched solver is the
-structured multigrid one.
+The members of amr_configs() also get 0-2 levels of |grad T| refinement of
+their base grid (seeded), as the configuration asks; they start from tanh
+boundary layers with seeded modes, so the refinement follows the layers.  The
+batched solver is the structured multigrid one, so refined members are solved
+by the refined-mesh solver, one launch each, after the batched launch.
 """
 import math
 import os
@@ -64,3 +67,23 @@ def make(n=256, seed=4, sizes=SIZES):
     e = Ensemble(configs(n, seed, sizes))
     e.initial_temperature()
     return e
+
+
+def amr_levels(n=256, seed=4):
+    """0, 1 or 2 refinement levels per member (seeded)."""
+    return np.random.default_rng(seed + 7919).integers(0, 3, n).astype(np.int32)
+
+
+def amr_configs(n=256, seed=4, sizes=SIZES):
+    """Members with the boundary-layer start that |grad T| refinement follows."""
+    out = configs(n, seed, sizes)
+    for c in out:
+        c.ic_kind = 2
+        c.ic_bl_thickness = 0.02
+        c.ic_modes = 8
+        c.ic_mode_amp = 0.005
+    return out
+
+
+def make_amr(n=256, seed=4, sizes=SIZES):
+    return Ensemble(amr_configs(n, seed, sizes), amr_levels(n, seed))

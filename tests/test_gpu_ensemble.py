@@ -67,3 +67,25 @@ def test_batch_rejects_members_it_cannot_batch():
     with pytest.raises(MclgError) as ex:
         Ensemble([_cfg1_converged(), tall])
     assert ex.value.status == BAD_INPUT
+
+
+def test_refined_members_match_models_stepped_alone():
+    cfgs = ensemble.amr_configs(4, seed=3, sizes=(32, 64))
+    levels = [0, 1, 2, 1]
+    with Ensemble(cfgs, levels) as e:
+        e.initial_temperature()
+        refined = [m.nh > 0 or m.nel != (1 << (2 * (c.level - 1))) for m, c in zip(e.members, cfgs)]
+        assert refined == [False, True, True, True]
+        leaves = [m.mesh("Mcode") >> 4 for m in e.members]
+        for _ in range(3):
+            for s in e.step():
+                assert s.status == 0 and max(s.res_momentum, s.res_continuity) < 1e-8
+        got = [(m.get("V0"), m.get("T")) for m in e.members]
+    for i in (1, 2):
+        c = cfgs[i]
+        c.level += levels[i]
+        with Model(c, leaves=leaves[i]) as m:
+            m.initial_temperature()
+            for _ in range(3):
+                m.step()
+            assert rel(got[i][0], m.get("V0")) < 1e-12 and rel(got[i][1], m.get("T")) < 1e-12
