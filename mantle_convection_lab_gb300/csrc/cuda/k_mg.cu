@@ -884,7 +884,8 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 		// -- FP64 residual R = [F - K d - G p ; G^T d]
 		double rs[3];
 		stokes_residual(a, sm, sy, a.d, a.p, rs);
-		fnorm = sqrt(rs[2]);
+		// a zero load (|F| = 0): the residual is measured absolutely
+		fnorm = rs[2] > 0.0 ? sqrt(rs[2]) : 1.0;
 		res_m = sqrt(rs[0]) / fnorm;
 		res_c = sqrt(rs[1]) / fnorm;
 		const double res = sqrt(rs[0] + rs[1]) / fnorm;

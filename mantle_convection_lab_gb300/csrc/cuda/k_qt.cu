@@ -623,7 +623,8 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 	while (true) {
 		double rs[3];
 		qt_residual(g, red, a, a.d, a.p, rs, tid, nth);
-		const double fnorm = sqrt(rs[2]);
+		// a zero load (|C^T F| = 0): the residual is measured absolutely
+		const double fnorm = rs[2] > 0.0 ? sqrt(rs[2]) : 1.0;
 		res_m = sqrt(rs[0]) / fnorm;
 		res_c = sqrt(rs[1]) / fnorm;
 		const double res = sqrt(rs[0] + rs[1]) / fnorm;

@@ -86,4 +86,6 @@ def amr_configs(n=256, seed=4, sizes=SIZES):
 
 
 def make_amr(n=256, seed=4, sizes=SIZES):
-    return Ensemble(amr_configs(n, seed, sizes), amr_levels(n, seed))
+    e = Ensemble(amr_configs(n, seed, sizes), amr_levels(n, seed))
+    e.initial_temperature()
+    return e
