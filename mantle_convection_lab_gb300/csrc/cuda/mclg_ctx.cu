@@ -2355,6 +2355,8 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 			mclg_ensemble_destroy(e);
 			return MCLG_BAD_INPUT;
 		}
+		if (c->qt_on)   // refined members keep their own stream: their steps run concurrently
+			continue;
 		CKE(cudaStreamSynchronize(c->st));
 		CKE(cudaStreamDestroy(c->st));
 		c->st = e->st;
@@ -2446,11 +2448,22 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	for (int i = 0; i < e->n; i++)
 		l0 += e->m[i]->launches;
 	CK(cudaEventRecord(e->ev[0], e->st));
+	// refined members: the whole step on the member's own stream, concurrent with
+	// one another and with the batched members
+	for (int k = 0; k < e->namr; k++) {
+		mclg_ctx *c = e->m[e->amr[k]];
+		CK(cudaStreamWaitEvent(c->st, e->ev[0], 0));
+		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = launch_stokes_qt(c)) ||
+		    (rc = launch_stress(c)) || (rc = launch_heat(c)))
+			return rc;
+		CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, c->st));
+		CK(cudaEventRecord(c->ev[5], c->st));
+	}
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
-		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)))
-			return rc;
-		if (!c->qt_on && (rc = stokes_mg_prepare(c)))
+		if (c->qt_on)
+			continue;
+		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
 			return rc;
 	}
 	// autotuner: steps 2, 3, ... (the warm start settles after two steps) time one
@@ -2465,16 +2478,17 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
 		CK(launch_batch(e, cs, grid));
 	}
-	for (int k = 0; k < e->namr; k++)   // refined members: one solver launch each
-		if ((rc = launch_stokes_qt(e->m[e->amr[k]])))
-			return rc;
 	CK(cudaEventRecord(e->ev[2], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
-		if ((!c->qt_on && (rc = stokes_mg_finish(c))) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
+		if (c->qt_on)
+			continue;
+		if ((rc = stokes_mg_finish(c)) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
 			return rc;
 		CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, e->st));
 	}
+	for (int k = 0; k < e->namr; k++)
+		CK(cudaStreamWaitEvent(e->st, e->m[e->amr[k]]->ev[5], 0));
 	CK(cudaEventRecord(e->ev[3], e->st));
 	CK(cudaStreamSynchronize(e->st));
 	float ms_total = 0.f, ms_solver = 0.f;
