@@ -23,7 +23,10 @@ template <class T>
 struct TileSmem {
 	static constexpr int TX = TileCfg<T>::TX, PX = TX + 2, PZ = TZN + 2, EX = TX + 1, EZ = TZN + 1;
 	T u[PX][PZ], w[PX][PZ], e[PX][PZ];
-	T s[EX][EZ][12];
+	// 12 stress values per element, padded to 13 words so that the 32 elements
+	// a warp touches at once fall in 32 different shared-memory banks (a
+	// stride of 12 words put every 8th element in the same bank)
+	T s[EX][EZ][13];
 };
 constexpr int kSmemBytes = sizeof(TileSmem<double>) > sizeof(TileSmem<float>) ? sizeof(TileSmem<double>)
                                                                                 : sizeof(TileSmem<float>);
