@@ -696,12 +696,34 @@ __global__ void __launch_bounds__(kBlock) k_qt_extrapolate(int n2, int ne, const
 		p[i] = 2.0 * p1[i] - p2[i];
 }
 
-// coarse-level viscosity: the finer level's value at the same node
-__global__ void __launch_bounds__(kBlock) k_qt_inject(int n, const int *map, const double *src, double *dst)
+// Coarse-level viscosity from the finer level around the same node: the value
+// there (avg 0), or the mean (1) or log-mean (2) over the node and its matrix
+// neighbours on the finer level, weighted 1 (the node), 1/2 (a neighbour
+// along an axis), 1/4 (a diagonal neighbour) -- full weighting where the
+// finer level is uniform.
+__global__ void __launch_bounds__(kBlock) k_qt_inject(int n, const int *map, const double *src, double *dst, int avg,
+                                                      int nno_f, const int *nb_f, const unsigned char *cnt_f,
+                                                      const double *X_f)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n)
-		dst[i] = src[map[i]];
+	if (i >= n)
+		return;
+	const int a = map[i];
+	if (avg == 0) {
+		dst[i] = src[a];
+		return;
+	}
+	const double xa = X_f[a], za = X_f[nno_f + a];
+	double s = 0.0, ws = 0.0;
+	for (int k = 0; k < cnt_f[a]; k++) {
+		const int B = nb_f[(size_t)k * nno_f + a] & ~kQtCon;
+		const bool ax = X_f[B] == xa, az = X_f[nno_f + B] == za;
+		const double w = (ax && az) ? 1.0 : (ax || az) ? 0.5 : 0.25;
+		s += w * (avg == 2 ? log(src[B]) : src[B]);
+		ws += w;
+	}
+	s /= ws;
+	dst[i] = avg == 2 ? exp(s) : s;
 }
 
 void *qt_kernel(int fp64) { return fp64 ? (void *)k_stokes_qt<double> : (void *)k_stokes_qt<float>; }

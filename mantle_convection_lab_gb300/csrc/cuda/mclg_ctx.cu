@@ -27,7 +27,8 @@ void upload_shape_tables_mg(const ShapeTables &s, cudaStream_t st);
 void upload_shape_tables_qt(const ShapeTables &s, cudaStream_t st);
 __global__ void k_qt_extrapolate(int n2, int ne, const double *d1, const double *d2, const double *p1, const double *p2,
                                  double *d, double *p);
-__global__ void k_qt_inject(int n, const int *map, const double *src, double *dst);
+__global__ void k_qt_inject(int n, const int *map, const double *src, double *dst, int avg, int nno_f,
+                            const int *nb_f, const unsigned char *cnt_f, const double *X_f);
 void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st);
 void *stokes_mg_kernel(int fp64);
 void *stokes_mg_batch_kernel(int fp64);
@@ -876,8 +877,12 @@ static int launch_stokes_qt(mclg_ctx *c)
 	const int nlev = c->cfg.precision == 2 ? c->qtd.H.nlev : c->qtf.H.nlev;
 	for (int k = nlev - 2; k >= 0; k--) {
 		const DevLevel &L = c->lvl_L[k];
+		const DevLevel &U = k == nlev - 2 ? c->L : c->lvl_L[k + 1];
 		const double *src = k == nlev - 2 ? c->vis : c->lvl_vis[k + 1];
-		k_qt_inject<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L.nno, c->lvl_map[k], src, c->lvl_vis[k]);
+		const int *nbu = c->cfg.precision == 2 ? c->qtd.H.lv[k + 1].nb : c->qtf.H.lv[k + 1].nb;
+		const unsigned char *cntu = c->cfg.precision == 2 ? c->qtd.H.lv[k + 1].cnt : c->qtf.H.lv[k + 1].cnt;
+		k_qt_inject<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L.nno, c->lvl_map[k], src, c->lvl_vis[k],
+		                                                      c->cfg.mg_eta_avg, U.nno, nbu, cntu, U.X);
 		if ((rc = check_launch(c, "k_qt_inject")))
 			return rc;
 		k_assemble_stokes<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->lvl_vis[k], c->lvl_buoy[k], c->lvl_K[k],
@@ -2649,6 +2654,44 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 		}
 		if (rc == MCLG_OK)
 			rc = mclg_set_field(n, MCLG_F_P, -1, P_new.data(), ne2);
+		// the previous step's solution too, so that the extrapolated warm start
+		// goes on across the remesh
+		if (rc == MCLG_OK && c->d_h2 != NULL && n->d_h2 != NULL && c->ghist >= 2) {
+			std::vector<double> D_old(2 * nn), D_new(2 * nn2, 0.0), comp_old(nn), comp_new(nn2), Ph(ne), Phn(ne2);
+			cudaError_t e = cudaMemcpy(D_old.data(), c->d_h2, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost);
+			if (e == cudaSuccess)
+				e = cudaMemcpy(Ph.data(), c->p_h2, ne * sizeof(double), cudaMemcpyDeviceToHost);
+			if (e != cudaSuccess)
+				rc = cuda_fail(e, "mclg_amr_remesh");
+			for (int comp = 0; comp < 2 && rc == MCLG_OK; comp++) {
+				for (size_t A = 0; A < nn; A++)
+					comp_old[A] = D_old[2 * A + comp];
+				rc = mclg_amr_transfer(&c->mesh, comp_old.data(), &n->mesh, comp_new.data());
+				for (size_t A = 0; A < nn2 && rc == MCLG_OK; A++)
+					if (HN.id[(size_t)comp * nn2 + A] >= 0)
+						D_new[2 * A + comp] = comp_new[A];
+			}
+			for (size_t e2 = 0; e2 < ne2 && rc == MCLG_OK; e2++) {
+				double x = 0.0, z = 0.0;
+				for (int a = 0; a < 4; a++) {
+					const int A = HN.ienl[(size_t)a * ne2 + e2];
+					x += 0.25 * HN.X[A];
+					z += 0.25 * HN.X[nn2 + A];
+				}
+				int cx = (int)(x / dxc), cz = (int)(z / dzc);
+				cx = cx < 0 ? 0 : cx >= ncell ? ncell - 1 : cx;
+				cz = cz < 0 ? 0 : cz >= ncell ? ncell - 1 : cz;
+				Phn[e2] = Ph[HO.cell_elem[(size_t)cx * ncell + cz]];
+			}
+			if (rc == MCLG_OK) {
+				e = cudaMemcpy(n->d_h2, D_new.data(), 2 * nn2 * sizeof(double), cudaMemcpyHostToDevice);
+				if (e == cudaSuccess)
+					e = cudaMemcpy(n->p_h2, Phn.data(), ne2 * sizeof(double), cudaMemcpyHostToDevice);
+				if (e != cudaSuccess)
+					rc = cuda_fail(e, "mclg_amr_remesh");
+				n->ghist = c->ghist;
+			}
+		}
 	}
 	if (rc == MCLG_OK) {
 		cudaError_t e = cudaMemcpyAsync(n->sc, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToDevice, n->st);
