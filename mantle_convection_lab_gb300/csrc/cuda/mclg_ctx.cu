@@ -862,7 +862,9 @@ static int launch_stokes_qt(mclg_ctx *c)
 	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
 	CK(cudaMemsetAsync(&c->sc->guess_used, 0xff, sizeof(int), c->st));
 	const bool track = c->d_h1 != NULL;
-	if (track) {
+	if (track) {   // history: d_h2 <- d_h1, d_h1 <- d (the last two solutions)
+		CK(cudaMemcpyAsync(c->d_h2, c->d_h1, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+		CK(cudaMemcpyAsync(c->p_h2, c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		if (f.warm_start == 3 && c->ghist >= 2) {
@@ -898,11 +900,8 @@ static int launch_stokes_qt(mclg_ctx *c)
 		CK(cudaLaunchCooperativeKernel(qt_kernel(0), dim3(c->coop_qt), dim3(kBlock), args, 0, c->st));
 	}
 	c->launches++;
-	if (track) {
-		std::swap(c->d_h1, c->d_h2);
-		std::swap(c->p_h1, c->p_h2);
+	if (track)
 		c->ghist++;
-	}
 	return MCLG_OK;
 }
 
@@ -955,7 +954,11 @@ static int stokes_mg_prepare(mclg_ctx *c)
 	if (track) {
 		// features from (T, eta, last two solutions) before d is overwritten
 		if (feat)
-			guess_features(c->st, N0, c->gs, c->T, c->vis, c->d, c->p, c->d_h2, c->p_h2, c->gX, c->gscale);
+			guess_features(c->st, N0, c->gs, c->T, c->vis, c->d, c->p, c->d_h1, c->p_h1, c->gX, c->gscale);
+		// history: d_h2 <- d_h1, d_h1 <- d (the last two solutions; device copies,
+		// so that a captured step replays unchanged)
+		CK(cudaMemcpyAsync(c->d_h2, c->d_h1, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+		CK(cudaMemcpyAsync(c->p_h2, c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		if (extrap) {
@@ -1007,12 +1010,6 @@ static int stokes_mg_finish(mclg_ctx *c)
 			c->launches++;
 		}
 		CK(cudaGetLastError());
-		double2 *t2 = c->d_h2;
-		c->d_h2 = c->d_h1;
-		c->d_h1 = t2;
-		double *t1 = c->p_h2;
-		c->p_h2 = c->p_h1;
-		c->p_h1 = t1;
 		c->ghist++;
 	}
 	return MCLG_OK;
@@ -2656,11 +2653,11 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 			rc = mclg_set_field(n, MCLG_F_P, -1, P_new.data(), ne2);
 		// the previous step's solution too, so that the extrapolated warm start
 		// goes on across the remesh
-		if (rc == MCLG_OK && c->d_h2 != NULL && n->d_h2 != NULL && c->ghist >= 2) {
+		if (rc == MCLG_OK && c->d_h1 != NULL && n->d_h1 != NULL && c->ghist >= 2) {
 			std::vector<double> D_old(2 * nn), D_new(2 * nn2, 0.0), comp_old(nn), comp_new(nn2), Ph(ne), Phn(ne2);
-			cudaError_t e = cudaMemcpy(D_old.data(), c->d_h2, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost);
+			cudaError_t e = cudaMemcpy(D_old.data(), c->d_h1, 2 * nn * sizeof(double), cudaMemcpyDeviceToHost);
 			if (e == cudaSuccess)
-				e = cudaMemcpy(Ph.data(), c->p_h2, ne * sizeof(double), cudaMemcpyDeviceToHost);
+				e = cudaMemcpy(Ph.data(), c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToHost);
 			if (e != cudaSuccess)
 				rc = cuda_fail(e, "mclg_amr_remesh");
 			for (int comp = 0; comp < 2 && rc == MCLG_OK; comp++) {
@@ -2684,9 +2681,9 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 				Phn[e2] = Ph[HO.cell_elem[(size_t)cx * ncell + cz]];
 			}
 			if (rc == MCLG_OK) {
-				e = cudaMemcpy(n->d_h2, D_new.data(), 2 * nn2 * sizeof(double), cudaMemcpyHostToDevice);
+				e = cudaMemcpy(n->d_h1, D_new.data(), 2 * nn2 * sizeof(double), cudaMemcpyHostToDevice);
 				if (e == cudaSuccess)
-					e = cudaMemcpy(n->p_h2, Phn.data(), ne2 * sizeof(double), cudaMemcpyHostToDevice);
+					e = cudaMemcpy(n->p_h1, Phn.data(), ne2 * sizeof(double), cudaMemcpyHostToDevice);
 				if (e != cudaSuccess)
 					rc = cuda_fail(e, "mclg_amr_remesh");
 				n->ghist = c->ghist;
@@ -2772,8 +2769,8 @@ static int ckp_arrays(mclg_ctx *c, bool history, void **ptr, size_t *bytes)
 	ptr[n] = c->d; bytes[n++] = nn * sizeof(double2);
 	ptr[n] = c->p; bytes[n++] = ne * sizeof(double);
 	if (history) {
-		ptr[n] = c->d_h2; bytes[n++] = nn * sizeof(double2);
-		ptr[n] = c->p_h2; bytes[n++] = ne * sizeof(double);
+		ptr[n] = c->d_h1; bytes[n++] = nn * sizeof(double2);   // the previous step's solution
+		ptr[n] = c->p_h1; bytes[n++] = ne * sizeof(double);
 	}
 	return n;
 }
