@@ -341,6 +341,11 @@ int mclg_ensemble_create(mclg_ensemble **e, const mclg_config *cfgs, int n);
  * members are solved by the refined-mesh solver, one launch each after the
  * batched launch of the uniform members. */
 int mclg_ensemble_create_amr(mclg_ensemble **e, const mclg_config *cfgs, const int *amr_levels, int n);
+/* 1 when steps replay a CUDA graph of the whole ensemble step: captured once the
+ * cluster-size autotuner has chosen (step 7) and every member's warm start is
+ * steady; until then, or where capture is refused, the step is issued launch by
+ * launch. */
+int mclg_ensemble_graph(const mclg_ensemble *e);
 void mclg_ensemble_destroy(mclg_ensemble *e);
 int mclg_ensemble_size(const mclg_ensemble *e);
 /* Member i as a context (fields, mesh, single operators); owned by the ensemble. */

@@ -154,6 +154,7 @@ def lib():
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
+        "mclg_ensemble_graph": (C.c_int, [vp]),
         "mclg_ensemble_size": (C.c_int, [vp]), "mclg_ensemble_member": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "mclg_ensemble_initial_temperature": (C.c_int, [vp]),
         "mclg_ensemble_step": (C.c_int, [vp, vp, ip]),
@@ -586,6 +587,11 @@ class Ensemble:
         _check(lib().mclg_ensemble_initial_temperature(self._e), "ensemble_initial_temperature")
         for m in self.members:
             m.timestep = 0
+
+    @property
+    def graph(self):
+        """True when steps replay the captured CUDA graph of the whole step."""
+        return bool(lib().mclg_ensemble_graph(self._e))
 
     def step(self):
         stats = (StepStats * self.n)()

@@ -2196,6 +2196,11 @@ struct mclg_ensemble {
 	long long steps;
 	int nbatch;            // members in the batched launch (uniform meshes)
 	int *amr, namr;        // members on refined meshes, solved one launch each
+	// the whole step as a CUDA graph, captured once the autotuner has chosen and
+	// every member's warm start is in its steady form, replayed afterwards
+	cudaGraphExec_t graph;
+	int graph_failed;
+	long long graph_launches;   // kernels one replay launches
 };
 
 static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
@@ -2257,6 +2262,8 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 	free(e->m);
 	free(e->order);
 	free(e->amr);
+	if (e->graph)
+		cudaGraphExecDestroy(e->graph);
 	if (e->dargs)
 		cudaFree(e->dargs);
 	if (e->queue)
@@ -2416,6 +2423,11 @@ int mclg_ensemble_create_amr(mclg_ensemble **out, const mclg_config *cfgs, const
 	return ensemble_create(out, cfgs, amr_levels, n);
 }
 
+int mclg_ensemble_graph(const mclg_ensemble *e)
+{
+	return e != NULL && e->graph != NULL;
+}
+
 int mclg_ensemble_size(const mclg_ensemble *e)
 {
 	return e ? e->n : 0;
@@ -2441,15 +2453,11 @@ int mclg_ensemble_initial_temperature(mclg_ensemble *e)
 	return MCLG_OK;
 }
 
-int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
+// The work of one ensemble step, issued on the ensemble's stream (refined
+// members fork onto their own streams and join back).
+static int ensemble_issue(mclg_ensemble *e, int cs, int grid)
 {
-	if (e == NULL)
-		return MCLG_BAD_INPUT;
 	int rc;
-	long long l0 = 0;
-	for (int i = 0; i < e->n; i++)
-		l0 += e->m[i]->launches;
-	CK(cudaEventRecord(e->ev[0], e->st));
 	// refined members: the whole step on the member's own stream, concurrent with
 	// one another and with the batched members
 	for (int k = 0; k < e->namr; k++) {
@@ -2468,13 +2476,6 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
 			return rc;
 	}
-	// autotuner: steps 2, 3, ... (the warm start settles after two steps) time one
-	// candidate cluster size each; later steps use the cheapest per inner iteration
-	int tune = -1;
-	if (e->steps >= 2 && e->steps < 2 + mclg_ensemble::kCand)
-		tune = (int)(e->steps - 2);
-	const int cs = tune >= 0 ? e->cs_cand[tune] : e->cs;
-	const int grid = tune >= 0 ? e->grid_cand[tune] : e->grid;
 	CK(cudaEventRecord(e->ev[1], e->st));
 	if (e->nbatch > 0) {
 		CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
@@ -2491,6 +2492,88 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 	}
 	for (int k = 0; k < e->namr; k++)
 		CK(cudaStreamWaitEvent(e->st, e->m[e->amr[k]]->ev[5], 0));
+	return MCLG_OK;
+}
+
+// Every member's warm start is in the form it keeps from now on (a graph
+// replays exactly what it captured).
+static bool ensemble_steady(const mclg_ensemble *e)
+{
+	for (int i = 0; i < e->n; i++) {
+		const mclg_ctx *c = e->m[i];
+		if (c->gmode != MCLG_GUESS_OFF || c->gnet != NULL)
+			return false;
+		if (c->d_h1 != NULL && c->ghist < 2)
+			return false;
+	}
+	return true;
+}
+
+int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
+{
+	if (e == NULL)
+		return MCLG_BAD_INPUT;
+	int rc;
+	long long l0 = 0;
+	for (int i = 0; i < e->n; i++)
+		l0 += e->m[i]->launches;
+	// autotuner: steps 2, 3, ... (the warm start settles after two steps) time one
+	// candidate cluster size each; later steps use the cheapest per inner iteration
+	int tune = -1;
+	if (e->steps >= 2 && e->steps < 2 + mclg_ensemble::kCand)
+		tune = (int)(e->steps - 2);
+	const int cs = tune >= 0 ? e->cs_cand[tune] : e->cs;
+	const int grid = tune >= 0 ? e->grid_cand[tune] : e->grid;
+	// capture the step once the tuning is over and the warm starts are steady
+	if (tune < 0 && e->steps >= 2 + mclg_ensemble::kCand && e->graph == NULL && !e->graph_failed &&
+	    ensemble_steady(e)) {
+		cudaGraph_t g = NULL;
+		std::vector<int> ghist0(e->n);
+		std::vector<long long> launches0(e->n);
+		for (int i = 0; i < e->n; i++) {
+			ghist0[i] = e->m[i]->ghist;
+			launches0[i] = e->m[i]->launches;
+		}
+		cudaError_t ce = cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal);
+		if (ce == cudaSuccess) {
+			ce = cudaEventRecord(e->ev[0], e->st);
+			rc = ce == cudaSuccess ? ensemble_issue(e, cs, grid) : MCLG_CUDA_ERROR;
+			const cudaError_t ee = cudaStreamEndCapture(e->st, &g);   // always ends the capture
+			if (ce == cudaSuccess)
+				ce = ee;
+			if (rc == MCLG_OK && ce == cudaSuccess && g != NULL)
+				ce = cudaGraphInstantiate(&e->graph, g, 0);
+			else if (ce == cudaSuccess)
+				ce = cudaErrorUnknown;
+		}
+		if (g)
+			cudaGraphDestroy(g);
+		long long per_step = 0;
+		for (int i = 0; i < e->n; i++) {   // the capture ran nothing: undo its bookkeeping
+			per_step += e->m[i]->launches - launches0[i];
+			e->m[i]->launches = launches0[i];
+			e->m[i]->ghist = ghist0[i];
+		}
+		if (ce != cudaSuccess) {
+			cudaGetLastError();
+			e->graph = NULL;
+			e->graph_failed = 1;
+		} else {
+			e->graph_launches = per_step;
+		}
+	}
+	CK(cudaEventRecord(e->ev[0], e->st));
+	if (e->graph != NULL) {
+		CK(cudaGraphLaunch(e->graph, e->st));
+		for (int i = 0; i < e->n; i++) {   // what the issue path counts on the host
+			mclg_ctx *c = e->m[i];
+			if (c->d_h1 != NULL)
+				c->ghist++;
+		}
+		e->m[0]->launches += e->graph_launches;
+	} else if ((rc = ensemble_issue(e, cs, grid))) {
+		return rc;
+	}
 	CK(cudaEventRecord(e->ev[3], e->st));
 	CK(cudaStreamSynchronize(e->st));
 	float ms_total = 0.f, ms_solver = 0.f;

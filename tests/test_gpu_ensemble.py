@@ -89,3 +89,25 @@ def test_refined_members_match_models_stepped_alone():
             for _ in range(3):
                 m.step()
             assert rel(got[i][0], m.get("V0")) < 1e-12 and rel(got[i][1], m.get("T")) < 1e-12
+
+
+def test_graph_replay_matches_members_stepped_alone():
+    """From step 7 on (after the cluster-size autotuner) the step is replayed as one
+    CUDA graph; the members still match themselves stepped alone."""
+    cfgs = ensemble.configs(3, seed=5, sizes=(32,))
+    steps = 11
+    with Ensemble(cfgs) as e:
+        e.initial_temperature()
+        used = []
+        for _ in range(steps):
+            for s in e.step():
+                assert s.status == 0 and max(s.res_momentum, s.res_continuity) < 1e-8
+            used.append(e.graph)
+        assert used[:7] == [False] * 7 and all(used[8:]), used
+        got = [(m.get("V0"), m.get("T")) for m in e.members]
+    for i, c in enumerate(cfgs):
+        with Model(c) as m:
+            m.initial_temperature()
+            for _ in range(steps):
+                m.step()
+            assert rel(got[i][0], m.get("V0")) < 1e-8 and rel(got[i][1], m.get("T")) < 1e-10
