@@ -2256,14 +2256,14 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 		return;
 	if (e->st)
 		cudaStreamSynchronize(e->st);
+	if (e->graph)   // before the members: the graph records their events
+		cudaGraphExecDestroy(e->graph);
 	for (int i = 0; i < e->n; i++)
 		if (e->m && e->m[i])
 			mclg_destroy(e->m[i]);
 	free(e->m);
 	free(e->order);
 	free(e->amr);
-	if (e->graph)
-		cudaGraphExecDestroy(e->graph);
 	if (e->dargs)
 		cudaFree(e->dargs);
 	if (e->queue)
