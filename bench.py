@@ -396,7 +396,7 @@ def run_ensemble(args, wl):
         dist.barrier()
     torch.cuda.synchronize()
     ms, ms_solver, launches, res, inner = 0.0, 0.0, 0, 0.0, 0
-    grids = []
+    grids, graph_used = [], False
     for _ in range(args.steps):
         st = e.step()
         ms += st[0].ms_total
@@ -406,6 +406,7 @@ def run_ensemble(args, wl):
         inner += sum(s.cg_cycles for s in st)
         assert all(s.status == 0 for s in st), [s.status for s in st]
         grids.append(e.cluster_used)
+        graph_used = e.graph
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -430,7 +431,8 @@ def run_ensemble(args, wl):
                    "members_by_refinement_levels": ({str(k): int((levels == k).sum()) for k in (0, 1, 2)}
                                                     if levels is not None else {"0": n}),
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (256 models)",
-                   "solver_ms_per_step": ms_solver / args.steps, "cluster_size_per_step": grids,
+                   "solver_ms_per_step": ms_solver / args.steps if ms_solver > 0 else None,
+                   "step_graph": graph_used, "cluster_size_per_step": grids,
                    "inner_per_model_step": inner / (n * args.steps), "max_stokes_residual": res},
         "e2e": {"value": e2e, "unit": "model-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
