@@ -315,6 +315,14 @@ int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /*
 int mclg_create_leaves(mclg_ctx **ctx, const mclg_config *cfg, const int *leaves, size_t n);
 int mclg_amr_flags(mclg_ctx *ctx, double frac, unsigned char *flags, size_t n, double *gmax);
 int mclg_amr_remesh(mclg_ctx *ctx, double frac, int base_level, int target_level, size_t *nel);
+/* The same in two halves, so that the host work overlaps the GPU's: begin takes
+ * the flags of the current T and the new leaves, then builds the new mesh and
+ * the refined-mesh solver's lists on a worker thread and returns; the caller
+ * may go on stepping the old mesh; end waits for the worker, creates the new
+ * device state and carries the current fields over (as mclg_amr_remesh).  One
+ * remesh may be pending at a time; mclg_destroy finishes a pending one. */
+int mclg_amr_remesh_begin(mclg_ctx *ctx, double frac, int base_level, int target_level);
+int mclg_amr_remesh_end(mclg_ctx *ctx, size_t *nel);
 int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n);
 int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, size_t nflags, int base_level,
                          int target_level, int *leaves, size_t cap, size_t *n);

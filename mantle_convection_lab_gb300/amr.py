@@ -26,15 +26,22 @@ def uniform_leaves(finest_level, base_level):
 
 
 class AmrRun:
-    def __init__(self, config=None, base_level=7, extra_levels=3, frac=0.2, remesh_every=10):
+    """Configuration 2's run: remesh every `remesh_every` steps.  With lag > 0 a
+    remesh after the first is asynchronous: its flags come from the temperature
+    at step k, its mesh is built on a host thread while steps k .. k+lag-1 run
+    on the old mesh, and it is swapped in before step k+lag (the fields carried
+    over are those of that moment)."""
+
+    def __init__(self, config=None, base_level=7, extra_levels=3, frac=0.2, remesh_every=10, lag=0):
         self.config = config if config is not None else Config.from_input(CFG2_INPUT)
         self.F = self.config.level - 1
         self.base, self.target = base_level, min(base_level + extra_levels, self.F)
-        self.frac, self.every = frac, remesh_every
+        self.frac, self.every, self.lag = frac, remesh_every, lag
         self.model = Model(self.config, leaves=uniform_leaves(self.F, self.base))
         self.model.initial_temperature()
         self.steps = 0
         self.remeshes = 0
+        self._pending = False
 
     def remesh(self):
         n = self.model.remesh(self.frac, self.base, self.target)
@@ -42,8 +49,17 @@ class AmrRun:
         return n
 
     def step(self):
-        if self.steps % self.every == 0:
-            self.remesh()
+        k = self.steps % self.every
+        if self._pending and k == self.lag:
+            self.model.remesh_end()
+            self._pending = False
+            self.remeshes += 1
+        if k == 0:
+            if self.lag > 0 and self.steps > 0:
+                self.model.remesh_begin(self.frac, self.base, self.target)
+                self._pending = True
+            else:
+                self.remesh()
         st = self.model.step()
         self.steps += 1
         return st

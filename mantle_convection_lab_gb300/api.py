@@ -149,6 +149,8 @@ def lib():
         "mclg_create_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
         "mclg_amr_flags": (C.c_int, [vp, C.c_double, C.POINTER(C.c_ubyte), sz, dp]),
         "mclg_amr_remesh": (C.c_int, [vp, C.c_double, C.c_int, C.c_int, C.POINTER(sz)]),
+        "mclg_amr_remesh_begin": (C.c_int, [vp, C.c_double, C.c_int, C.c_int]),
+        "mclg_amr_remesh_end": (C.c_int, [vp, C.POINTER(sz)]),
         "mclg_mesh_new_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
         "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
@@ -518,6 +520,18 @@ class Model:
         """Refine by |grad T| and rebuild the model on the new mesh in place."""
         n = C.c_size_t()
         _check(lib().mclg_amr_remesh(self._c, frac, base_level, target_level, C.byref(n)), "amr_remesh")
+        s = self.mesh("sizes")
+        self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
+        return n.value
+
+    def remesh_begin(self, frac, base_level, target_level):
+        """First half of remesh(): flags and leaves now, the new mesh built on a host thread."""
+        _check(lib().mclg_amr_remesh_begin(self._c, frac, base_level, target_level), "amr_remesh_begin")
+
+    def remesh_end(self):
+        """Second half: wait for the new mesh, carry the current fields over, swap it in."""
+        n = C.c_size_t()
+        _check(lib().mclg_amr_remesh_end(self._c, C.byref(n)), "amr_remesh_end")
         s = self.mesh("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
         return n.value

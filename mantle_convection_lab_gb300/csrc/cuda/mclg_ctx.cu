@@ -5,6 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <thread>
 #include <vector>
 #include "k_mg.cuh"
 #include "cnn.cuh"
@@ -125,6 +126,7 @@ struct mclg_ctx {
 	QtArgs<float> qtf;
 	QtArgs<double> qtd;
 	OutWriter *writer;            // asynchronous output, created on first use
+	struct RemeshJob *rj;         // a remesh begun and not yet finished
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -659,6 +661,22 @@ static bool coarse_level(const mclg_ctx *c, int lev, int *k)
 }
 
 // ---- converged solver on refined meshes ------------------------------------------
+// Host structures of a model built ahead of it (a remesh prepares them on a
+// worker thread while the GPU keeps stepping the old mesh).
+struct Prebuilt {
+	mclg_mesh mesh;
+	mclg_qt_level q[MCLG_MAX_LEVEL];
+	int nq;                        // levels of q built (refined meshes with a converged solver)
+};
+
+static void prebuilt_free(Prebuilt *pb)
+{
+	for (int i = 0; i < pb->nq; i++)
+		mclg_qt_free(&pb->q[i]);
+	pb->nq = 0;
+	mclg_mesh_free(&pb->mesh);
+}
+
 template <class TW, class TS>
 static cudaError_t dev_upload_cast(mclg_ctx *c, TW **p, const TS *h, size_t n)
 {
@@ -681,7 +699,7 @@ static cudaError_t dev_upload_n(mclg_ctx *c, T **p, const T *h, size_t n)
 // (mclg_qtmg.c), the TI operators and work vectors, the coarsest level's
 // dense inverse and the FP64 MINRES vectors.
 template <class TI>
-static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
+static int qt_setup(mclg_ctx *c, QtArgs<TI> &a, Prebuilt *pre)
 {
 	typedef typename Q2T<TI>::t V;
 	typedef typename V4T<TI>::t K4;
@@ -699,7 +717,15 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a)
 				return MCLG_BAD_INPUT;
 			}
 	std::vector<mclg_qt_level> q((size_t)nlev);
-	int rc = mclg_qt_build(&m, lo, q.data());
+	int rc = MCLG_OK;
+	if (pre != NULL && pre->nq == nlev) {   // built ahead: take them over
+		for (int i = 0; i < nlev; i++)
+			q[i] = pre->q[i];
+		memset(pre->q, 0, sizeof pre->q);
+		pre->nq = 0;
+	} else {
+		rc = mclg_qt_build(&m, lo, q.data());
+	}
 	struct Free {
 		std::vector<mclg_qt_level> &q;
 		~Free()
@@ -1086,7 +1112,41 @@ const char *mclg_status_string(int s)
 void mclg_destroy(mclg_ctx *c);
 
 // leaves != NULL: the mesh is built from that leaf set instead of develop_mode
-static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves, long nleaves)
+// The configuration the mesh is built with: the converged solvers' hierarchy on
+// a refined mesh goes down to a grid of mg_coarse elements per side, so the
+// mesh keeps levels that far down.
+static mclg_config mesh_config(const mclg_config *cfg)
+{
+	mclg_config mcfg = *cfg;
+	if (cfg->precision != 0) {
+		int cl = 1;
+		while ((1 << (cl + 1)) <= cfg->mg_coarse)
+			cl++;
+		if (cl < mcfg.mg_min_level)
+			mcfg.mg_min_level = cl;
+	}
+	return mcfg;
+}
+
+// The host structures of a model on a leaf set: the mesh and, for a converged
+// solver on a refined mesh, its constrained-space lists.  No device work.
+static int prebuild(Prebuilt *pb, const mclg_config *cfg, const int *leaves, long n)
+{
+	memset(pb, 0, sizeof *pb);
+	const mclg_config mcfg = mesh_config(cfg);
+	int rc = mclg_mesh_build_leaves(&pb->mesh, &mcfg, leaves, n);
+	if (rc != MCLG_OK)
+		return rc;
+	const int top = pb->mesh.max_level - 1, lo = pb->mesh.min_level, nlev = top - lo + 1;
+	if (cfg->precision != 0 && !pb->mesh.uniform && nlev >= 2 && nlev <= 16) {
+		rc = mclg_qt_build(&pb->mesh, lo, pb->q);
+		pb->nq = nlev;
+	}
+	return rc;
+}
+
+// pre: host structures built ahead (taken over; NULL: built here)
+static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves, long nleaves, Prebuilt *pre = NULL)
 {
 	if (out == NULL || cfg == NULL)
 		return MCLG_BAD_INPUT;
@@ -1110,17 +1170,14 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
 	c->cfg = *cfg;
-	// the converged solvers' hierarchy on a refined mesh goes down to a grid of
-	// mg_coarse elements per side: the mesh keeps levels that far down
-	mclg_config mcfg = *cfg;
-	if (cfg->precision != 0) {
-		int cl = 1;
-		while ((1 << (cl + 1)) <= cfg->mg_coarse)
-			cl++;
-		if (cl < mcfg.mg_min_level)
-			mcfg.mg_min_level = cl;
+	const mclg_config mcfg = mesh_config(cfg);
+	int rc = MCLG_OK;
+	if (pre != NULL) {   // take the mesh over
+		c->mesh = pre->mesh;
+		memset(&pre->mesh, 0, sizeof pre->mesh);
+	} else {
+		rc = leaves ? mclg_mesh_build_leaves(&c->mesh, &mcfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, &mcfg);
 	}
-	int rc = leaves ? mclg_mesh_build_leaves(&c->mesh, &mcfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, &mcfg);
 	if (rc != MCLG_OK) {
 		mclg_mesh_free(&c->mesh);
 		free(c);
@@ -1221,7 +1278,7 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	c->coop_uzawa = coop_blocks(uzawa_kernel_ptr(c->ref_kind != kRefNone), c->num_sms, work);
 	c->coop_heat = coop_blocks(heat_cg_kernel_ptr(), c->num_sms, (int)nn);
 	if (cfg->precision != 0 && !c->mesh.uniform) {
-		rc = cfg->precision == 2 ? qt_setup<double>(c, c->qtd) : qt_setup<float>(c, c->qtf);
+		rc = cfg->precision == 2 ? qt_setup<double>(c, c->qtd, pre) : qt_setup<float>(c, c->qtf, pre);
 		if (rc == MCLG_OK)
 			c->coop_qt = coop_blocks(qt_kernel(cfg->precision == 2), c->num_sms, (int)nn);
 		if (rc == MCLG_OK && c->coop_qt < 1) {
@@ -1274,11 +1331,14 @@ int mclg_create_leaves(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	return create_impl(out, cfg, leaves, (long)n);
 }
 
+static void remesh_job_free(mclg_ctx *c);
+
 void mclg_destroy(mclg_ctx *c)
 {
 	if (c == NULL)
 		return;
 	writer_free(c->writer);   // pending outputs are written first
+	remesh_job_free(c);
 	if (c->st)
 		cudaStreamSynchronize(c->st);
 	free_level_buf(c->lb);
@@ -2671,11 +2731,39 @@ int mclg_amr_flags(mclg_ctx *c, double frac, unsigned char *flags, size_t n, dou
 // then the context is rebuilt on the new mesh in place: the handle stays
 // valid, time step and model time carry over, velocity and pressure restart
 // from zero.
-int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, size_t *nel_out)
+// A remesh in two halves: begin() takes the flags and the new leaves and
+// builds the new mesh and the solver's lists on a worker thread; end() waits
+// for it, creates the device state, carries the fields over and swaps it in.
+// Between them the caller may go on stepping the old mesh.
+struct RemeshJob {
+	std::thread th;
+	mclg_config cfg;
+	std::vector<int> leaves;
+	Prebuilt pb;
+	int rc;
+	char err[512];
+};
+
+static void remesh_job_free(mclg_ctx *c)
+{
+	if (c->rj == NULL)
+		return;
+	if (c->rj->th.joinable())
+		c->rj->th.join();
+	prebuilt_free(&c->rj->pb);
+	delete c->rj;
+	c->rj = NULL;
+}
+
+int mclg_amr_remesh_begin(mclg_ctx *c, double frac, int base_level, int target_level)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	const size_t ne = (size_t)c->L.nel, nn = (size_t)c->L.nno;
+	if (c->rj != NULL) {
+		mclg_set_error("a remesh is already pending: finish it with mclg_amr_remesh_end");
+		return MCLG_BAD_INPUT;
+	}
+	const size_t ne = (size_t)c->L.nel;
 	std::vector<unsigned char> flags(ne);
 	int rc = mclg_amr_flags(c, frac, flags.data(), ne, NULL);
 	if (rc)
@@ -2685,10 +2773,48 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 	rc = mclg_amr_build_leaves(&c->mesh, flags.data(), base_level, target_level, &leaves, &nl);
 	if (rc)
 		return rc;
+	RemeshJob *j = new RemeshJob();
+	j->cfg = c->cfg;
+	j->leaves.assign(leaves, leaves + nl);
+	free(leaves);
+	j->rc = MCLG_OK;
+	j->err[0] = 0;
+	memset(&j->pb, 0, sizeof j->pb);
+	c->rj = j;
+	try {
+		j->th = std::thread([j]() {
+			j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
+			if (j->rc != MCLG_OK)
+				snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+		});
+	} catch (...) {   // no thread: build here
+		j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
+		if (j->rc != MCLG_OK)
+			snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+	}
+	return MCLG_OK;
+}
+
+int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
+{
+	if (c == NULL || c->rj == NULL) {
+		mclg_set_error("no remesh is pending");
+		return MCLG_BAD_INPUT;
+	}
+	RemeshJob *j = c->rj;
+	if (j->th.joinable())
+		j->th.join();
+	if (j->rc != MCLG_OK) {
+		const int rc = j->rc;
+		mclg_set_error("%s", j->err);
+		remesh_job_free(c);
+		return rc;
+	}
+	const size_t ne = (size_t)c->L.nel, nn = (size_t)c->L.nno;
 	mclg_config cfg = c->cfg;
 	mclg_ctx *n = NULL;
-	rc = create_impl(&n, &cfg, leaves, nl);
-	free(leaves);
+	int rc = create_impl(&n, &cfg, j->leaves.data(), (long)j->leaves.size(), &j->pb);
+	remesh_job_free(c);
 	if (rc)
 		return rc;
 	std::vector<double> T_old(nn), T_new((size_t)n->L.nno);
@@ -2798,6 +2924,12 @@ int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, 
 	if (nel_out)
 		*nel_out = (size_t)c->L.nel;
 	return MCLG_OK;
+}
+
+int mclg_amr_remesh(mclg_ctx *c, double frac, int base_level, int target_level, size_t *nel_out)
+{
+	const int rc = mclg_amr_remesh_begin(c, frac, base_level, target_level);
+	return rc ? rc : mclg_amr_remesh_end(c, nel_out);
 }
 
 // ---- checkpoint / restart ------------------------------------------------------

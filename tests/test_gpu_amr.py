@@ -13,7 +13,7 @@ import pytest
 from conftest import golden_input, rel
 
 import amr_oracle as ao
-from mantle_convection_lab_gb300 import Config, Mesh, Model
+from mantle_convection_lab_gb300 import Config, MclgError, Mesh, Model, amr
 from oracle_port import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -92,3 +92,38 @@ def test_remesh_matches_host_pipeline_and_oracle():
             assert sm.uzawa_cycles == sd.uzawa_cycles and sm.dt == sd.dt
             for f in ("V0", "V1", "P", "T"):
                 np.testing.assert_array_equal(m.get(f), d.get(f), err_msg=f)
+
+
+def test_asynchronous_remesh_equals_synchronous():
+    """remesh_begin / remesh_end with nothing in between builds the same model as
+    remesh(); with steps in between, the old mesh keeps stepping and the new one
+    takes the fields of the moment it is swapped in."""
+    cfg = Config.from_input(amr.CFG2_INPUT)
+    cfg.level = 8
+    cfg.precision, cfg.warm_start = 1, 3
+    runs = []
+    for mode in ("sync", "async"):
+        with Model(cfg, leaves=amr.uniform_leaves(cfg.level - 1, 5)) as m:
+            m.initial_temperature()
+            m.step()
+            if mode == "sync":
+                m.remesh(0.2, 5, 7)
+            else:
+                m.remesh_begin(0.2, 5, 7)
+                m.remesh_end()
+            m.step()
+            runs.append((m.nel, m.nh, m.get("T"), m.get("V0")))
+    assert runs[0][:2] == runs[1][:2]
+    for a, b in zip(runs[0][2:], runs[1][2:]):
+        np.testing.assert_array_equal(a, b)
+    with Model(cfg, leaves=amr.uniform_leaves(cfg.level - 1, 5)) as m:
+        m.initial_temperature()
+        nel0 = m.nel
+        m.remesh_begin(0.2, 5, 7)
+        for _ in range(2):
+            assert m.step().status == 0
+            assert m.nel == nel0
+        m.remesh_end()
+        assert m.nel > nel0 and m.step().status == 0
+        with pytest.raises(MclgError):
+            m.remesh_end()                     # nothing pending
