@@ -304,16 +304,23 @@ int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /*
  *   mclg_amr_flags       per finest-level element (Morton order): |grad T| at
  *                        its centre > frac * max over elements (device, IEEE
  *                        rounding, bit-reproducible on the CPU);
- *   mclg_amr_remesh      flags -> a new tree (flagged leaves' cells at
- *                        target_level, the rest at base_level, 2:1 balanced
- *                        across edges and corners) -> the model rebuilt on it
- *                        in place, T carried over by bilinear interpolation,
- *                        time step and model time kept.  Refined meshes run
- *                        the FP64 replica solver (precision=fp64).
+ *   mclg_amr_leaves      flags (host buffer, one per finest-level element) ->
+ *                        the new tree's leaves, built on the device: flagged
+ *                        leaves' cells at target_level, the rest at
+ *                        base_level, 2:1 balanced across edges and corners;
+ *                        equal to mclg_mesh_amr_leaves on the same flags;
+ *   mclg_amr_remesh      flags and the new tree on the device -> the model
+ *                        rebuilt on it in place (numbering and hanging nodes
+ *                        on the host), T carried over by bilinear
+ *                        interpolation, time step and model time kept.
+ *                        Refined meshes run the FP64 replica (precision=fp64)
+ *                        or the converged refined-mesh solver (mixed, fp64mg).
  * Host-only counterparts for checking the tree and the transfer without a GPU:
  * mclg_mesh_new_leaves, mclg_mesh_amr_leaves, mclg_mesh_transfer. */
 int mclg_create_leaves(mclg_ctx **ctx, const mclg_config *cfg, const int *leaves, size_t n);
 int mclg_amr_flags(mclg_ctx *ctx, double frac, unsigned char *flags, size_t n, double *gmax);
+int mclg_amr_leaves(mclg_ctx *ctx, const unsigned char *flags, size_t n, int base_level, int target_level, int *leaves,
+                    size_t cap, size_t *nleaves);
 int mclg_amr_remesh(mclg_ctx *ctx, double frac, int base_level, int target_level, size_t *nel);
 /* The same in two halves, so that the host work overlaps the GPU's: begin takes
  * the flags of the current T and the new leaves, then builds the new mesh and

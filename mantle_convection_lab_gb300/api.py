@@ -153,6 +153,7 @@ def lib():
         "mclg_amr_remesh_end": (C.c_int, [vp, C.POINTER(sz)]),
         "mclg_mesh_new_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
         "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
+        "mclg_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
@@ -515,6 +516,17 @@ class Model:
         gmax = C.c_double()
         _check(lib().mclg_amr_flags(self._c, frac, _uptr(f), f.size, C.byref(gmax)), "amr_flags")
         return f, gmax.value
+
+    def amr_leaves(self, flags, base_level, target_level):
+        """Leaves of the refined tree for per-element flags of the finest level,
+        built on the device (Mesh.amr_leaves builds the same on the host)."""
+        f = np.ascontiguousarray(flags, np.uint8)
+        cap = 1 << (2 * (self.max_level - 1))
+        out = np.zeros(cap, np.int32)
+        n = C.c_size_t()
+        _check(lib().mclg_amr_leaves(self._c, _uptr(f), f.size, base_level, target_level, _iptr(out), cap,
+                                     C.byref(n)), "amr_leaves")
+        return out[:n.value].copy()
 
     def remesh(self, frac, base_level, target_level):
         """Refine by |grad T| and rebuild the model on the new mesh in place."""

@@ -696,6 +696,17 @@ __global__ void __launch_bounds__(kBlock) k_qt_extrapolate(int n2, int ne, const
 		p[i] = 2.0 * p1[i] - p2[i];
 }
 
+// d1 <- d - (d1 - d2): the history shift of the second step after a remesh
+__global__ void __launch_bounds__(kBlock) k_qt_shift(int n2, int ne, const double *d, const double *p, double *d1,
+                                                     double *p1, const double *d2, const double *p2)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n2)
+		d1[i] = d[i] - d1[i] + d2[i];
+	if (i < ne)
+		p1[i] = p[i] - p1[i] + p2[i];
+}
+
 // Coarse-level viscosity from the finer level around the same node: the value
 // there (avg 0), or the mean (1) or log-mean (2) over the node and its matrix
 // neighbours on the finer level, weighted 1 (the node), 1/2 (a neighbour

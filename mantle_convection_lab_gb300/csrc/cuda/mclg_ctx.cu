@@ -28,9 +28,15 @@ void upload_shape_tables_mg(const ShapeTables &s, cudaStream_t st);
 void upload_shape_tables_qt(const ShapeTables &s, cudaStream_t st);
 __global__ void k_qt_extrapolate(int n2, int ne, const double *d1, const double *d2, const double *p1, const double *p2,
                                  double *d, double *p);
+__global__ void k_qt_shift(int n2, int ne, const double *d, const double *p, double *d1, double *p1, const double *d2,
+                           const double *p2);
 __global__ void k_qt_inject(int n, const int *map, const double *src, double *dst, int avg, int nno_f,
                             const int *nb_f, const unsigned char *cnt_f, const double *X_f);
 void upload_op_tables(const ShapeTables &S, double r, cudaStream_t st);
+// refined meshes: levels of at most this many nodes run in one block of the
+// solver kernel (block barriers instead of grid barriers); from a sweep on
+// configuration 2 (2048: 25.8, 512: 27.5, 128: 27.8, 0: 27.4 steps/s)
+constexpr int kQtBlockNodes = 256;
 void *stokes_mg_kernel(int fp64);
 void *stokes_mg_batch_kernel(int fp64);
 __global__ void k_bab(DevLevel L, const double2 *Kdiag, double *bab);
@@ -99,6 +105,7 @@ struct mclg_ctx {
 	mclg_cnn *gnet;
 	int gmode, gs, gnc;           // mode, coarsening factor, coarse elements per side
 	int ghist;                    // solutions seen since the guess was switched on
+	int hist_shift;               // steps until the history is shifted after a remesh (see launch_stokes_qt)
 	int gsample, gtimed;          // a sample from the last solve exists; ev[6] was recorded
 	double2 *d_h1, *d_h2, *d_cand;   // last two solutions, second candidate guess
 	double *p_h1, *p_h2, *p_cand, *gscale;
@@ -747,8 +754,9 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a, Prebuilt *pre)
 	H.nlev = nlev;
 	H.smooth = f.mg_smooth > 0 ? f.mg_smooth : 1;
 	H.omega = (TI)f.mg_omega;
-	H.nblk = 0;   // the smallest levels run in one block
-	while (H.nblk < nlev - 1 && m.lev[lo + H.nblk].nno <= 2048)
+	// the smallest levels (at most kQtBlockNodes nodes) run in one block
+	H.nblk = 0;
+	while (H.nblk < nlev - 1 && m.lev[lo + H.nblk].nno <= kQtBlockNodes)
 		H.nblk++;
 	for (int l = lo; l <= top; l++) {
 		const int k = l - lo;
@@ -889,12 +897,26 @@ static int launch_stokes_qt(mclg_ctx *c)
 	CK(cudaMemsetAsync(&c->sc->guess_used, 0xff, sizeof(int), c->st));
 	const bool track = c->d_h1 != NULL;
 	if (track) {   // history: d_h2 <- d_h1, d_h1 <- d (the last two solutions)
+		const size_t n = 2 * nn > ne ? 2 * nn : ne;
+		if (c->hist_shift == 1 && f.warm_start == 3 && c->ghist >= 2) {
+			// the second step after a remesh: d_h1, d_h2 are the last two solutions of
+			// the old mesh interpolated, d the first solution on the new one.  Their
+			// extrapolation 2 d - d_h1 would add the interpolation error of d_h1 once
+			// more; d_h1 <- d - (d_h1 - d_h2) makes it d + (d_h1 - d_h2), the last
+			// interpolated increment on top of the new mesh's solution.
+			k_qt_shift<<<blocks_for(n), kBlock, 0, c->st>>>((int)(2 * nn), (int)ne, (const double *)c->d, c->p,
+			                                               (double *)c->d_h1, c->p_h1, (const double *)c->d_h2,
+			                                               c->p_h2);
+			if ((rc = check_launch(c, "k_qt_shift")))
+				return rc;
+		}
+		if (c->hist_shift > 0)
+			c->hist_shift--;
 		CK(cudaMemcpyAsync(c->d_h2, c->d_h1, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h2, c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		if (f.warm_start == 3 && c->ghist >= 2) {
-			const size_t n = 2 * nn > ne ? 2 * nn : ne;
 			k_qt_extrapolate<<<blocks_for(n), kBlock, 0, c->st>>>((int)(2 * nn), (int)ne, (const double *)c->d_h1,
 			                                                       (const double *)c->d_h2, c->p_h1, c->p_h2,
 			                                                       (double *)c->d, c->p);
@@ -2689,6 +2711,8 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 
 // ---- |grad T| adaptive refinement ----------------------------------------------------
 namespace mclg {
+cudaError_t amr_tree_leaves(cudaStream_t st, int nel, const int *Mcode, const unsigned char *flags, int F, int base,
+                            int target, std::vector<int> &leaves, long long *launches);
 void amr_flags(cudaStream_t st, const DevLevel &L, const double *T, double frac, double *g, unsigned char *flags,
                double *gmax);
 }
@@ -2724,6 +2748,77 @@ int mclg_amr_flags(mclg_ctx *c, double frac, unsigned char *flags, size_t n, dou
 		return cuda_fail(e, "mclg_amr_flags");
 	if (gmax)
 		*gmax = hm;
+	return MCLG_OK;
+}
+
+// The refined tree's leaves from per-element flags on the device (df: device
+// flags of the finest level's elements, NULL to compute them from T with frac).
+static int device_leaves(mclg_ctx *c, const unsigned char *df_in, double frac, int base_level, int target_level,
+                         std::vector<int> &leaves)
+{
+	const int F = c->mesh.max_level - 1;
+	if (base_level < 0 || base_level > target_level || target_level > F) {
+		mclg_set_error("refinement levels base=%d target=%d: need 0 <= base <= target <= %d", base_level,
+		               target_level, F);
+		return MCLG_BAD_INPUT;
+	}
+	const mclg_level &H = c->mesh.lev[c->fl];
+	const size_t n = (size_t)H.nel;
+	int *dM = NULL;
+	double *g = NULL, *dmax = NULL;
+	unsigned char *df = NULL;
+	cudaError_t e = cudaMalloc((void **)&dM, (n + 1) * sizeof(int));
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(dM, H.Mcode, n * sizeof(int), cudaMemcpyHostToDevice, c->st);
+	if (e == cudaSuccess && df_in == NULL) {
+		e = cudaMalloc((void **)&g, (n + 1) * sizeof(double));
+		if (e == cudaSuccess) e = cudaMalloc((void **)&df, n + 1);
+		if (e == cudaSuccess) e = cudaMalloc((void **)&dmax, sizeof(double));
+		if (e == cudaSuccess) {
+			amr_flags(c->st, c->L, c->T, frac, g, df, dmax);
+			c->launches += 2;
+			e = cudaGetLastError();
+		}
+	}
+	if (e == cudaSuccess)
+		e = amr_tree_leaves(c->st, (int)n, dM, df_in ? df_in : df, F, base_level, target_level, leaves, &c->launches);
+	cudaFree(dM);
+	cudaFree(g);
+	cudaFree(df);
+	cudaFree(dmax);
+	if (e != cudaSuccess)
+		return cuda_fail(e, "refined tree on the device");
+	return MCLG_OK;
+}
+
+int mclg_amr_leaves(mclg_ctx *c, const unsigned char *flags, size_t n, int base_level, int target_level, int *leaves,
+                    size_t cap, size_t *nleaves)
+{
+	if (c == NULL || flags == NULL || leaves == NULL || nleaves == NULL)
+		return MCLG_BAD_INPUT;
+	if (n != (size_t)c->L.nel) {
+		mclg_set_error("flag buffer has %zu entries, the mesh %d elements", n, c->L.nel);
+		return MCLG_BAD_INPUT;
+	}
+	unsigned char *df = NULL;
+	cudaError_t e = cudaMalloc((void **)&df, n + 1);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(df, flags, n, cudaMemcpyHostToDevice, c->st);
+	if (e != cudaSuccess) {
+		cudaFree(df);
+		return cuda_fail(e, "mclg_amr_leaves");
+	}
+	std::vector<int> out;
+	const int rc = device_leaves(c, df, 0.0, base_level, target_level, out);
+	cudaFree(df);
+	if (rc)
+		return rc;
+	*nleaves = out.size();
+	if (out.size() > cap) {
+		mclg_set_error("the refined tree has %zu leaves, the buffer holds %zu", out.size(), cap);
+		return MCLG_BAD_INPUT;
+	}
+	memcpy(leaves, out.data(), out.size() * sizeof(int));
 	return MCLG_OK;
 }
 
@@ -2763,20 +2858,16 @@ int mclg_amr_remesh_begin(mclg_ctx *c, double frac, int base_level, int target_l
 		mclg_set_error("a remesh is already pending: finish it with mclg_amr_remesh_end");
 		return MCLG_BAD_INPUT;
 	}
-	const size_t ne = (size_t)c->L.nel;
-	std::vector<unsigned char> flags(ne);
-	int rc = mclg_amr_flags(c, frac, flags.data(), ne, NULL);
-	if (rc)
-		return rc;
-	int *leaves = NULL;
-	long nl = 0;
-	rc = mclg_amr_build_leaves(&c->mesh, flags.data(), base_level, target_level, &leaves, &nl);
+	if (!(frac >= 0.0))
+		return MCLG_BAD_INPUT;
+	// flags and the new tree on the device
+	std::vector<int> leaves;
+	int rc = device_leaves(c, NULL, frac, base_level, target_level, leaves);
 	if (rc)
 		return rc;
 	RemeshJob *j = new RemeshJob();
 	j->cfg = c->cfg;
-	j->leaves.assign(leaves, leaves + nl);
-	free(leaves);
+	j->leaves.swap(leaves);
 	j->rc = MCLG_OK;
 	j->err[0] = 0;
 	memset(&j->pb, 0, sizeof j->pb);
@@ -2899,6 +2990,7 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 				if (e != cudaSuccess)
 					rc = cuda_fail(e, "mclg_amr_remesh");
 				n->ghist = c->ghist;
+				n->hist_shift = 2;
 			}
 		}
 	}

@@ -1,6 +1,9 @@
 """|grad T| refinement on the GPU.
 
 - the device flags equal the numpy oracle's bit for bit;
+- the device tree builder (mclg_amr_leaves) gives the host builder's leaves
+  bit for bit, on random flags over uniform and graded meshes, on the edge
+  cases (no flag, every flag, base == target) and at configuration 2's size;
 - mclg_amr_remesh rebuilds the model on the tree the host builder makes from
   those flags and carries T over exactly as the host transfer does; on the
   refined mesh (hanging nodes) its operators match the CPU oracle's and its
@@ -47,6 +50,53 @@ def test_flags_equal_oracle():
     np.testing.assert_array_equal(flags, want)
     assert gmax == g.max()
     assert 0 < flags.sum() < flags.size
+
+
+def _graded_leaves(c, seed):
+    """A graded start mesh: the host builder's tree on random flags."""
+    m = Mesh(c, leaves=base_leaves())
+    flags = (np.random.default_rng(seed).random(m.nel) < 0.15).astype(np.uint8)
+    return m.amr_leaves(flags, BASE, TARGET)
+
+
+@pytest.mark.parametrize("seed,graded,base,target,density", [
+    (0, False, BASE, TARGET, 0.1), (1, False, 2, 6, 0.02), (2, True, BASE, TARGET, 0.3), (3, True, 1, 5, 0.05),
+    (4, True, 0, 6, 0.01), (5, False, BASE, TARGET, 0.0), (6, True, BASE, TARGET, 1.0), (7, True, 4, 4, 0.5),
+])
+def test_device_tree_equals_host_builder(seed, graded, base, target, density):
+    c = cfg()
+    start = _graded_leaves(c, 100 + seed) if graded else base_leaves()
+    host = Mesh(c, leaves=start)
+    flags = (np.random.default_rng(seed).random(host.nel) < density).astype(np.uint8)
+    want = host.amr_leaves(flags, base, target)
+    with Model(c, leaves=start) as m:
+        got = m.amr_leaves(flags, base, target)
+        np.testing.assert_array_equal(got, want)
+        with pytest.raises(MclgError):
+            m.amr_leaves(flags, 3, 2)                 # base above target
+        with pytest.raises(MclgError):
+            m.amr_leaves(flags, 0, F + 1)             # target beyond the finest level
+        with pytest.raises(MclgError):
+            m.amr_leaves(flags[:-1], base, target)    # one flag short
+
+
+def test_device_tree_at_configuration_2_size():
+    cfg2 = Config.from_input(amr.CFG2_INPUT)
+    cfg2.precision, cfg2.warm_start = 1, 3
+    start = amr.uniform_leaves(cfg2.level - 1, 7)
+    with Model(cfg2, leaves=start) as m:
+        m.initial_temperature()
+        flags, _ = m.amr_flags(0.2)
+        host = Mesh(cfg2, leaves=start)
+        want = host.amr_leaves(flags, 7, 10)
+        np.testing.assert_array_equal(m.amr_leaves(flags, 7, 10), want)
+        # and once more from the refined mesh, as the next remesh sees it
+        m.remesh(0.2, 7, 10)
+        for _ in range(2):
+            m.step()
+        flags2, _ = m.amr_flags(0.2)
+        host2 = Mesh(cfg2, leaves=want)
+        np.testing.assert_array_equal(m.amr_leaves(flags2, 7, 10), host2.amr_leaves(flags2, 7, 10))
 
 
 def test_remesh_matches_host_pipeline_and_oracle():
