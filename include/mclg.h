@@ -323,11 +323,11 @@ int mclg_amr_leaves(mclg_ctx *ctx, const unsigned char *flags, size_t n, int bas
                     size_t cap, size_t *nleaves);
 int mclg_amr_remesh(mclg_ctx *ctx, double frac, int base_level, int target_level, size_t *nel);
 /* The same in two halves, so that the host work overlaps the GPU's: begin takes
- * the flags of the current T and the new leaves, then builds the new mesh and
- * the refined-mesh solver's lists on a worker thread and returns; the caller
- * may go on stepping the old mesh; end waits for the worker, creates the new
- * device state and carries the current fields over (as mclg_amr_remesh).  One
- * remesh may be pending at a time; mclg_destroy finishes a pending one. */
+ * the flags of the current T and the new tree (device), then builds the new
+ * mesh, the refined-mesh solver's lists and the new device state on a worker
+ * thread and returns; the caller may go on stepping the old mesh; end waits
+ * for the worker and carries the current fields over (as mclg_amr_remesh).
+ * One remesh may be pending at a time; mclg_destroy finishes a pending one. */
 int mclg_amr_remesh_begin(mclg_ctx *ctx, double frac, int base_level, int target_level);
 int mclg_amr_remesh_end(mclg_ctx *ctx, size_t *nel);
 int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n);

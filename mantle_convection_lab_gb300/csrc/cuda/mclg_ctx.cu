@@ -5,6 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <mutex>
 #include <thread>
 #include <vector>
 #include "k_mg.cuh"
@@ -670,6 +671,48 @@ static bool coarse_level(const mclg_ctx *c, int lev, int *k)
 // ---- converged solver on refined meshes ------------------------------------------
 // Host structures of a model built ahead of it (a remesh prepares them on a
 // worker thread while the GPU keeps stepping the old mesh).
+// The constant-memory tables of the kernels are the same for every context on a
+// device (the Q1 element tables are fixed; the operator tables depend on the
+// box's aspect ratio r): each kind is uploaded once per device (again when r
+// changes) and waited for, so that no context's kernel reads a table before
+// its upload and no upload rewrites a table while another context's kernels
+// run (a remesh builds the new context on a worker thread while the old one
+// steps).
+enum { kTabElem = 1, kTabUzawa = 2, kTabHeat = 4, kTabMg = 8, kTabOp = 16, kTabQt = 32 };
+static std::mutex g_tab_mu;
+static unsigned g_tab_done[64];
+static double g_tab_r[64];
+
+static int tables_once(mclg_ctx *c, unsigned kinds, double r)
+{
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+		return cuda_fail(cudaErrorInvalidDevice, "tables_once");
+	std::lock_guard<std::mutex> lock(g_tab_mu);
+	unsigned need = kinds & ~g_tab_done[dev];
+	if ((kinds & kTabOp) && (g_tab_done[dev] & kTabOp) && g_tab_r[dev] != r)
+		need |= kTabOp;
+	if (need == 0)
+		return MCLG_OK;
+	ShapeTables S;
+	shape_tables(S);
+	if (need & kTabElem) upload_shape_tables_elem(S, c->st);
+	if (need & kTabUzawa) upload_shape_tables_uzawa(S, c->st);
+	if (need & kTabHeat) upload_shape_tables_heat(S, c->st);
+	if (need & kTabMg) upload_shape_tables_mg(S, c->st);
+	if (need & kTabOp) upload_op_tables(S, r, c->st);
+	if (need & kTabQt) upload_shape_tables_qt(S, c->st);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(c->st);
+	if (e != cudaSuccess)
+		return cuda_fail(e, "constant tables");
+	g_tab_done[dev] |= need;
+	if (need & kTabOp)
+		g_tab_r[dev] = r;
+	return MCLG_OK;
+}
+
 struct Prebuilt {
 	mclg_mesh mesh;
 	mclg_qt_level q[MCLG_MAX_LEVEL];
@@ -873,9 +916,8 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a, Prebuilt *pre)
 	a.max_refine = f.max_refine;
 	a.max_outer = f.max_outer;
 	(void)sizeof(V);
-	ShapeTables S;
-	shape_tables(S);
-	upload_shape_tables_qt(S, c->st);
+	if ((rc = tables_once(c, kTabQt, 0.0)) != MCLG_OK)
+		return rc;
 	CK(cudaStreamSynchronize(c->st));
 	c->qt_on = 1;
 	return MCLG_OK;
@@ -1238,11 +1280,11 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 		*out = NULL;
 		return rc;
 	}
-	ShapeTables S;
-	shape_tables(S);
-	upload_shape_tables_elem(S, c->st);
-	upload_shape_tables_uzawa(S, c->st);
-	upload_shape_tables_heat(S, c->st);
+	if ((rc = tables_once(c, kTabElem | kTabUzawa | kTabHeat, 0.0)) != MCLG_OK) {
+		mclg_destroy(c);
+		*out = NULL;
+		return rc;
+	}
 	const size_t nn = c->L.nno, ne = c->L.nel, nbw = c->L.nbw;
 	CKD(dalloc(&c->T, nn));
 	CKD(dalloc(&c->vis, nn));
@@ -1321,8 +1363,11 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 			*out = NULL;
 			return rc;
 		}
-		upload_shape_tables_mg(S, c->st);
-		upload_op_tables(S, c->mesh.dz[c->fl] / c->mesh.dx[c->fl], c->st);
+		if ((rc = tables_once(c, kTabMg | kTabOp, c->mesh.dz[c->fl] / c->mesh.dx[c->fl])) != MCLG_OK) {
+			mclg_destroy(c);
+			*out = NULL;
+			return rc;
+		}
 		c->coop_mg = coop_blocks(stokes_mg_kernel(cfg->precision == 2), c->num_sms, 1 << 30);
 		if (cfg->warm_start == 3 && (rc = alloc_history(c)) != MCLG_OK) {
 			mclg_destroy(c);
@@ -2826,18 +2871,76 @@ int mclg_amr_leaves(mclg_ctx *c, const unsigned char *flags, size_t n, int base_
 // then the context is rebuilt on the new mesh in place: the handle stays
 // valid, time step and model time carry over, velocity and pressure restart
 // from zero.
-// A remesh in two halves: begin() takes the flags and the new leaves and
-// builds the new mesh and the solver's lists on a worker thread; end() waits
-// for it, creates the device state, carries the fields over and swaps it in.
-// Between them the caller may go on stepping the old mesh.
+// A remesh in two halves: begin() computes the flags and the new tree on the
+// device and starts a worker thread that builds the new mesh, the solver's
+// lists and the new context's device state (on a stream of its own); end()
+// waits for it, carries the fields over and swaps the new state in.  Between
+// them the caller may go on stepping the old mesh.
+// Element-wise fields (the pressure) between two trees of the same finest
+// level: a new element takes the area mean of the old field over it.  Where
+// the old leaf covering it is as coarse or coarser that is the old value;
+// where the old mesh was finer, the mean of its children (recursively by
+// quadrant), so that a pattern alternating over the children (the Q1-P0
+// pressure's checkerboard modes, null on the old mesh but not on the new one)
+// is not carried into the new element.
+static unsigned pt_compact16(unsigned v)
+{
+	v &= 0x55555555u;
+	v = (v | (v >> 1)) & 0x33333333u;
+	v = (v | (v >> 2)) & 0x0f0f0f0fu;
+	v = (v | (v >> 4)) & 0x00ff00ffu;
+	v = (v | (v >> 8)) & 0x0000ffffu;
+	return v;
+}
+
+static double region_mean(const mclg_level &HO, int F, int ncell, const double *P, int x0, int z0, int s)
+{
+	const int e = HO.cell_elem[(size_t)x0 * ncell + z0];
+	const int so = 1 << (F - (HO.Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1)));
+	if (so >= s)
+		return P[e];
+	const int h = s >> 1;
+	return 0.25 * ((region_mean(HO, F, ncell, P, x0, z0, h) + region_mean(HO, F, ncell, P, x0, z0 + h, h)) +
+	               (region_mean(HO, F, ncell, P, x0 + h, z0, h) + region_mean(HO, F, ncell, P, x0 + h, z0 + h, h)));
+}
+
+static void element_transfer(const mclg_mesh &from, const double *P_old, const mclg_mesh &to, double *P_new)
+{
+	const int F = from.max_level - 1, ncell = from.gnox - 1;
+	const mclg_level &HO = from.lev[F], &HN = to.lev[to.max_level - 1];
+	for (int e = 0; e < HN.nel; e++) {
+		const int lvl = HN.Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
+		const unsigned code = (unsigned)(HN.Mcode[e] >> MCLG_LEVEL_BITS);
+		P_new[e] = region_mean(HO, F, ncell, P_old, (int)pt_compact16(code >> 1), (int)pt_compact16(code),
+		                       1 << (F - lvl));
+	}
+}
+
 struct RemeshJob {
 	std::thread th;
 	mclg_config cfg;
 	std::vector<int> leaves;
 	Prebuilt pb;
+	int device;        // the caller's device (the current device is per thread)
+	mclg_ctx *n;       // the new context, created by the worker
 	int rc;
 	char err[512];
 };
+
+// The worker: the host structures, then the new context's device state on a
+// stream of its own (the old context keeps stepping on its stream meanwhile).
+static void remesh_work(RemeshJob *j)
+{
+	j->rc = cudaSetDevice(j->device) == cudaSuccess ? MCLG_OK : MCLG_CUDA_ERROR;
+	if (j->rc != MCLG_OK)
+		mclg_set_error("remesh worker: cannot select device %d", j->device);
+	if (j->rc == MCLG_OK)
+		j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
+	if (j->rc == MCLG_OK)
+		j->rc = create_impl(&j->n, &j->cfg, j->leaves.data(), (long)j->leaves.size(), &j->pb);
+	if (j->rc != MCLG_OK)
+		snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+}
 
 static void remesh_job_free(mclg_ctx *c)
 {
@@ -2846,6 +2949,8 @@ static void remesh_job_free(mclg_ctx *c)
 	if (c->rj->th.joinable())
 		c->rj->th.join();
 	prebuilt_free(&c->rj->pb);
+	if (c->rj->n != NULL)
+		mclg_destroy(c->rj->n);
 	delete c->rj;
 	c->rj = NULL;
 }
@@ -2870,18 +2975,17 @@ int mclg_amr_remesh_begin(mclg_ctx *c, double frac, int base_level, int target_l
 	j->leaves.swap(leaves);
 	j->rc = MCLG_OK;
 	j->err[0] = 0;
+	j->n = NULL;
 	memset(&j->pb, 0, sizeof j->pb);
+	if (cudaGetDevice(&j->device) != cudaSuccess) {
+		delete j;
+		return cuda_fail(cudaErrorInvalidDevice, "mclg_amr_remesh_begin");
+	}
 	c->rj = j;
 	try {
-		j->th = std::thread([j]() {
-			j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
-			if (j->rc != MCLG_OK)
-				snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
-		});
+		j->th = std::thread(remesh_work, j);
 	} catch (...) {   // no thread: build here
-		j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
-		if (j->rc != MCLG_OK)
-			snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
+		remesh_work(j);
 	}
 	return MCLG_OK;
 }
@@ -2902,20 +3006,18 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 		return rc;
 	}
 	const size_t ne = (size_t)c->L.nel, nn = (size_t)c->L.nno;
-	mclg_config cfg = c->cfg;
-	mclg_ctx *n = NULL;
-	int rc = create_impl(&n, &cfg, j->leaves.data(), (long)j->leaves.size(), &j->pb);
+	const mclg_config cfg = c->cfg;
+	mclg_ctx *n = j->n;   // created by the worker
+	j->n = NULL;
 	remesh_job_free(c);
-	if (rc)
-		return rc;
 	std::vector<double> T_old(nn), T_new((size_t)n->L.nno);
-	rc = mclg_get_field(c, MCLG_F_T, -1, T_old.data(), nn);
+	int rc = mclg_get_field(c, MCLG_F_T, -1, T_old.data(), nn);
 	if (rc == MCLG_OK)
 		rc = mclg_amr_transfer(&c->mesh, T_old.data(), &n->mesh, T_new.data());
 	if (rc == MCLG_OK)
 		rc = mclg_set_field(n, MCLG_F_T, -1, T_new.data(), T_new.size());
-	// converged solvers: the velocity (bilinear, as T) and the pressure (the old element
-	// holding the new element's centre) start the first solve on the new mesh; the FP64
+	// converged solvers: the velocity (bilinear, as T) and the pressure (area mean of the
+	// old pressure over the new element) start the first solve on the new mesh; the FP64
 	// replica starts as the reference does (d = 0, p = 0 on a new mesh)
 	const bool carry = cfg.precision != 0;
 	const mclg_level &HN = n->mesh.lev[n->fl], &HO = c->mesh.lev[c->fl];
@@ -2938,20 +3040,8 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 	if (rc == MCLG_OK && carry) {
 		std::vector<double> P_old(ne), P_new(ne2);
 		rc = mclg_get_field(c, MCLG_F_P, -1, P_old.data(), ne);
-		const int ncell = c->mesh.gnox - 1;
-		const double dxc = c->mesh.length / ncell, dzc = c->mesh.height / ncell;
-		for (size_t e = 0; e < ne2 && rc == MCLG_OK; e++) {
-			double x = 0.0, z = 0.0;
-			for (int a = 0; a < 4; a++) {
-				const int A = HN.ienl[(size_t)a * ne2 + e];
-				x += 0.25 * HN.X[A];
-				z += 0.25 * HN.X[nn2 + A];
-			}
-			int cx = (int)(x / dxc), cz = (int)(z / dzc);
-			cx = cx < 0 ? 0 : cx >= ncell ? ncell - 1 : cx;
-			cz = cz < 0 ? 0 : cz >= ncell ? ncell - 1 : cz;
-			P_new[e] = P_old[HO.cell_elem[(size_t)cx * ncell + cz]];
-		}
+		if (rc == MCLG_OK)
+			element_transfer(c->mesh, P_old.data(), n->mesh, P_new.data());
 		if (rc == MCLG_OK)
 			rc = mclg_set_field(n, MCLG_F_P, -1, P_new.data(), ne2);
 		// the previous step's solution too, so that the extrapolated warm start
@@ -2971,18 +3061,8 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 					if (HN.id[(size_t)comp * nn2 + A] >= 0)
 						D_new[2 * A + comp] = comp_new[A];
 			}
-			for (size_t e2 = 0; e2 < ne2 && rc == MCLG_OK; e2++) {
-				double x = 0.0, z = 0.0;
-				for (int a = 0; a < 4; a++) {
-					const int A = HN.ienl[(size_t)a * ne2 + e2];
-					x += 0.25 * HN.X[A];
-					z += 0.25 * HN.X[nn2 + A];
-				}
-				int cx = (int)(x / dxc), cz = (int)(z / dzc);
-				cx = cx < 0 ? 0 : cx >= ncell ? ncell - 1 : cx;
-				cz = cz < 0 ? 0 : cz >= ncell ? ncell - 1 : cz;
-				Phn[e2] = Ph[HO.cell_elem[(size_t)cx * ncell + cz]];
-			}
+			if (rc == MCLG_OK)
+				element_transfer(c->mesh, Ph.data(), n->mesh, Phn.data());
 			if (rc == MCLG_OK) {
 				e = cudaMemcpy(n->d_h1, D_new.data(), 2 * nn2 * sizeof(double), cudaMemcpyHostToDevice);
 				if (e == cudaSuccess)

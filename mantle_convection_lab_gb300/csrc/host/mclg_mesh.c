@@ -69,7 +69,21 @@ static long sort_unique(int *a, long n)
 	long i, j = 0;
 	if (n <= 1)
 		return n;
-	qsort(a, (size_t)n, sizeof(int), cmp_int);
+	for (i = 1; i < n && a[i - 1] < a[i]; i++)
+		;
+	if (i == n)   /* already strictly increasing (a leaf list) */
+		return n;
+	if (n <= 32) {   /* a node's neighbours: insertion sort */
+		for (i = 1; i < n; i++) {
+			const int v = a[i];
+			long k = i;
+			for (; k > 0 && a[k - 1] > v; k--)
+				a[k] = a[k - 1];
+			a[k] = v;
+		}
+	} else {
+		qsort(a, (size_t)n, sizeof(int), cmp_int);
+	}
 	for (i = 1; i < n; i++)
 		if (a[i] != a[j])
 			a[++j] = a[i];

@@ -349,187 +349,234 @@ static int cmp_contrib(const void *a, const void *b)
 	return x->src < y->src ? -1 : x->src > y->src;
 }
 
-static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
+/* One row of C^T K C: its contributions (tgt = 4*slot + cc, sorted by tgt, then
+ * src) and its reduced columns (sorted).  row/rcap: a growable scratch list;
+ * cols: room for 512 columns.  Returns 0, or -1 when out of memory or a row
+ * has more than 512 columns. */
+static int reduced_row(const mclg_level *L, const mclg_qt_level *q, int A, contrib **rowp, long *rcap, int *cols,
+                       long *rn_out, int *ncols_out)
 {
 	const int nno = L->nno;
-	contrib *row = NULL;
-	long rn = 0, rcap = 0, tot = 0, tcap = 0;
-	int *cols = NULL, ncols, maxw = 1, rc = MCLG_BAD_INPUT;
-	int **rnb_rows = NULL, *rcnt = NULL;
-	q->rc_off = (int *)calloc((size_t)nno + 1, sizeof(int));
-	rnb_rows = (int **)calloc((size_t)nno, sizeof(int *));
-	rcnt = (int *)calloc((size_t)nno, sizeof(int));
-	cols = (int *)malloc(512 * sizeof(int));
-	if (!q->rc_off || !rnb_rows || !rcnt || !cols)
-		goto out;
-	for (int A = 0; A < nno; A++) {
-		rn = 0;
-		/* the common row: nothing folded into it and no constrained column, so
-		 * its reduced row is K's row, in K's (sorted) column order */
-		int plain = q->fo_off[2 * A + 2] == q->fo_off[2 * A];
-		for (int k = 0; plain && k < L->nb_cnt[A]; k++) {
+	contrib *row = *rowp;
+	long rn = 0;
+	int ncols = 0;
+#define PUSH_CONTRIB(B_, tgt_, src_, w_)                                            \
+	do {                                                                           \
+		if (rn == *rcap) {                                                         \
+			long cap_ = *rcap ? 2 * *rcap : 256;                                   \
+			contrib *r2_ = (contrib *)realloc(row, (size_t)cap_ * sizeof(contrib)); \
+			if (r2_ == NULL)                                                       \
+				goto fail;                                                         \
+			row = r2_;                                                             \
+			*rowp = row;                                                           \
+			*rcap = cap_;                                                          \
+		}                                                                          \
+		row[rn].B = (B_);                                                          \
+		row[rn].tgt = (tgt_);                                                      \
+		row[rn].src = (src_);                                                      \
+		row[rn].w = (w_);                                                          \
+		rn++;                                                                      \
+	} while (0)
+	/* the common row: nothing folded into it and no constrained column, so its
+	 * reduced row is K's row, in K's (sorted) column order */
+	int plain = q->fo_off[2 * A + 2] == q->fo_off[2 * A];
+	for (int k = 0; plain && k < L->nb_cnt[A]; k++) {
+		const int B = L->nb[(size_t)k * nno + A];
+		plain = q->kind[2 * B] != 2 && q->kind[2 * B + 1] != 2;
+	}
+	if (plain) {
+		for (int k = 0; k < L->nb_cnt[A]; k++) {
 			const int B = L->nb[(size_t)k * nno + A];
-			plain = q->kind[2 * B] != 2 && q->kind[2 * B + 1] != 2;
-		}
-		if (plain) {
-			ncols = 0;
-			for (int k = 0; k < L->nb_cnt[A]; k++) {
-				const int B = L->nb[(size_t)k * nno + A];
-				if (q->kind[2 * B] == 0 && q->kind[2 * B + 1] == 0)
-					continue;
-				for (int cc = 0; cc < 4; cc++) {
-					const int c = cc >> 1, c2 = cc & 1;
-					if (q->kind[2 * A + c] != 1 || q->kind[2 * B + c2] != 1)
-						continue;
-					if (rn == rcap) {
-						long cap = rcap ? 2 * rcap : 256;
-						contrib *r2 = (contrib *)realloc(row, (size_t)cap * sizeof(contrib));
-						if (r2 == NULL)
-							goto out;
-						row = r2;
-						rcap = cap;
-					}
-					row[rn].B = B;
-					row[rn].tgt = 4 * ncols + cc;
-					row[rn].src = (int)(((size_t)k * nno + A) * 4 + (size_t)cc);
-					row[rn].w = 1.0;
-					rn++;
-				}
-				if (ncols == 512)
-					goto out;
-				cols[ncols++] = B;
-			}
-			goto row_done;
-		}
-		for (int c = 0; c < 2; c++) {
-			const int da = 2 * A + c;
-			if (q->kind[da] != 1)
+			if (q->kind[2 * B] == 0 && q->kind[2 * B + 1] == 0)
 				continue;
-			/* rows holding dof (A,c): itself and the constrained dofs folded into it */
-			for (int t = -1; t < q->fo_off[da + 1] - q->fo_off[da]; t++) {
-				const int jd = t < 0 ? da : q->fo_dof[q->fo_off[da] + t];
-				const double wj = t < 0 ? 1.0 : q->fo_w[q->fo_off[da] + t];
-				const int j = jd >> 1;
-				for (int k = 0; k < L->nb_cnt[j]; k++) {
-					const int B = L->nb[(size_t)k * nno + j];
-					for (int c2 = 0; c2 < 2; c2++) {
-						const int db = 2 * B + c2;
-						const int src = (int)(((size_t)k * nno + j) * 4 + (size_t)(c * 2 + c2));
-						int ni = 1, first = 0;
-						if (q->kind[db] == 0)
-							continue;
-						if (q->kind[db] == 2) {
-							first = q->ex_off[db];
-							ni = q->ex_off[db + 1] - first;
-						}
-						for (int i = 0; i < ni; i++) {
-							const int Bp = q->kind[db] == 2 ? q->ex_src[first + i] >> 1 : B;
-							const double wb = q->kind[db] == 2 ? q->ex_w[first + i] : 1.0;
-							if (rn == rcap) {
-								long cap = rcap ? 2 * rcap : 256;
-								contrib *r2 = (contrib *)realloc(row, (size_t)cap * sizeof(contrib));
-								if (r2 == NULL)
-									goto out;
-								row = r2;
-								rcap = cap;
-							}
-							row[rn].B = Bp;
-							row[rn].tgt = c * 2 + c2;   /* slot added below */
-							row[rn].src = src;
-							row[rn].w = wj * wb;
-							rn++;
-						}
+			for (int cc = 0; cc < 4; cc++) {
+				const int c = cc >> 1, c2 = cc & 1;
+				if (q->kind[2 * A + c] != 1 || q->kind[2 * B + c2] != 1)
+					continue;
+				PUSH_CONTRIB(B, 4 * ncols + cc, (int)(((size_t)k * nno + A) * 4 + (size_t)cc), 1.0);
+			}
+			if (ncols == 512)
+				goto fail;
+			cols[ncols++] = B;
+		}
+		*rn_out = rn;
+		*ncols_out = ncols;
+		return 0;
+	}
+	for (int c = 0; c < 2; c++) {
+		const int da = 2 * A + c;
+		if (q->kind[da] != 1)
+			continue;
+		/* rows holding dof (A,c): itself and the constrained dofs folded into it */
+		for (int t = -1; t < q->fo_off[da + 1] - q->fo_off[da]; t++) {
+			const int jd = t < 0 ? da : q->fo_dof[q->fo_off[da] + t];
+			const double wj = t < 0 ? 1.0 : q->fo_w[q->fo_off[da] + t];
+			const int j = jd >> 1;
+			for (int k = 0; k < L->nb_cnt[j]; k++) {
+				const int B = L->nb[(size_t)k * nno + j];
+				for (int c2 = 0; c2 < 2; c2++) {
+					const int db = 2 * B + c2;
+					const int src = (int)(((size_t)k * nno + j) * 4 + (size_t)(c * 2 + c2));
+					int ni = 1, first = 0;
+					if (q->kind[db] == 0)
+						continue;
+					if (q->kind[db] == 2) {
+						first = q->ex_off[db];
+						ni = q->ex_off[db + 1] - first;
+					}
+					for (int i = 0; i < ni; i++) {
+						const int Bp = q->kind[db] == 2 ? q->ex_src[first + i] >> 1 : B;
+						const double wb = q->kind[db] == 2 ? q->ex_w[first + i] : 1.0;
+						PUSH_CONTRIB(Bp, c * 2 + c2, src, wj * wb);   /* slot added below */
 					}
 				}
 			}
 		}
-		/* the row's reduced columns, sorted; the node itself first when present */
-		ncols = 0;
-		for (long i = 0; i < rn; i++) {
-			int f = 0;
-			for (int u = 0; u < ncols; u++)
-				if (cols[u] == row[i].B) {
-					f = 1;
-					break;
-				}
-			if (!f) {
-				if (ncols == 512)
-					goto out;
-				cols[ncols++] = row[i].B;
+	}
+#undef PUSH_CONTRIB
+	/* the row's reduced columns, sorted */
+	for (long i = 0; i < rn; i++) {
+		int f = 0;
+		for (int u = 0; u < ncols; u++)
+			if (cols[u] == row[i].B) {
+				f = 1;
+				break;
 			}
-		}
-		for (int u = 1; u < ncols; u++)
-			for (int v = u; v > 0 && cols[v - 1] > cols[v]; v--) {
-				int t = cols[v];
-				cols[v] = cols[v - 1];
-				cols[v - 1] = t;
-			}
-		for (long i = 0; i < rn; i++) {
-			int slot = 0;
-			while (cols[slot] != row[i].B)
-				slot++;
-			row[i].tgt += 4 * slot;
-		}
-		qsort(row, (size_t)rn, sizeof(contrib), cmp_contrib);
-	row_done:
-		if (ncols > maxw)
-			maxw = ncols;
-		rcnt[A] = ncols;
-		rnb_rows[A] = (int *)malloc((size_t)(ncols > 0 ? ncols : 1) * sizeof(int));
-		if (rnb_rows[A] == NULL)
-			goto out;
-		memcpy(rnb_rows[A], cols, (size_t)ncols * sizeof(int));
-		q->rc_off[A] = (int)tot;
-		if (tot + rn > tcap) {
-			long cap = tcap ? 2 * tcap : 4096;
-			while (cap < tot + rn)
-				cap *= 2;
-			int *t1 = (int *)realloc(q->rc_tgt, (size_t)cap * sizeof(int));
-			if (t1)
-				q->rc_tgt = t1;
-			int *t2 = (int *)realloc(q->rc_src, (size_t)cap * sizeof(int));
-			if (t2)
-				q->rc_src = t2;
-			double *t3 = (double *)realloc(q->rc_w, (size_t)cap * sizeof(double));
-			if (t3)
-				q->rc_w = t3;
-			if (!t1 || !t2 || !t3)
-				goto out;
-			tcap = cap;
-		}
-		for (long i = 0; i < rn; i++) {
-			q->rc_tgt[tot] = row[i].tgt;
-			q->rc_src[tot] = row[i].src;
-			q->rc_w[tot] = row[i].w;
-			tot++;
+		if (!f) {
+			if (ncols == 512)
+				goto fail;
+			cols[ncols++] = row[i].B;
 		}
 	}
-	q->rc_off[nno] = (int)tot;
-	q->n_rc = (int)tot;
-	q->rnbw = maxw;
-	q->rnb = (int *)malloc((size_t)maxw * nno * sizeof(int));
-	q->rcnt = (unsigned char *)malloc((size_t)nno);
-	if (!q->rnb || !q->rcnt || maxw > 255)
+	for (int u = 1; u < ncols; u++)
+		for (int v = u; v > 0 && cols[v - 1] > cols[v]; v--) {
+			int t = cols[v];
+			cols[v] = cols[v - 1];
+			cols[v - 1] = t;
+		}
+	for (long i = 0; i < rn; i++) {
+		int slot = 0;
+		while (cols[slot] != row[i].B)
+			slot++;
+		row[i].tgt += 4 * slot;
+	}
+	qsort(row, (size_t)rn, sizeof(contrib), cmp_contrib);
+	*rn_out = rn;
+	*ncols_out = ncols;
+	return 0;
+fail:
+	return -1;
+}
+
+/* Rows [A0, A1) of a level, on a thread of their own.  Pass 0 counts each
+ * row's contributions and columns; pass 1 writes them at the offsets the
+ * counts gave, into the level's arrays (rows are independent, so the result
+ * does not depend on how the rows are split). */
+typedef struct {
+	const mclg_level *L;
+	mclg_qt_level *q;
+	int A0, A1, pass, maxw, rc;
+	int *cnt;   /* pass 0: [nno] contributions per row; rcnt holds the columns */
+} ro_chunk;
+
+static void *reduced_rows(void *arg)
+{
+	ro_chunk *o = (ro_chunk *)arg;
+	const mclg_level *L = o->L;
+	mclg_qt_level *q = o->q;
+	const int nno = L->nno;
+	contrib *row = NULL;
+	long rn, rcap = 0;
+	int *cols = (int *)malloc(512 * sizeof(int)), ncols;
+	o->rc = MCLG_BAD_INPUT;
+	o->maxw = 1;
+	if (cols == NULL)
 		goto out;
-	for (int A = 0; A < nno; A++) {
-		q->rcnt[A] = (unsigned char)rcnt[A];
-		for (int u = 0; u < maxw; u++)
-			q->rnb[(size_t)u * nno + A] = u < rcnt[A] ? rnb_rows[A][u] : A;
+	for (int A = o->A0; A < o->A1; A++) {
+		if (reduced_row(L, q, A, &row, &rcap, cols, &rn, &ncols))
+			goto out;
+		if (o->pass == 0) {
+			o->cnt[A] = (int)rn;
+			if (ncols > 255)
+				goto out;
+			q->rcnt[A] = (unsigned char)ncols;
+			if (ncols > o->maxw)
+				o->maxw = ncols;
+			continue;
+		}
+		const size_t at = (size_t)q->rc_off[A];
+		for (long i = 0; i < rn; i++) {
+			q->rc_tgt[at + i] = row[i].tgt;
+			q->rc_src[at + i] = row[i].src;
+			q->rc_w[at + i] = row[i].w;
+		}
+		for (int u = 0; u < q->rnbw; u++)
+			q->rnb[(size_t)u * nno + A] = u < ncols ? cols[u] : A;
 	}
-	if (q->rc_tgt == NULL) {   /* no reduced dof at all */
-		q->rc_tgt = (int *)malloc(sizeof(int));
-		q->rc_src = (int *)malloc(sizeof(int));
-		q->rc_w = (double *)malloc(sizeof(double));
-	}
-	rc = MCLG_OK;
+	o->rc = MCLG_OK;
 out:
-	if (rnb_rows)
-		for (int A = 0; A < nno; A++)
-			free(rnb_rows[A]);
-	free(rnb_rows);
-	free(rcnt);
 	free(cols);
 	free(row);
+	return NULL;
+}
+
+static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
+{
+	enum { kMaxChunks = 16 };
+	const int nno = L->nno;
+	/* rows in chunks of at least 8192 nodes, one thread each */
+	int nch = nno / 8192;
+	nch = nch < 1 ? 1 : nch > kMaxChunks ? kMaxChunks : nch;
+	ro_chunk ch[kMaxChunks];
+	pthread_t th[kMaxChunks];
+	int started[kMaxChunks];
+	int rc = MCLG_BAD_INPUT, maxw = 1;
+	long tot = 0;
+	int *cnt = (int *)malloc(((size_t)nno + 1) * sizeof(int));
+	q->rc_off = (int *)malloc(((size_t)nno + 1) * sizeof(int));
+	q->rcnt = (unsigned char *)malloc((size_t)nno + 1);
+	if (!cnt || !q->rc_off || !q->rcnt)
+		goto out;
+	for (int pass = 0; pass < 2; pass++) {
+		for (int i = 0; i < nch; i++) {
+			ch[i].L = L;
+			ch[i].q = q;
+			ch[i].A0 = (int)((long)nno * i / nch);
+			ch[i].A1 = (int)((long)nno * (i + 1) / nch);
+			ch[i].pass = pass;
+			ch[i].cnt = cnt;
+			started[i] = nch > 1 && pthread_create(&th[i], NULL, reduced_rows, &ch[i]) == 0;
+			if (!started[i])
+				reduced_rows(&ch[i]);
+		}
+		for (int i = 0; i < nch; i++)
+			if (started[i])
+				pthread_join(th[i], NULL);
+		for (int i = 0; i < nch; i++)
+			if (ch[i].rc != MCLG_OK)
+				goto out;
+		if (pass == 1)
+			break;
+		for (int i = 0; i < nch; i++)
+			if (ch[i].maxw > maxw)
+				maxw = ch[i].maxw;
+		for (int A = 0; A < nno; A++) {
+			q->rc_off[A] = (int)tot;
+			tot += cnt[A];
+		}
+		q->rc_off[nno] = (int)tot;
+		q->rnbw = maxw;
+		q->rc_tgt = (int *)malloc((size_t)(tot > 0 ? tot : 1) * sizeof(int));
+		q->rc_src = (int *)malloc((size_t)(tot > 0 ? tot : 1) * sizeof(int));
+		q->rc_w = (double *)malloc((size_t)(tot > 0 ? tot : 1) * sizeof(double));
+		q->rnb = (int *)malloc((size_t)maxw * nno * sizeof(int));
+		if (!q->rc_tgt || !q->rc_src || !q->rc_w || !q->rnb)
+			goto out;
+	}
+	q->n_rc = (int)tot;
+	rc = MCLG_OK;
+out:
+	free(cnt);
 	return rc;
 }
 
