@@ -397,8 +397,16 @@ def run_ensemble(args, wl):
     torch.cuda.synchronize()
     ms, ms_solver, launches, res, inner = 0.0, 0.0, 0, 0.0, 0
     grids, graph_used = [], False
+    # one loop for both figures, so that they cover the same steps: value from the
+    # device time of each step (CUDA events), e2e from the wall clock of the same
+    # step followed by every member's temperature read back to the host
+    wall, d2h = 0.0, 0
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         st = e.step()
+        for m in e.members:
+            d2h += 8 * m.get("T").size
+        wall += time.perf_counter() - t0
         ms += st[0].ms_total
         ms_solver += st[0].solver_kernel_ms
         launches += st[0].kernel_launches
@@ -412,14 +420,7 @@ def run_ensemble(args, wl):
         dist.barrier()
     clocks = sampler.stop() if sampler else None
     value = job_throughput(dist, n * args.steps, ms / 1e3)
-    # end to end: the same steps with every member's temperature read back to the host
-    t0 = time.perf_counter()
-    d2h = 0
-    for _ in range(args.steps):
-        e.step()
-        for m in e.members:
-            d2h += 8 * m.get("T").size
-    e2e = job_throughput(dist, n * args.steps, time.perf_counter() - t0)
+    e2e = job_throughput(dist, n * args.steps, wall)
     sizes = [p[0] for p in ensemble.draw(256, 4)]
     # algorithmic bytes of the batched solver launch: the per-model MINRES model, summed
     line = {
