@@ -100,15 +100,43 @@ __device__ __forceinline__ void qt_op_node(const QtLevel<T> &L, const K4 *__rest
 	y1 = y[1];
 }
 
+// Sources of the x a V-cycle pass reads at a node: the stored vector, or the
+// first Jacobi sweep from zero, omega D^-1 b, formed where it is read (so the
+// pass after it needs no barrier for it) with the operations, in the order, of
+// the pass it replaces.  (Forming the prolongation x + P xc the same way inside
+// the first sweep up was measured 2x slower on configuration 2: every
+// neighbour's prolongation is recomputed through a deeper chain of gathers.)
+template <class TI>
+struct QtXStored {
+	typedef typename Q2T<TI>::t X2;
+	const X2 *x;
+	__device__ __forceinline__ X2 operator()(int B) const { return x[B]; }
+};
+
+template <class TI>
+struct QtXFirst {
+	typedef typename Q2T<TI>::t X2;
+	const X2 *b;
+	const TI *invD;
+	TI omega;
+	__device__ __forceinline__ X2 operator()(int B) const
+	{
+		const X2 bv = b[B];
+		X2 o;
+		o.x = omega * invD[2 * B] * bv.x;
+		o.y = omega * invD[2 * B + 1] * bv.y;
+		return o;
+	}
+};
+
 // (C^T K C x) at both dofs of node A from the assembled reduced operator: a
 // plain node-block ELL row (x's constrained and fixed entries are stored as 0
-// and the reduced columns hold every coupling).
-template <class TI>
-__device__ __forceinline__ void qt_kr_node(const QtLevel<TI> &L, const TI *__restrict__ xf, int A, TI &y0, TI &y1)
+// and the reduced columns hold every coupling); x read through src.
+template <class TI, class XS>
+__device__ __forceinline__ void qt_kr_node_src(const QtLevel<TI> &L, const XS &src, int A, TI &y0, TI &y1)
 {
 	typedef typename Q2T<TI>::t X2;
 	typedef typename V4T<TI>::t K4;
-	const X2 *x2 = reinterpret_cast<const X2 *>(xf);
 	TI s0 = TI(0), s1 = TI(0);
 	const int n = L.rcnt[A];
 	for (int k0 = 0; k0 < n; k0 += 4) {
@@ -123,7 +151,7 @@ __device__ __forceinline__ void qt_kr_node(const QtLevel<TI> &L, const TI *__res
 		X2 xv[4];
 #pragma unroll
 		for (int u = 0; u < 4; u++)
-			xv[u] = x2[B[u]];
+			xv[u] = src(B[u]);
 #pragma unroll
 		for (int u = 0; u < 4; u++) {
 			s0 += kb[u].x * xv[u].x + kb[u].y * xv[u].y;
@@ -132,6 +160,13 @@ __device__ __forceinline__ void qt_kr_node(const QtLevel<TI> &L, const TI *__res
 	}
 	y0 = s0;
 	y1 = s1;
+}
+
+template <class TI>
+__device__ __forceinline__ void qt_kr_node(const QtLevel<TI> &L, const TI *__restrict__ xf, int A, TI &y0, TI &y1)
+{
+	const QtXStored<TI> src{reinterpret_cast<const typename Q2T<TI>::t *>(xf)};
+	qt_kr_node_src(L, src, A, y0, y1);
 }
 
 // (C^T G p) at both dofs of node A (FP64, the finest level)
@@ -177,22 +212,30 @@ __device__ __forceinline__ double qt_gt_elem(const QtLevel<T> &Q, const DevLevel
 }
 
 // ---- the V-cycle (TI) -------------------------------------------------------------
-// One damped Jacobi sweep on the constrained operator: xo = xi + w D^-1 (b - A xi).
-template <class TI>
-__device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const typename Q2T<TI>::t *xi,
-                                         typename Q2T<TI>::t *xo, int tid, int nth)
+// One damped Jacobi sweep on the constrained operator: xo = xi + w D^-1 (b - A xi),
+// xi read through src.
+template <class TI, class XS>
+__device__ __forceinline__ void qt_sweep_src(const QtLevel<TI> &L, TI omega, const XS &src,
+                                             typename Q2T<TI>::t *xo, int tid, int nth)
 {
 	typedef typename Q2T<TI>::t V;
-	const TI *xf = reinterpret_cast<const TI *>(xi);
 	for (int A = tid; A < L.nno; A += nth) {
 		TI y0, y1;
-		qt_kr_node(L, xf, A, y0, y1);
-		const V x = xi[A], b = L.b[A];
+		qt_kr_node_src(L, src, A, y0, y1);
+		const V x = src(A), b = L.b[A];
 		V o;
 		o.x = L.kind[2 * A] == 1 ? x.x + omega * L.invD[2 * A] * (b.x - y0) : TI(0);
 		o.y = L.kind[2 * A + 1] == 1 ? x.y + omega * L.invD[2 * A + 1] * (b.y - y1) : TI(0);
 		xo[A] = o;
 	}
+}
+
+template <class TI>
+__device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const typename Q2T<TI>::t *xi,
+                                         typename Q2T<TI>::t *xo, int tid, int nth)
+{
+	const QtXStored<TI> src{xi};
+	qt_sweep_src(L, omega, src, xo, tid, nth);
 }
 
 // The team running a part of the V-cycle: the whole grid, or block 0 alone
@@ -220,37 +263,51 @@ __device__ __forceinline__ int qt_final(const QtHier<TI> &H, int l)
 }
 
 // Level l on the way down: smoothing from zero, residual, restriction into l-1.
+// The first sweep from zero, x0 = w D^-1 b, is formed where the next pass reads
+// it (the residual, or the second sweep), so it costs no barrier of its own.
 template <class TI>
 __device__ void qt_down(const QtHier<TI> &H, int l, QtTeam &t)
 {
 	typedef typename Q2T<TI>::t V;
 	const QtLevel<TI> &L = H.lv[l];
-	V *x0 = L.x[0];
-	for (int A = t.tid; A < L.nno; A += t.nth) {   // first sweep from zero: w D^-1 b
-		const V b = L.b[A];
-		V o;
-		o.x = H.omega * L.invD[2 * A] * b.x;
-		o.y = H.omega * L.invD[2 * A + 1] * b.y;
-		x0[A] = o;
-	}
-	int cur = 0;
-	t.sync();
-	for (int s = 1; s < H.smooth; s++) {
-		qt_sweep(L, H.omega, L.x[cur], L.x[1 - cur], t.tid, t.nth);
-		cur = 1 - cur;
+	const QtXFirst<TI> first{L.b, L.invD, H.omega};
+	int cur;
+	if (H.smooth == 1) {
+		// x0 stored for the way up, and the residual b - A x0 in the same pass
+		V *x0 = L.x[0];
+		for (int A = t.tid; A < L.nno; A += t.nth) {
+			TI y0, y1;
+			qt_kr_node_src(L, first, A, y0, y1);
+			x0[A] = first(A);
+			const V b = L.b[A];
+			V r;
+			r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
+			r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
+			L.r[A] = r;
+		}
+		cur = 0;
+		t.sync();
+	} else {
+		qt_sweep_src(L, H.omega, first, L.x[1], t.tid, t.nth);   // sweeps 1 and 2
+		cur = 1;
+		t.sync();
+		for (int s = 2; s < H.smooth; s++) {
+			qt_sweep(L, H.omega, L.x[cur], L.x[1 - cur], t.tid, t.nth);
+			cur = 1 - cur;
+			t.sync();
+		}
+		const TI *xf = reinterpret_cast<const TI *>(L.x[cur]);
+		for (int A = t.tid; A < L.nno; A += t.nth) {
+			TI y0, y1;
+			qt_kr_node(L, xf, A, y0, y1);
+			const V b = L.b[A];
+			V r;
+			r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
+			r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
+			L.r[A] = r;
+		}
 		t.sync();
 	}
-	const TI *xf = reinterpret_cast<const TI *>(L.x[cur]);
-	for (int A = t.tid; A < L.nno; A += t.nth) {
-		TI y0, y1;
-		qt_kr_node(L, xf, A, y0, y1);
-		const V b = L.b[A];
-		V r;
-		r.x = L.kind[2 * A] == 1 ? b.x - y0 : TI(0);
-		r.y = L.kind[2 * A + 1] == 1 ? b.y - y1 : TI(0);
-		L.r[A] = r;
-	}
-	t.sync();
 	const QtLevel<TI> &C = H.lv[l - 1];
 	const TI *rf = reinterpret_cast<const TI *>(L.r);
 	TI *cb = reinterpret_cast<TI *>(C.b);
