@@ -315,8 +315,11 @@ int mclg_heat_matvec(mclg_ctx *ctx, int which, const double *x, double *y);   /*
  *                        interpolation, time step and model time kept.
  *                        Refined meshes run the FP64 replica (precision=fp64)
  *                        or the converged refined-mesh solver (mixed, fp64mg).
- * Host-only counterparts for checking the tree and the transfer without a GPU:
- * mclg_mesh_new_leaves, mclg_mesh_amr_leaves, mclg_mesh_transfer. */
+ * Host-only counterparts for checking the tree and the transfers without a GPU:
+ * mclg_mesh_new_leaves, mclg_mesh_amr_leaves, mclg_mesh_transfer (nodal fields,
+ * bilinear) and mclg_mesh_transfer_elem (element fields such as the pressure:
+ * the area mean of the old field over each new element, as a remesh carries
+ * the converged solvers' pressure over). */
 int mclg_create_leaves(mclg_ctx **ctx, const mclg_config *cfg, const int *leaves, size_t n);
 int mclg_amr_flags(mclg_ctx *ctx, double frac, unsigned char *flags, size_t n, double *gmax);
 int mclg_amr_leaves(mclg_ctx *ctx, const unsigned char *flags, size_t n, int base_level, int target_level, int *leaves,
@@ -335,6 +338,8 @@ int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, 
                          int target_level, int *leaves, size_t cap, size_t *n);
 int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_t n_from,
                        const mclg_mesh_handle *to, double *T_to, size_t n_to);
+int mclg_mesh_transfer_elem(const mclg_mesh_handle *from, const double *P_from, size_t n_from,
+                            const mclg_mesh_handle *to, double *P_to, size_t n_to);
 
 /* ---- batched ensembles (no reference counterpart) ------------------------
  * n independent models, each built from its own configuration (converged

@@ -155,6 +155,7 @@ def lib():
         "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
+        "mclg_mesh_transfer_elem": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
         "mclg_ensemble_graph": (C.c_int, [vp]),
@@ -336,6 +337,15 @@ class Mesh:
         T = np.ascontiguousarray(T, np.float64)
         out = np.zeros(to.nno)
         _check(lib().mclg_mesh_transfer(self._h, _dptr(T), T.size, to._h, _dptr(out), out.size), "mesh_transfer")
+        return out
+
+    def transfer_elem(self, P, to):
+        """An element field of this mesh (the pressure) onto `to`'s elements: the
+        area mean of P over each new element."""
+        P = np.ascontiguousarray(P, np.float64)
+        out = np.zeros(to.nel)
+        _check(lib().mclg_mesh_transfer_elem(self._h, _dptr(P), P.size, to._h, _dptr(out), out.size),
+               "mesh_transfer_elem")
         return out
 
     def write_output(self, data_dir, timestep, T, V0, V1, stress, vis):

@@ -2876,46 +2876,6 @@ int mclg_amr_leaves(mclg_ctx *c, const unsigned char *flags, size_t n, int base_
 // lists and the new context's device state (on a stream of its own); end()
 // waits for it, carries the fields over and swaps the new state in.  Between
 // them the caller may go on stepping the old mesh.
-// Element-wise fields (the pressure) between two trees of the same finest
-// level: a new element takes the area mean of the old field over it.  Where
-// the old leaf covering it is as coarse or coarser that is the old value;
-// where the old mesh was finer, the mean of its children (recursively by
-// quadrant), so that a pattern alternating over the children (the Q1-P0
-// pressure's checkerboard modes, null on the old mesh but not on the new one)
-// is not carried into the new element.
-static unsigned pt_compact16(unsigned v)
-{
-	v &= 0x55555555u;
-	v = (v | (v >> 1)) & 0x33333333u;
-	v = (v | (v >> 2)) & 0x0f0f0f0fu;
-	v = (v | (v >> 4)) & 0x00ff00ffu;
-	v = (v | (v >> 8)) & 0x0000ffffu;
-	return v;
-}
-
-static double region_mean(const mclg_level &HO, int F, int ncell, const double *P, int x0, int z0, int s)
-{
-	const int e = HO.cell_elem[(size_t)x0 * ncell + z0];
-	const int so = 1 << (F - (HO.Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1)));
-	if (so >= s)
-		return P[e];
-	const int h = s >> 1;
-	return 0.25 * ((region_mean(HO, F, ncell, P, x0, z0, h) + region_mean(HO, F, ncell, P, x0, z0 + h, h)) +
-	               (region_mean(HO, F, ncell, P, x0 + h, z0, h) + region_mean(HO, F, ncell, P, x0 + h, z0 + h, h)));
-}
-
-static void element_transfer(const mclg_mesh &from, const double *P_old, const mclg_mesh &to, double *P_new)
-{
-	const int F = from.max_level - 1, ncell = from.gnox - 1;
-	const mclg_level &HO = from.lev[F], &HN = to.lev[to.max_level - 1];
-	for (int e = 0; e < HN.nel; e++) {
-		const int lvl = HN.Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
-		const unsigned code = (unsigned)(HN.Mcode[e] >> MCLG_LEVEL_BITS);
-		P_new[e] = region_mean(HO, F, ncell, P_old, (int)pt_compact16(code >> 1), (int)pt_compact16(code),
-		                       1 << (F - lvl));
-	}
-}
-
 struct RemeshJob {
 	std::thread th;
 	mclg_config cfg;
@@ -3041,7 +3001,7 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 		std::vector<double> P_old(ne), P_new(ne2);
 		rc = mclg_get_field(c, MCLG_F_P, -1, P_old.data(), ne);
 		if (rc == MCLG_OK)
-			element_transfer(c->mesh, P_old.data(), n->mesh, P_new.data());
+			rc = mclg_amr_transfer_elem(&c->mesh, P_old.data(), &n->mesh, P_new.data());
 		if (rc == MCLG_OK)
 			rc = mclg_set_field(n, MCLG_F_P, -1, P_new.data(), ne2);
 		// the previous step's solution too, so that the extrapolated warm start
@@ -3062,7 +3022,7 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 						D_new[2 * A + comp] = comp_new[A];
 			}
 			if (rc == MCLG_OK)
-				element_transfer(c->mesh, Ph.data(), n->mesh, Phn.data());
+				rc = mclg_amr_transfer_elem(&c->mesh, Ph.data(), &n->mesh, Phn.data());
 			if (rc == MCLG_OK) {
 				e = cudaMemcpy(n->d_h1, D_new.data(), 2 * nn2 * sizeof(double), cudaMemcpyHostToDevice);
 				if (e == cudaSuccess)

@@ -197,6 +197,51 @@ done:
 	return rc;
 }
 
+/* Mean of an element field of `from` over the square of fine cells (x0, z0, s):
+ * the covering leaf's value where that leaf is at least as large, else the mean
+ * of the four quadrants' means. */
+static double region_mean(const mclg_level *A, int F, int ncell, const double *P, int x0, int z0, int s)
+{
+	const int e = A->cell_elem[(long)x0 * ncell + z0];
+	const int so = 1 << (F - (A->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1)));
+	const int h = s >> 1;
+	if (so >= s)
+		return P[e];
+	return 0.25 * ((region_mean(A, F, ncell, P, x0, z0, h) + region_mean(A, F, ncell, P, x0, z0 + h, h)) +
+	               (region_mean(A, F, ncell, P, x0 + h, z0, h) + region_mean(A, F, ncell, P, x0 + h, z0 + h, h)));
+}
+
+/* P_to per finest-level element of `to`: the area mean of the element field
+ * P_from of `from` over it.  Where the leaf of `from` covering the new element
+ * is as large or larger, that is its value; where `from` was finer, the mean of
+ * its leaves there, so that the integral of P is kept and a pattern alternating
+ * over the children (the Q1-P0 pressure's checkerboard modes) averages out
+ * instead of being sampled into the new element.  Both meshes must share the
+ * finest level and the box. */
+int mclg_amr_transfer_elem(const mclg_mesh *from, const double *P_from, const mclg_mesh *to, double *P_to)
+{
+	const int F = from->max_level - 1;
+	const mclg_level *A = &from->lev[F], *B = &to->lev[to->max_level - 1];
+	const int ncell = from->gnox - 1;
+	int e;
+	if (to->max_level != from->max_level || to->gnox != from->gnox ||
+	    fabs(from->length - to->length) > 1e-12 * from->length ||
+	    fabs(from->height - to->height) > 1e-12 * from->height) {
+		mclg_set_error("element field transfer between meshes of different finest level or box");
+		return MCLG_BAD_INPUT;
+	}
+	if (A->cell_elem == NULL) {
+		mclg_set_error("element field transfer: the source mesh has no cell map");
+		return MCLG_BAD_INPUT;
+	}
+	for (e = 0; e < B->nel; e++) {
+		const int lvl = B->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
+		const unsigned code = (unsigned)(B->Mcode[e] >> MCLG_LEVEL_BITS);
+		P_to[e] = region_mean(A, F, ncell, P_from, (int)compact16(code >> 1), (int)compact16(code), 1 << (F - lvl));
+	}
+	return MCLG_OK;
+}
+
 /* T_to at the finest-level nodes of `to`: the bilinear interpolant of T_from
  * on the finest-level leaf of `from` that contains each node (hanging nodes
  * of `from` hold their parents' mean, so the interpolant is continuous). */

@@ -71,6 +71,7 @@ int mclg_mesh_build_leaves(mclg_mesh *m, const mclg_config *cfg, const int *leav
 int mclg_amr_build_leaves(const mclg_mesh *m, const unsigned char *flags, int base_level, int target_level,
                           int **leaves, long *n);
 int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to);
+int mclg_amr_transfer_elem(const mclg_mesh *from, const double *P_from, const mclg_mesh *to, double *P_to);
 void mclg_mesh_free(mclg_mesh *m);
 /* The reference's multigrid maps and the Gauss-Seidel wavefronts (mclg_refmg.c).
  * interp: lev in (min_level, max_level); n[neq(lev)], src[4*neq(lev)] (src[i*neq + u]).

@@ -246,6 +246,19 @@ int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, 
 	return MCLG_OK;
 }
 
+int mclg_mesh_transfer_elem(const mclg_mesh_handle *from, const double *P_from, size_t n_from,
+                            const mclg_mesh_handle *to, double *P_to, size_t n_to)
+{
+	if (from == NULL || to == NULL || P_from == NULL || P_to == NULL)
+		return MCLG_BAD_INPUT;
+	if (n_from != (size_t)from->mesh.lev[from->mesh.max_level - 1].nel ||
+	    n_to != (size_t)to->mesh.lev[to->mesh.max_level - 1].nel) {
+		mclg_set_error("field buffers do not match the meshes' element counts");
+		return MCLG_BAD_INPUT;
+	}
+	return mclg_amr_transfer_elem(&from->mesh, P_from, &to->mesh, P_to);
+}
+
 int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_t n_from,
                        const mclg_mesh_handle *to, double *T_to, size_t n_to)
 {

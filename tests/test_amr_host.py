@@ -5,7 +5,11 @@
   of the develop_mode meshes against the reference);
 - the refined tree from given flags equals the oracle's, leaf for leaf, and is
   2:1 balanced with the flagged regions at the target level;
-- the bilinear transfer equals the oracle's and is exact for bilinear fields.
+- the bilinear transfer equals the oracle's and is exact for bilinear fields;
+- the element-field (pressure) transfer is the area mean of the old field over
+  each new element: equal to a fine-cell raster mean in numpy, exact where the
+  new mesh refines, conserving the field's integral, averaging a checkerboard
+  over refined children to zero.
 """
 import numpy as np
 import pytest
@@ -98,3 +102,95 @@ def test_bad_leaf_lists_are_rejected():
         Mesh(c, leaves=np.array([0, 16, 8], np.int32))        # not increasing
     with pytest.raises(MclgError):
         Mesh(c, leaves=np.array([0], np.int32))               # too few
+
+
+def _compact16(v):
+    v = v & 0x55555555
+    v = (v | (v >> 1)) & 0x33333333
+    v = (v | (v >> 2)) & 0x0F0F0F0F
+    v = (v | (v >> 4)) & 0x00FF00FF
+    v = (v | (v >> 8)) & 0x0000FFFF
+    return v
+
+
+def _squares(m):
+    """Per finest-level element: fine-cell origin (x0, z0) and side s."""
+    M = m.get("Mcode").astype(np.int64)
+    F = m.max_level - 1
+    code = M >> 4
+    return _compact16(code >> 1), _compact16(code), 1 << (F - (M & 15))
+
+
+def _raster_mean(src, P, dst):
+    """The area mean of src's element field P over each element of dst, by
+    painting P on the finest cells and averaging."""
+    F = src.max_level - 1
+    grid = np.zeros((1 << F, 1 << F))
+    for e, (x, z, s) in enumerate(zip(*_squares(src))):
+        grid[x:x + s, z:z + s] = P[e]
+    return np.array([grid[x:x + s, z:z + s].mean() for x, z, s in zip(*_squares(dst))])
+
+
+def _graded(c, F, base, seed, density):
+    m = Mesh(c, leaves=uniform_leaves(F, base))
+    flg = (np.random.default_rng(seed).random(m.nel) < density).astype(np.uint8)
+    return Mesh(c, leaves=m.amr_leaves(flg, base, F))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_element_transfer_is_the_area_mean(seed):
+    F, base = 6, 2
+    c = cfg(F + 1)
+    a, b = _graded(c, F, base, 10 + seed, 0.1), _graded(c, F, base, 20 + seed, 0.1)
+    P = np.random.default_rng(seed).standard_normal(a.nel)
+    got = a.transfer_elem(P, b)
+    want = _raster_mean(a, P, b)
+    assert np.abs(got - want).max() <= 1e-14 * np.abs(P).max()
+    # the integral of the field is kept
+    ia, ib = (a.get("area") * P).sum(), (b.get("area") * got).sum()
+    assert abs(ia - ib) <= 1e-13 * (a.get("area") * np.abs(P)).sum()
+    # onto the same mesh it is the identity
+    np.testing.assert_array_equal(a.transfer_elem(P, a), P)
+
+
+def test_element_transfer_is_exact_where_the_new_mesh_refines():
+    F, base = 6, 3
+    c = cfg(F + 1)
+    coarse = Mesh(c, leaves=uniform_leaves(F, base))
+    fine = _graded(c, F, base, 3, 0.3)
+    P = np.random.default_rng(3).standard_normal(coarse.nel)
+    got = coarse.transfer_elem(P, fine)
+    # every new element lies in one old element and takes its value, bit for bit
+    xs, zs, ss = _squares(coarse)
+    owner = np.empty((1 << F, 1 << F), np.int64)
+    for e, (x, z, s) in enumerate(zip(xs, zs, ss)):
+        owner[x:x + s, z:z + s] = e
+    x2, z2, _ = _squares(fine)
+    np.testing.assert_array_equal(got, P[owner[x2, z2]])
+
+
+def test_element_transfer_averages_a_checkerboard_away():
+    F, base = 6, 3
+    c = cfg(F + 1)
+    fine = _graded(c, F, base, 4, 0.3)
+    coarse = Mesh(c, leaves=uniform_leaves(F, base))
+    x, z, s = _squares(fine)
+    P = np.where(((x // s) + (z // s)) % 2 == 0, 1.0, -1.0)   # alternating over siblings of one size
+    got = fine.transfer_elem(P, coarse)
+    # the base elements split into children of a single size average to exactly 0
+    split = []
+    for x0, z0, w in zip(*_squares(coarse)):
+        inside = s[(x >= x0) & (x < x0 + w) & (z >= z0) & (z < z0 + w)]
+        split.append(inside.size > 1 and np.unique(inside).size == 1)
+    split = np.array(split)
+    assert split.any()
+    np.testing.assert_array_equal(got[split], 0.0)
+
+
+def test_element_transfer_rejects_mismatched_meshes():
+    c6, c7 = cfg(6), cfg(7)
+    a, b = Mesh(c6, leaves=uniform_leaves(5, 3)), Mesh(c7, leaves=uniform_leaves(6, 3))
+    with pytest.raises(MclgError):
+        a.transfer_elem(np.zeros(a.nel), b)                   # different finest level
+    with pytest.raises(MclgError):
+        a.transfer_elem(np.zeros(a.nel + 1), a)               # wrong field size
