@@ -272,6 +272,112 @@ int mclg_node_index(const mclg_level *L, int gid)
 
 #define ALLOC(p, n) do { (p) = calloc((size_t)(n) + 1, sizeof(*(p))); if ((p) == NULL) goto oom; } while (0)
 
+/* fn(ctx, i0, i1) over [0, n) in chunks of at least `grain` items, one thread
+ * per chunk (at most 8); each chunk writes only its own items, so the result
+ * does not depend on the split. */
+typedef struct {
+	void (*fn)(void *, long, long);
+	void *ctx;
+	long i0, i1;
+} pf_job;
+
+static void *pf_run(void *p)
+{
+	pf_job *j = (pf_job *)p;
+	j->fn(j->ctx, j->i0, j->i1);
+	return NULL;
+}
+
+static void parallel_for(long n, long grain, void (*fn)(void *, long, long), void *ctx)
+{
+	enum { kMaxT = 8 };
+	pf_job jobs[kMaxT];
+	pthread_t th[kMaxT];
+	int started[kMaxT], nt = (int)(n / (grain > 0 ? grain : 1)), i;
+	nt = nt < 1 ? 1 : nt > kMaxT ? kMaxT : nt;
+	for (i = 0; i < nt; i++) {
+		jobs[i].fn = fn;
+		jobs[i].ctx = ctx;
+		jobs[i].i0 = n * i / nt;
+		jobs[i].i1 = n * (i + 1) / nt;
+		started[i] = i < nt - 1 && pthread_create(&th[i], NULL, pf_run, &jobs[i]) == 0;
+		if (!started[i])
+			pf_run(&jobs[i]);
+	}
+	for (i = 0; i < nt; i++)
+		if (started[i])
+			pthread_join(th[i], NULL);
+}
+
+/* a node's neighbours: the distinct nodes of the elements touching it, sorted */
+typedef struct {
+	const mclg_level *L;
+	int *lists;   /* [16*nno] */
+} nb_ctx;
+
+static void nb_lists(void *p, long a0, long a1)
+{
+	nb_ctx *x = (nb_ctx *)p;
+	const mclg_level *L = x->L;
+	const long nn = L->nno, ne = L->nel;
+	for (long A = a0; A < a1; A++) {
+		int *nb = x->lists + 16 * A, cnt = 0;
+		for (int s = 0; s < L->p2n_cnt[A]; s++) {
+			const int el = L->p2n_el[(long)s * nn + A];
+			for (int j = 0; j < 4; j++)
+				nb[cnt++] = L->ienl[(long)j * ne + el];
+		}
+		L->nb_cnt[A] = (int)sort_unique(nb, cnt);
+	}
+}
+
+typedef struct {
+	const mclg_level *L;
+	const int *lists;
+	int w;
+	int *nb;
+} nb_fill_ctx;
+
+static void nb_fill(void *p, long a0, long a1)
+{
+	nb_fill_ctx *x = (nb_fill_ctx *)p;
+	const long nn = x->L->nno;
+	for (long A = a0; A < a1; A++)
+		for (int j = 0; j < x->w; j++)
+			x->nb[(long)j * nn + A] = j < x->L->nb_cnt[A] ? x->lists[16 * A + j] : (int)A;
+}
+
+/* the slot of corner b in the neighbour list of corner a, per element */
+typedef struct {
+	mclg_level *L;
+	int bad;
+} kslot_ctx;
+
+static void kslot_fill(void *p, long e0, long e1)
+{
+	kslot_ctx *x = (kslot_ctx *)p;
+	mclg_level *L = x->L;
+	const long nn = L->nno, ne = L->nel;
+	for (long e = e0; e < e1; e++)
+		for (int a = 0; a < 4; a++) {
+			const int An = L->ienl[(long)a * ne + e];
+			for (int b = 0; b < 4; b++) {
+				const int Bn = L->ienl[(long)b * ne + e];
+				int slot = -1;
+				for (int j = 0; j < L->nb_cnt[An]; j++)
+					if (L->nb[(long)j * nn + An] == Bn) {
+						slot = j;
+						break;
+					}
+				if (slot < 0) {
+					x->bad = 1;
+					slot = 0;
+				}
+				L->kslot[(long)(a * 4 + b) * ne + e] = (unsigned char)slot;
+			}
+		}
+}
+
 static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 {
 	mclg_level *L = &m->lev[lev];
@@ -474,59 +580,47 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 			free(is_h);
 		}
 	}
-	/* sorted neighbour lists and element slot map (for the node-block operator) */
+	/* sorted neighbour lists and element slot map (for the node-block operator),
+	 * node and element loops in chunks on threads */
 	{
-		int nb[4 * 4], cnt, w = 0;
+		int w = 0;
+		nb_ctx nc;
+		nb_fill_ctx fc;
+		kslot_ctx kc;
 		ALLOC(L->nb_cnt, nn);
-		for (A = 0; A < nn; A++) {
-			int s, j;
-			cnt = 0;
-			for (s = 0; s < L->p2n_cnt[A]; s++) {
-				int el = L->p2n_el[(long)s * nn + A];
-				for (j = 0; j < 4; j++)
-					nb[cnt++] = L->ienl[(long)j * ne + el];
-			}
-			cnt = (int)sort_unique(nb, cnt);
-			L->nb_cnt[A] = cnt;
-			if (cnt > w)
-				w = cnt;
-		}
+		nc.L = L;
+		nc.lists = (int *)malloc((size_t)16 * nn * sizeof(int));
+		if (nc.lists == NULL)
+			goto oom;
+		parallel_for(nn, 16384, nb_lists, &nc);
+		for (A = 0; A < nn; A++)
+			if (L->nb_cnt[A] > w)
+				w = L->nb_cnt[A];
 		if (w > MCLG_NB_MAX) {
+			free(nc.lists);
 			mclg_set_error("a node has %d neighbours (max %d)", w, MCLG_NB_MAX);
 			return MCLG_BAD_INPUT;
 		}
 		L->nbw = w;
-		ALLOC(L->nb, (long)w * nn);
-		for (A = 0; A < nn; A++) {
-			int s, j;
-			cnt = 0;
-			for (s = 0; s < L->p2n_cnt[A]; s++) {
-				int el = L->p2n_el[(long)s * nn + A];
-				for (j = 0; j < 4; j++)
-					nb[cnt++] = L->ienl[(long)j * ne + el];
-			}
-			cnt = (int)sort_unique(nb, cnt);
-			for (j = 0; j < w; j++)
-				L->nb[(long)j * nn + A] = j < cnt ? nb[j] : A;
+		L->nb = (int *)calloc((size_t)w * nn + 1, sizeof(int));
+		if (L->nb == NULL) {
+			free(nc.lists);
+			goto oom;
 		}
+		fc.L = L;
+		fc.lists = nc.lists;
+		fc.w = w;
+		fc.nb = L->nb;
+		parallel_for(nn, 16384, nb_fill, &fc);
+		free(nc.lists);
 		ALLOC(L->kslot, 16L * ne);
-		for (e = 0; e < ne; e++)
-			for (a = 0; a < 4; a++) {
-				int An = L->ienl[(long)a * ne + e], b;
-				for (b = 0; b < 4; b++) {
-					int Bn = L->ienl[(long)b * ne + e], j, slot = -1;
-					for (j = 0; j < L->nb_cnt[An]; j++)
-						if (L->nb[(long)j * nn + An] == Bn) {
-							slot = j;
-							break;
-						}
-					if (slot < 0) {
-						mclg_set_error("internal: neighbour slot not found");
-						return MCLG_BAD_INPUT;
-					}
-					L->kslot[(long)(a * 4 + b) * ne + e] = (unsigned char)slot;
-				}
-			}
+		kc.L = L;
+		kc.bad = 0;
+		parallel_for(ne, 16384, kslot_fill, &kc);
+		if (kc.bad) {
+			mclg_set_error("internal: neighbour slot not found");
+			return MCLG_BAD_INPUT;
+		}
 	}
 	/* fine cell -> covering element (the horizontal average and the field
 	 * transfers of the finest level; coarser levels do not need it) */
