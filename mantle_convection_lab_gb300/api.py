@@ -65,7 +65,7 @@ class Config(C.Structure):
         ("max_refine", C.c_int), ("max_outer", C.c_int), ("max_inner", C.c_int),
         ("mg_eta_avg", C.c_int), ("mg_block_n", C.c_int), ("guess_smooth", C.c_int),
         ("stokes_method", C.c_int), ("mg_cycle", C.c_int), ("mg_finest_iteration", C.c_int),
-        ("mg_coarse_iteration", C.c_int),
+        ("mg_coarse_iteration", C.c_int), ("lowest_vis", C.c_double), ("highest_vis", C.c_double),
     ]
 
     @classmethod

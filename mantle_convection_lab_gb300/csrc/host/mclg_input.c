@@ -220,6 +220,8 @@ void mclg_config_defaults(mclg_config *c)
 	c->mg_cycle = 2;
 	c->mg_finest_iteration = 4;
 	c->mg_coarse_iteration = 4;
+	c->lowest_vis = 1.0;
+	c->highest_vis = 1.0;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -316,6 +318,8 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_int(&pl, "mg_cycle", &c->mg_cycle, 2);
 	get_int(&pl, "mg_finest_iteration", &c->mg_finest_iteration, 4);
 	get_int(&pl, "mg_coarse_iteration", &c->mg_coarse_iteration, 4);
+	get_double(&pl, "lowest_vis", &c->lowest_vis, 1.0);
+	get_double(&pl, "highest_vis", &c->highest_vis, 1.0);
 	free(pl.e);
 	return MCLG_OK;
 }

@@ -56,6 +56,10 @@ typedef struct orc {
 	double *HKval, *HCval, *HAval, *HF, *tau0, *tau1, *hd;
 	double dt, model_time, res_m, res_c;
 	int p_init, uzawa_cycles, cg_cycles, heat_cycles;
+	/* grain-size rheology (grain_damage=1): the reference's static first-call flag
+	 * and clock, the nodal grain size, and the clip of the viscosity it sets */
+	int grain, gs_init;
+	double gs_t, gs_lo, gs_hi, *gs;
 	struct orc_mg *mg;   /* solver="mg": the coarser levels and the transfer maps */
 } orc;
 
@@ -207,6 +211,92 @@ static void viscosity(orc *o)
 			v = fmin(fmax(v, o->vmin), o->vmax);
 		o->vis[i] = v;
 	}
+}
+
+/* ---- grain-size rheology (Grain_size_evolution.c:3-152), one level ---------
+ * Called after viscosity() when grain_damage=1.  The reference keeps a static
+ * first-call flag and a static clock t (seconds) shared by every call:
+ *   - the first call sets the grain size r = 1e-3 everywhere and returns;
+ *   - every later call scales the nodal stress to Pa, then, while t is behind
+ *     the model time in seconds, takes one explicit 100-year step over the
+ *     nodes: those deeper than 200 km get stress 0 and keep their viscosity;
+ *     the others update r by growth minus damage at the absolute temperature
+ *     T*2500 + 273.5 + 0.3 K/km * depth and get the composite viscosity of
+ *     dislocation and diffusion creep at their stress and new r, scaled by the
+ *     reference viscosity and clipped to [lowest_vis, highest_vis].
+ * On a single-level mesh the level visited is the finest one, so this is
+ * exactly the reference's result.  Every expression keeps the reference's
+ * operand order (the library is built without contraction). */
+static double gs_creep_A(double A0, double Edisp, double T) { return A0 * exp(0.0 - Edisp / (8.3145 * T)); }
+static double gs_creep_B(double B0, double Ediff, double T, double m)
+{
+	return pow(M_PI * 0.5, 0.0 - m) * B0 * exp(0.0 - Ediff / (8.3145 * T));
+}
+static double gs_growth(double G0, double EG, double T) { return G0 * exp(0.0 - EG / (8.3145 * T)); }
+static double gs_damage_fraction(double f1, double f2, double T_M, double T_W, double T, double k)
+{
+	const double x = (pow(T_M, k) - pow(T, k)) / (pow(T_M, k) - pow(T_W, k));
+	return f1 * pow(f2 / f1, x);
+}
+
+static void grain_size(orc *o)
+{
+	const double mu = 0.72, gamma = 1.0, q = 4.0, p = 2.0, T_M = 1500.0, T_W = 285.0, Tref = 2500.0;
+	const double f1 = 1e-12, f2 = 1e-2, k = 2, n = 3.0, m = 3.0;
+	const double A0 = 1.1e5 / pow(1e6, n), Edisp = 530.0 * 1e3;
+	const double B0 = 13.6 * pow(1e-6, m) / 1e6, Ediff = 300 * 1e3;
+	const double G0 = 2e4 * pow(1e-6, p), EG = 300 * 1e3;
+	const double alpha = 1e-5, kappa = 1e-6, D = 2890e3, rho = 3300.0, g = 9.8, y2s = 3.1536e7;
+	const double vis_ref = (rho * g * alpha * Tref * D * D * D) / (o->Ra * kappa);
+	const double stress_scale = (vis_ref * kappa) / (D * D), time_scale = D * D / kappa;
+	const double dt = 1e2 * y2s;
+	int i;
+	if (!o->gs_init) {
+		for (i = 0; i < o->nno; i++)
+			o->gs[i] = 1e-3;
+		o->gs_init = 1;
+		return;
+	}
+	for (i = 0; i < o->nno; i++)
+		o->stress[i] *= stress_scale;
+	while (o->gs_t < o->model_time * time_scale) {
+		for (i = 0; i < o->nno; i++) {
+			const double z = o->X[o->nno + i];
+			double T, r, A, B, tau, GG, GI, fI, ratio, rF, psi, dr, v;
+			if (2890 * (1.0 - z) > 200.0) {
+				o->stress[i] = 0.0;
+				continue;
+			}
+			T = o->T[i] * Tref + 273.5 + 2890.0 * (1.0 - z) * 0.3;
+			r = o->gs[i];
+			A = gs_creep_A(A0, Edisp, T);
+			B = gs_creep_B(B0, Ediff, T, m);
+			tau = o->stress[i];
+			GG = gs_growth(G0, EG, T);
+			GI = q / p * pow(1e-6, q - p) * GG / 250.0;
+			fI = gs_damage_fraction(f1, f2, T_M, T_W, T, k);
+			ratio = B / (A * pow(tau, n - 1));
+			rF = pow(ratio, 1.0 / m);
+			psi = 2 * A * pow(tau, n + 1) * (1.0 + pow(rF / r, m));
+			dr = mu * GI / (q * pow(r, q - 1)) - fI * r * r * psi / (gamma * mu);
+			o->gs[i] += dr * dt;
+			v = 0.5 * tau / (A * pow(tau, n) + B * tau / pow(o->gs[i], m));
+			v /= vis_ref;
+			if (v < o->gs_lo)
+				v = o->gs_lo;
+			if (v > o->gs_hi)
+				v = o->gs_hi;
+			o->vis[i] = v;
+		}
+		o->gs_t += dt;
+	}
+}
+
+static void viscosity_step(orc *o)
+{
+	viscosity(o);
+	if (o->grain)
+		grain_size(o);
 }
 
 /* ---- Stokes assembly (Build_matrix.c) -------------------------------------- */
@@ -1058,9 +1148,11 @@ orc *orc_new(int nel, int nno, int gnox, int gnoz, int fine_level, const int *ie
 	o->Ra = dparam[0]; o->A = dparam[1]; o->refT = dparam[2]; o->lmj = dparam[3]; o->Q = dparam[4];
 	o->theta = dparam[5]; o->accuracy = dparam[6]; o->citcom_accu = dparam[7]; o->vmin = dparam[8];
 	o->vmax = dparam[9];
+	o->gs_lo = dparam[10]; o->gs_hi = dparam[11];
 	o->max_citcom = iparam[0]; o->max_cg = iparam[1]; o->precond = iparam[2]; o->check_v_only = iparam[3];
 	o->solver = iparam[4]; o->zero_P = iparam[5]; o->AMR = iparam[6]; o->auto_acc = iparam[7];
 	o->threads = iparam[8] > 0 ? iparam[8] : 1;
+	o->grain = iparam[9];
 	shape_tables(o);
 	o->dxh = malloc(sizeof(double) * nel); o->dzh = malloc(sizeof(double) * nel);
 	o->jac = malloc(sizeof(double) * nel); o->area = malloc(sizeof(double) * nel);
@@ -1089,6 +1181,7 @@ orc *orc_new(int nel, int nno, int gnox, int gnoz, int fine_level, const int *ie
 		}
 	o->T = calloc(nno, sizeof(double)); o->vis = calloc(nno, sizeof(double)); o->buoy = calloc(nno, sizeof(double));
 	o->V0 = calloc(nno, sizeof(double)); o->V1 = calloc(nno, sizeof(double)); o->stress = calloc(nno, sizeof(double));
+	o->gs = calloc(nno, sizeof(double));
 	o->d = calloc(o->neq + 1, sizeof(double)); o->p = calloc(nel, sizeof(double));
 	o->F = calloc(o->neq + 1, sizeof(double)); o->Kdiag = calloc(o->neq + 1, sizeof(double));
 	o->Kncol = calloc(o->neq + 1, sizeof(int)); o->Gncol = calloc(o->neq + 1, sizeof(int));
@@ -1116,6 +1209,7 @@ void orc_free(orc *o)
 	}
 	free(o->dxh); free(o->dzh); free(o->jac); free(o->area); free(o->id); free(o->hid); free(o->p2n_cnt);
 	free(o->p2n_el); free(o->T); free(o->vis); free(o->buoy); free(o->V0); free(o->V1); free(o->stress);
+	free(o->gs);
 	free(o->d); free(o->p); free(o->F); free(o->Kdiag); free(o->Kncol); free(o->Gncol); free(o->Kcol);
 	free(o->Gcol); free(o->Kval); free(o->Gval); free(o->HKncol); free(o->HCncol); free(o->HKcol);
 	free(o->HCcol); free(o->HKval); free(o->HCval); free(o->HAval); free(o->HF); free(o->hd); free(o->tau0); free(o->tau1);
@@ -1172,7 +1266,7 @@ static void assemble_coarse(orc *o)
 void orc_step(orc *o, double *stats)
 {
 	buoyancy_force(o);
-	viscosity(o);
+	viscosity_step(o);
 	assemble_stokes(o);
 	assemble_coarse(o);
 	solve_velocity_pressure(o);
@@ -1185,7 +1279,7 @@ void orc_step(orc *o, double *stats)
 void orc_stokes(orc *o, double *stats)
 {
 	buoyancy_force(o);
-	viscosity(o);
+	viscosity_step(o);
 	assemble_stokes(o);
 	assemble_coarse(o);
 	solve_velocity_pressure(o);
@@ -1195,12 +1289,13 @@ void orc_stokes(orc *o, double *stats)
 void orc_assemble(orc *o)
 {
 	buoyancy_force(o);
-	viscosity(o);
+	viscosity_step(o);
 	assemble_stokes(o);
 	assemble_coarse(o);
 }
 
-/* which: 0 T, 1 V0, 2 V1, 3 P, 4 d, 5 stress, 6 vis, 7 buoyancy, 8 F, 9 Kdiag, 10 tau0, 11 tau1, 12 heat F */
+/* which: 0 T, 1 V0, 2 V1, 3 P, 4 d, 5 stress, 6 vis, 7 buoyancy, 8 F, 9 Kdiag, 10 tau0, 11 tau1, 12 heat F,
+ * 13 grain size */
 int orc_get(const orc *o, int which, double *out)
 {
 	switch (which) {
@@ -1217,6 +1312,7 @@ int orc_get(const orc *o, int which, double *out)
 	case 10: memcpy(out, o->tau0, sizeof(double) * o->nel); return o->nel;
 	case 11: memcpy(out, o->tau1, sizeof(double) * o->nel); return o->nel;
 	case 12: memcpy(out, o->HF, sizeof(double) * o->hneq); return o->hneq;
+	case 13: memcpy(out, o->gs, sizeof(double) * o->nno); return o->nno;
 	default: return -1;
 	}
 }

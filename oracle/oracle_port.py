@@ -21,7 +21,7 @@ from build_oracle import LIB, build  # noqa: E402
 
 _L = None
 GET = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoyancy": 7, "F": 8, "Kdiag": 9,
-       "tau0": 10, "tau1": 11, "heat_F": 12}
+       "tau0": 10, "tau1": 11, "heat_F": 12, "gs": 13}
 
 
 def lib():
@@ -104,10 +104,13 @@ class Oracle:
         dx = np.array([L / (1 << l) for l in range(16)]); k(dx)
         dz = np.array([H / (1 << l) for l in range(16)]); k(dz)
         dpar = np.array([cfg.Rayleigh, cfg.A, cfg.refT, cfg.lower_mantle_jump, cfg.Q, cfg.theta, cfg.accuracy,
-                         cfg.citcom_solver_accu, cfg.vis_min, cfg.vis_max]); k(dpar)
+                         cfg.citcom_solver_accu, cfg.vis_min, cfg.vis_max, cfg.lowest_vis, cfg.highest_vis]); k(dpar)
+        # grain_damage: the reference evolves the grain size on the first level it visits
+        # (mg_min_level); only on a single-level mesh is that the finest one
+        grain = int(cfg.grain_damage == 1 and lev == m.max_level - 1 and cfg.mg_min_level == lev)
         ipar = np.array([cfg.max_citcom_cycle, cfg.max_cg_cycle, cfg.cg_precondition, cfg.check_v_only,
-                         SOLVERS.get(bytes(cfg.solver), 0), cfg.zero_P, cfg.AMR, cfg.auto_accuracy, threads],
-                        np.int32); k(ipar)
+                         SOLVERS.get(bytes(cfg.solver), 0), cfg.zero_P, cfg.AMR, cfg.auto_accuracy, threads,
+                         grain], np.int32); k(ipar)
         hp = [hang[i] if nh else np.zeros(1, np.int32) for i in range(3)]
         self._keep.extend(hp)
         if lev == m.max_level - 1:

@@ -239,6 +239,8 @@ void output()
 	rec_f8(fp, "vis", G.vis[lev], G.nno[lev]);
 	rec_f8(fp, "buoyancy", G.buoyancy[lev], G.nno[lev]);
 	rec_f8(fp, "F", G.F[lev], G.neq[lev]);
+	if (G.control.grain_damage == 1 && G.gs != NULL && G.gs[lev] != NULL)
+		rec_f8(fp, "gs", G.gs[lev], G.nno[lev]);   /* grain size (Grain_size_evolution.c:64-110) */
 	stokes_residual(res);
 	rec_f8(fp, "residual", res, 3);
 	fclose(fp);

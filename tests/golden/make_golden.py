@@ -113,6 +113,16 @@ CASES = {
     "vc_l6": ("level=6\nmg_min_level=3\nmax_timestep=2\ndevelop_mode=0\nRayleigh=1e6\n"
               "A=11.512925464970229\nic_kind=2\nic_seed=2024\nic_noise=0.0\nic_bl_thickness=0.02\n"
               "ic_modes=8\nic_mode_amp=0.005\n", None, True),
+    # grain-size rheology (grain_damage=1) on a single-level mesh, where the
+    # reference's routine is deterministic (the first level visited evolves; it is
+    # the only one): cold top (the grain size stays at 1e-3, the clip sets the
+    # viscosity near the top) and a warmer top boundary
+    "gd_l5": ("level=5\nmg_min_level=4\nmax_timestep=3\ndevelop_mode=0\nRayleigh=1e5\nA=0.0\n"
+              "ic_kind=1\nic_seed=42\nic_noise=1e-4\nT_mantle_perturb=0.01\nT_wave_number=1\n"
+              "grain_damage=1\nlowest_vis=1e-3\nhighest_vis=1e3\n", None, True),
+    "gdw_l5": ("level=5\nmg_min_level=4\nmax_timestep=2\ndevelop_mode=0\nRayleigh=1e5\nA=2.0\n"
+               "ic_kind=1\nic_seed=42\nic_noise=1e-4\nT_mantle_perturb=0.01\nT_wave_number=1\n"
+               "top_T_bc_val=0.5\ngrain_damage=1\nlowest_vis=1e-3\nhighest_vis=1e3\n", None, True),
 }
 
 

@@ -64,3 +64,26 @@ def test_capped_dev14_iterate_is_ill_conditioned():
     o.close()
     assert e["V0"] > 3e-5 and e["V1"] > 3e-5 and e["P"] > 3e-4, e
     assert max(e.values()) < 2e-3, e
+
+
+@pytest.mark.parametrize("case,steps", [("gd_l5", 2), ("gdw_l5", 2)])
+def test_oracle_grain_size(case, steps):
+    """Grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-152) on a
+    single-level mesh: the grain size, the viscosity it sets (clipped to
+    [lowest_vis, highest_vis]) and the fields of the steps built on it equal the
+    reference's.  gd_l5 has a cold top (the grain size stays at 1e-3, the clip
+    sets the viscosity within 200 km of the top); gdw_l5 a warmer top, where
+    the grain size evolves."""
+    g = golden(case)
+    o = oracle_port.Oracle(golden_input(case))
+    for s in range(steps):
+        st = o.step()
+        assert st["uzawa_cycles"] == g["series/uzawa_cycles"][s]
+        for name, key in (("gs", "gs"), ("vis", "vis"), ("V0", "V0"), ("V1", "V1"), ("P", "p"), ("d", "d"),
+                          ("stress", "stress")):
+            assert rel(o.get(name), g[f"step{s:04d}/{key}"]) < TOL, (s, name)
+        assert rel(o.get("T"), g[f"heat{s:04d}/T"]) < TOL
+    if case == "gdw_l5":   # the grain size did evolve, and the clip is active at both ends
+        assert g[f"step{steps - 1:04d}/gs"].min() < 1e-3
+        v = g[f"step{steps - 1:04d}/vis"]
+        assert v.min() == 1e-3 and v.max() == 1e3
