@@ -259,9 +259,15 @@ enum {
 	MCLG_M_PROJECT = 11, /* [neq]      lev < finest: the equation of lev+1 whose residual
 	                                   equation l of lev takes (G.project[lev].local_u), -1 none
 	                                   Connection.c:1051-1250 */
-	MCLG_M_GS_WAVE = 12  /* [nno]      Gauss-Seidel wavefront of each node: nodes of one
+	MCLG_M_GS_WAVE = 12, /* [nno]      Gauss-Seidel wavefront of each node: nodes of one
 	                                   wavefront share no matrix entry, and sweeping the
 	                                   wavefronts in order reproduces the sequential sweep */
+	/* the node-block operator's structure: */
+	MCLG_M_NB = 13,      /* [25*nno]   node A's matrix neighbours (the distinct nodes of the
+	                                   elements touching it, level-local indices, ascending)
+	                                   in out[25A ..], -1 after the last */
+	MCLG_M_KSLOT = 14    /* [16*nel]   slot of corner b in corner a's neighbour list,
+	                                   out[(4a+b)*nel + e] */
 };
 /* lev < 0 selects the finest level.  n is the caller's buffer length; the
  * call fails with MCLG_BAD_INPUT when it does not match the array size. */

@@ -28,7 +28,8 @@ OK, CAP_REACHED, NAN, BREAKDOWN, BAD_INPUT, CUDA_ERROR, IO_ERROR, NO_DEVICE = ra
 FIELDS = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoyancy": 7, "F": 8,
           "Kdiag": 9, "BAB": 10, "tau0": 11, "tau1": 12, "heat_F": 13, "X0": 14, "X1": 15}
 MESH = {"sizes": 0, "Mcode": 1, "node": 2, "ien": 3, "id": 4, "heat_id": 5, "lm": 6, "hang": 7,
-        "v_bc": 8, "T_bc": 9, "interp": 10, "project": 11, "gs_wave": 12}
+        "v_bc": 8, "T_bc": 9, "interp": 10, "project": 11, "gs_wave": 12, "nb": 13, "kslot": 14}
+NB_WIDTH = 25   # the width of the "nb" lists
 MESH_REAL = {"X": 0, "jacobi": 1, "area": 2, "v_bc_val": 3, "T_bc_val": 4}
 OUT_TEXT, OUT_BINARY = 1, 2
 
@@ -304,7 +305,8 @@ class Mesh:
         nel, nno, neq, hneq, nh = (int(v) for v in s[:5])
         return {"Mcode": nel, "node": nno, "ien": 4 * nel, "id": 2 * nno, "heat_id": nno, "lm": 8 * nel,
                 "hang": 3 * nh, "v_bc": 2 * nno, "T_bc": nno, "X": 2 * nno, "jacobi": nel, "area": nel,
-                "v_bc_val": 2 * nno, "T_bc_val": nno, "interp": 5 * neq, "project": neq, "gs_wave": nno}[which]
+                "v_bc_val": 2 * nno, "T_bc_val": nno, "interp": 5 * neq, "project": neq, "gs_wave": nno,
+                "nb": NB_WIDTH * nno, "kslot": 16 * nel}[which]
 
     def get(self, which, lev=-1):
         n = self._size(which, lev)

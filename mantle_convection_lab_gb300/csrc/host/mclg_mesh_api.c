@@ -86,6 +86,8 @@ int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t 
 	case MCLG_M_INTERP: need = 5 * (size_t)L->neq; break;
 	case MCLG_M_PROJECT: need = (size_t)L->neq; break;
 	case MCLG_M_GS_WAVE: need = nn; break;
+	case MCLG_M_NB: need = (size_t)MCLG_NB_MAX * nn; break;
+	case MCLG_M_KSLOT: need = 16 * ne; break;
 	default:
 		mclg_set_error("unknown mesh array %d", which);
 		return MCLG_BAD_INPUT;
@@ -141,6 +143,15 @@ int mclg_host_mesh_get(const mclg_mesh *m, int which, int lev, int *out, size_t 
 		break;
 	}
 	case MCLG_M_GS_WAVE: mclg_refmg_waves(L, out); break;
+	case MCLG_M_NB:
+		for (i = 0; i < nn; i++)
+			for (size_t j = 0; j < MCLG_NB_MAX; j++)
+				out[i * MCLG_NB_MAX + j] = (int)j < L->nb_cnt[i] ? L->nb[j * nn + i] : -1;
+		break;
+	case MCLG_M_KSLOT:
+		for (i = 0; i < 16 * ne; i++)
+			out[i] = L->kslot[i];
+		break;
 	}
 	return MCLG_OK;
 }
