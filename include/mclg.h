@@ -350,6 +350,22 @@ int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_
                        const mclg_mesh_handle *to, double *T_to, size_t n_to);
 int mclg_mesh_transfer_elem(const mclg_mesh_handle *from, const double *P_from, size_t n_from,
                             const mclg_mesh_handle *to, double *P_to, size_t n_to);
+/* The refined-mesh solver's host lists of one level (lev < 0: the finest), as
+ * the converged solvers upload them, for checking without a GPU.  Built on
+ * the first call for every level from mg_min_level up.  Dofs are 2*node + c.
+ *   SIZES  int[4]       nno, width of C^T K C's node-block rows, contributions,
+ *                       expansion entries
+ *   KIND   int[2*nno]   0 fixed, 1 reduced, 2 constrained (hanging)
+ *   RC_OFF int[nno+1], RC_TGT int[n], RC_SRC int[n], RC_W double[n]: row A of
+ *          C^T K C gets, for i in RC_OFF[A] .. RC_OFF[A+1]-1, entry
+ *          (slot RC_TGT>>2, component pair RC_TGT&3) += RC_W * K[RC_SRC], K the
+ *          node-block operator as flat doubles: K[((k*nno + A)*4 + 2c + c')]
+ *          couples (A,c) with (the k-th neighbour of A, c')
+ *   RNB    int[width*nno] the row's reduced column nodes, slot-major
+ *   RCNT   int[nno]       columns per row */
+enum { MCLG_QT_SIZES = 0, MCLG_QT_KIND = 1, MCLG_QT_RC_OFF = 2, MCLG_QT_RC_TGT = 3, MCLG_QT_RC_SRC = 4,
+       MCLG_QT_RC_W = 5, MCLG_QT_RNB = 6, MCLG_QT_RCNT = 7 };
+int mclg_mesh_qt_get(mclg_mesh_handle *h, int lev, int which, void *out, size_t n);
 
 /* ---- batched ensembles (no reference counterpart) ------------------------
  * n independent models, each built from its own configuration (converged

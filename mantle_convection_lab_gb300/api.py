@@ -157,6 +157,7 @@ def lib():
         "mclg_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_mesh_transfer_elem": (C.c_int, [vp, dp, sz, vp, dp, sz]),
+        "mclg_mesh_qt_get": (C.c_int, [vp, C.c_int, C.c_int, vp, sz]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
         "mclg_ensemble_graph": (C.c_int, [vp]),
@@ -340,6 +341,19 @@ class Mesh:
         out = np.zeros(to.nno)
         _check(lib().mclg_mesh_transfer(self._h, _dptr(T), T.size, to._h, _dptr(out), out.size), "mesh_transfer")
         return out
+
+    def qt(self, lev=-1):
+        """The refined-mesh solver's host lists of one level (mclg_mesh_qt_get):
+        kind, and the contribution lists that assemble C^T K C."""
+        def fetch(which, n, dtype):
+            out = np.zeros(n, dtype)
+            _check(lib().mclg_mesh_qt_get(self._h, lev, which, out.ctypes.data_as(C.c_void_p), n), "mesh_qt_get")
+            return out
+        nno, width, n_rc, n_ex = (int(v) for v in fetch(0, 4, np.int32))
+        return {"nno": nno, "width": width, "kind": fetch(1, 2 * nno, np.int32),
+                "rc_off": fetch(2, nno + 1, np.int32), "rc_tgt": fetch(3, n_rc, np.int32),
+                "rc_src": fetch(4, n_rc, np.int32), "rc_w": fetch(5, n_rc, np.float64),
+                "rnb": fetch(6, width * nno, np.int32), "rcnt": fetch(7, nno, np.int32)}
 
     def transfer_elem(self, P, to):
         """An element field of this mesh (the pressure) onto `to`'s elements: the

@@ -9,6 +9,8 @@
 struct mclg_mesh_handle {
 	mclg_mesh mesh;
 	mclg_config cfg;
+	mclg_qt_level qt[MCLG_MAX_LEVEL];   /* the refined-mesh solver's lists, built on first use */
+	int qt_lo, qt_n;
 };
 
 static int mesh_new(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, long n)
@@ -48,8 +50,81 @@ void mclg_mesh_delete(mclg_mesh_handle *h)
 {
 	if (h == NULL)
 		return;
+	for (int k = 0; k < h->qt_n; k++)
+		mclg_qt_free(&h->qt[k]);
 	mclg_mesh_free(&h->mesh);
 	free(h);
+}
+
+int mclg_mesh_qt_get(mclg_mesh_handle *h, int lev, int which, void *out, size_t n)
+{
+	const mclg_qt_level *q;
+	size_t need;
+	int top, k;
+	if (h == NULL || out == NULL)
+		return MCLG_BAD_INPUT;
+	top = h->mesh.max_level - 1;
+	if (h->qt_n == 0) {
+		const int lo = h->mesh.min_level;
+		int rc;
+		if (lo >= top) {
+			mclg_set_error("the refined-mesh lists need at least two levels (levels %d..%d)", lo, top);
+			return MCLG_BAD_INPUT;
+		}
+		rc = mclg_qt_build(&h->mesh, lo, h->qt);
+		if (rc != MCLG_OK) {
+			for (k = 0; k <= top - lo; k++)
+				mclg_qt_free(&h->qt[k]);
+			return rc;
+		}
+		h->qt_lo = lo;
+		h->qt_n = top - lo + 1;
+	}
+	if (lev < 0)
+		lev = top;
+	if (lev < h->qt_lo || lev > top) {
+		mclg_set_error("level %d has no refined-mesh lists (levels %d..%d)", lev, h->qt_lo, top);
+		return MCLG_BAD_INPUT;
+	}
+	q = &h->qt[lev - h->qt_lo];
+	switch (which) {
+	case MCLG_QT_SIZES: need = 4; break;
+	case MCLG_QT_KIND: need = 2 * (size_t)q->nno; break;
+	case MCLG_QT_RC_OFF: need = (size_t)q->nno + 1; break;
+	case MCLG_QT_RC_TGT:
+	case MCLG_QT_RC_SRC:
+	case MCLG_QT_RC_W: need = (size_t)q->n_rc; break;
+	case MCLG_QT_RNB: need = (size_t)q->rnbw * q->nno; break;
+	case MCLG_QT_RCNT: need = (size_t)q->nno; break;
+	default:
+		mclg_set_error("unknown refined-mesh list %d", which);
+		return MCLG_BAD_INPUT;
+	}
+	if (n != need) {
+		mclg_set_error("refined-mesh list %d has %zu entries, buffer has %zu", which, need, n);
+		return MCLG_BAD_INPUT;
+	}
+	switch (which) {
+	case MCLG_QT_SIZES: {
+		int *o = (int *)out;
+		o[0] = q->nno; o[1] = q->rnbw; o[2] = q->n_rc; o[3] = q->n_ex;
+		break;
+	}
+	case MCLG_QT_KIND:
+		for (size_t i = 0; i < need; i++)
+			((int *)out)[i] = q->kind[i];
+		break;
+	case MCLG_QT_RC_OFF: memcpy(out, q->rc_off, need * sizeof(int)); break;
+	case MCLG_QT_RC_TGT: memcpy(out, q->rc_tgt, need * sizeof(int)); break;
+	case MCLG_QT_RC_SRC: memcpy(out, q->rc_src, need * sizeof(int)); break;
+	case MCLG_QT_RC_W: memcpy(out, q->rc_w, need * sizeof(double)); break;
+	case MCLG_QT_RNB: memcpy(out, q->rnb, need * sizeof(int)); break;
+	case MCLG_QT_RCNT:
+		for (size_t i = 0; i < need; i++)
+			((int *)out)[i] = q->rcnt[i];
+		break;
+	}
+	return MCLG_OK;
 }
 
 static const mclg_level *pick_level(const mclg_mesh *m, int lev)
