@@ -576,6 +576,9 @@ static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
 	q->n_rc = (int)tot;
 	rc = MCLG_OK;
 out:
+	if (rc != MCLG_OK)
+		mclg_set_error("refined-mesh operator of a %d-node level: a row with more than 255 reduced "
+		               "columns, or out of host memory", nno);
 	free(cnt);
 	return rc;
 }
