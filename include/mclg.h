@@ -363,6 +363,23 @@ int mclg_mesh_transfer_elem(const mclg_mesh_handle *from, const double *P_from, 
  *          couples (A,c) with (the k-th neighbour of A, c')
  *   RNB    int[width*nno] the row's reduced column nodes, slot-major
  *   RCNT   int[nno]       columns per row */
+/* Grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-152), host work:
+ * one call per time step after the exponential viscosity, on the level the
+ * reference evolves (a single-level mesh's only level).  The state holds the
+ * routine's first-call flag, its clock and the nodal grain size.  The first
+ * call sets the grain size to 1e-3; later calls scale `stress` (nodal,
+ * nondimensional) to Pa in place and, while the clock is behind model_time,
+ * take the reference's 100-year steps per node within 200 km of the top,
+ * setting `vis` there (clipped to [lowest_vis, highest_vis]) and the stress of
+ * the deeper nodes to 0.  X: [2*nno] node coordinates (x then z). */
+typedef struct mclg_grain_state mclg_grain_state;
+int mclg_grain_new(mclg_grain_state **g);
+int mclg_grain_update(mclg_grain_state *g, int nno, const double *X, const double *T, double *stress,
+                      double *vis, double model_time, double Ra, double lowest_vis, double highest_vis,
+                      int threads);
+int mclg_grain_get(const mclg_grain_state *g, double *grain_size, size_t n);
+void mclg_grain_delete(mclg_grain_state *g);
+
 enum { MCLG_QT_SIZES = 0, MCLG_QT_KIND = 1, MCLG_QT_RC_OFF = 2, MCLG_QT_RC_TGT = 3, MCLG_QT_RC_SRC = 4,
        MCLG_QT_RC_W = 5, MCLG_QT_RNB = 6, MCLG_QT_RCNT = 7 };
 int mclg_mesh_qt_get(mclg_mesh_handle *h, int lev, int which, void *out, size_t n);

@@ -7,4 +7,4 @@ The product is libmclg.so (C ABI, include/mclg.h) and the mclg_run driver;
 this package holds their sources (csrc/), the in-tree build (_build.py) and a
 ctypes binding (api.py).
 """
-from .api import Cnn, Config, Ensemble, Mesh, Model, MclgError, StepStats, lib  # noqa: F401
+from .api import Cnn, Config, Ensemble, GrainSize, Mesh, Model, MclgError, StepStats, lib  # noqa: F401

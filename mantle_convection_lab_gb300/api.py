@@ -158,6 +158,11 @@ def lib():
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_mesh_transfer_elem": (C.c_int, [vp, dp, sz, vp, dp, sz]),
         "mclg_mesh_qt_get": (C.c_int, [vp, C.c_int, C.c_int, vp, sz]),
+        "mclg_grain_new": (C.c_int, [C.POINTER(vp)]),
+        "mclg_grain_update": (C.c_int, [vp, C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_int]),
+        "mclg_grain_get": (C.c_int, [vp, dp, sz]),
+        "mclg_grain_delete": (None, [vp]),
         "mclg_ensemble_create": (C.c_int, [C.POINTER(vp), vp, C.c_int]), "mclg_ensemble_destroy": (None, [vp]),
         "mclg_ensemble_create_amr": (C.c_int, [C.POINTER(vp), vp, ip, C.c_int]),
         "mclg_ensemble_graph": (C.c_int, [vp]),
@@ -273,6 +278,40 @@ class Cnn:
 
 def _uptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_ubyte))
+
+
+class GrainSize:
+    """Grain-size rheology (grain_damage=1) on the host: the reference's routine
+    with its first-call flag, clock and nodal grain size (mclg_grain_*)."""
+
+    def __init__(self):
+        self._g = C.c_void_p()
+        _check(lib().mclg_grain_new(C.byref(self._g)), "grain_new")
+        self.nno = None
+
+    def update(self, X, T, stress, vis, model_time, Ra, lowest_vis, highest_vis, threads=4):
+        """One call of the routine; returns the (stress, vis) it leaves."""
+        X = np.ascontiguousarray(X, np.float64)
+        T = np.ascontiguousarray(T, np.float64)
+        stress = np.array(stress, np.float64)
+        vis = np.array(vis, np.float64)
+        self.nno = T.size
+        _check(lib().mclg_grain_update(self._g, T.size, _dptr(X), _dptr(T), _dptr(stress), _dptr(vis), model_time,
+                                       Ra, lowest_vis, highest_vis, threads), "grain_update")
+        return stress, vis
+
+    def grain_size(self):
+        out = np.zeros(self.nno)
+        _check(lib().mclg_grain_get(self._g, _dptr(out), out.size), "grain_get")
+        return out
+
+    def close(self):
+        if self._g:
+            lib().mclg_grain_delete(self._g)
+            self._g = C.c_void_p()
+
+    def __del__(self):
+        self.close()
 
 
 class Mesh:
