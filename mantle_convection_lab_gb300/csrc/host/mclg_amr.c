@@ -217,13 +217,30 @@ static double region_mean(const mclg_level *A, int F, int ncell, const double *P
  * its leaves there, so that the integral of P is kept and a pattern alternating
  * over the children (the Q1-P0 pressure's checkerboard modes) averages out
  * instead of being sampled into the new element.  Both meshes must share the
- * finest level and the box. */
+ * finest level and the box.  Elements in chunks on threads. */
+typedef struct {
+	const mclg_level *A, *B;
+	const double *P_from;
+	double *P_to;
+	int F, ncell;
+} elem_tr;
+
+static void elem_tr_run(void *p, long e0, long e1)
+{
+	const elem_tr *t = (const elem_tr *)p;
+	for (long e = e0; e < e1; e++) {
+		const int lvl = t->B->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
+		const unsigned code = (unsigned)(t->B->Mcode[e] >> MCLG_LEVEL_BITS);
+		t->P_to[e] = region_mean(t->A, t->F, t->ncell, t->P_from, (int)compact16(code >> 1), (int)compact16(code),
+		                         1 << (t->F - lvl));
+	}
+}
+
 int mclg_amr_transfer_elem(const mclg_mesh *from, const double *P_from, const mclg_mesh *to, double *P_to)
 {
 	const int F = from->max_level - 1;
 	const mclg_level *A = &from->lev[F], *B = &to->lev[to->max_level - 1];
-	const int ncell = from->gnox - 1;
-	int e;
+	elem_tr t;
 	if (to->max_level != from->max_level || to->gnox != from->gnox ||
 	    fabs(from->length - to->length) > 1e-12 * from->length ||
 	    fabs(from->height - to->height) > 1e-12 * from->height) {
@@ -234,32 +251,36 @@ int mclg_amr_transfer_elem(const mclg_mesh *from, const double *P_from, const mc
 		mclg_set_error("element field transfer: the source mesh has no cell map");
 		return MCLG_BAD_INPUT;
 	}
-	for (e = 0; e < B->nel; e++) {
-		const int lvl = B->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
-		const unsigned code = (unsigned)(B->Mcode[e] >> MCLG_LEVEL_BITS);
-		P_to[e] = region_mean(A, F, ncell, P_from, (int)compact16(code >> 1), (int)compact16(code), 1 << (F - lvl));
-	}
+	t.A = A;
+	t.B = B;
+	t.P_from = P_from;
+	t.P_to = P_to;
+	t.F = F;
+	t.ncell = from->gnox - 1;
+	mclg_parallel_for(B->nel, 16384, elem_tr_run, &t);
 	return MCLG_OK;
 }
 
 /* T_to at the finest-level nodes of `to`: the bilinear interpolant of T_from
  * on the finest-level leaf of `from` that contains each node (hanging nodes
- * of `from` hold their parents' mean, so the interpolant is continuous). */
-int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to)
+ * of `from` hold their parents' mean, so the interpolant is continuous).
+ * Nodes in chunks on threads. */
+typedef struct {
+	const mclg_level *A, *B;
+	const double *T_from;
+	double *T_to;
+	int ncell;
+	double dxc, dzc;
+} node_tr;
+
+static void node_tr_run(void *p, long i0, long i1)
 {
-	const int F = from->max_level - 1, G = to->max_level - 1;
-	const mclg_level *A = &from->lev[F], *B = &to->lev[G];
-	const int ncell = from->gnox - 1;
-	const double dxc = from->length / ncell, dzc = from->height / ncell;
-	int i;
-	if (fabs(from->length - to->length) > 1e-12 * from->length ||
-	    fabs(from->height - to->height) > 1e-12 * from->height) {
-		mclg_set_error("field transfer between boxes of different size");
-		return MCLG_BAD_INPUT;
-	}
-	for (i = 0; i < B->nno; i++) {
+	const node_tr *t = (const node_tr *)p;
+	const mclg_level *A = t->A, *B = t->B;
+	const int ncell = t->ncell;
+	for (long i = i0; i < i1; i++) {
 		const double x = B->X[i], z = B->X[B->nno + i];
-		int cx = (int)(x / dxc), cz = (int)(z / dzc), e;
+		int cx = (int)(x / t->dxc), cz = (int)(z / t->dzc), e;
 		double x0, z0, w, h, xi, ze;
 		int n0, n1, n2, n3;
 		cx = cx < 0 ? 0 : cx >= ncell ? ncell - 1 : cx;
@@ -275,7 +296,27 @@ int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_me
 		h = A->X[A->nno + n1] - z0;
 		xi = (x - x0) / w;
 		ze = (z - z0) / h;
-		T_to[i] = (1 - xi) * ((1 - ze) * T_from[n0] + ze * T_from[n1]) + xi * (ze * T_from[n2] + (1 - ze) * T_from[n3]);
+		t->T_to[i] = (1 - xi) * ((1 - ze) * t->T_from[n0] + ze * t->T_from[n1]) +
+		             xi * (ze * t->T_from[n2] + (1 - ze) * t->T_from[n3]);
 	}
+}
+
+int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to)
+{
+	const int F = from->max_level - 1, G = to->max_level - 1;
+	node_tr t;
+	if (fabs(from->length - to->length) > 1e-12 * from->length ||
+	    fabs(from->height - to->height) > 1e-12 * from->height) {
+		mclg_set_error("field transfer between boxes of different size");
+		return MCLG_BAD_INPUT;
+	}
+	t.A = &from->lev[F];
+	t.B = &to->lev[G];
+	t.T_from = T_from;
+	t.T_to = T_to;
+	t.ncell = from->gnox - 1;
+	t.dxc = from->length / t.ncell;
+	t.dzc = from->height / t.ncell;
+	mclg_parallel_for(t.B->nno, 16384, node_tr_run, &t);
 	return MCLG_OK;
 }

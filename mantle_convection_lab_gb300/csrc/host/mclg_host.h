@@ -72,6 +72,9 @@ int mclg_amr_build_leaves(const mclg_mesh *m, const unsigned char *flags, int ba
                           int **leaves, long *n);
 int mclg_amr_transfer(const mclg_mesh *from, const double *T_from, const mclg_mesh *to, double *T_to);
 int mclg_amr_transfer_elem(const mclg_mesh *from, const double *P_from, const mclg_mesh *to, double *P_to);
+/* fn(ctx, i0, i1) over [0, n) in chunks of at least `grain` items on up to 8
+ * threads; for loops whose items write only their own results */
+void mclg_parallel_for(long n, long grain, void (*fn)(void *, long, long), void *ctx);
 void mclg_mesh_free(mclg_mesh *m);
 /* The reference's multigrid maps and the Gauss-Seidel wavefronts (mclg_refmg.c).
  * interp: lev in (min_level, max_level); n[neq(lev)], src[4*neq(lev)] (src[i*neq + u]).

@@ -288,7 +288,7 @@ static void *pf_run(void *p)
 	return NULL;
 }
 
-static void parallel_for(long n, long grain, void (*fn)(void *, long, long), void *ctx)
+void mclg_parallel_for(long n, long grain, void (*fn)(void *, long, long), void *ctx)
 {
 	enum { kMaxT = 8 };
 	pf_job jobs[kMaxT];
@@ -592,7 +592,7 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 		nc.lists = (int *)malloc((size_t)16 * nn * sizeof(int));
 		if (nc.lists == NULL)
 			goto oom;
-		parallel_for(nn, 16384, nb_lists, &nc);
+		mclg_parallel_for(nn, 16384, nb_lists, &nc);
 		for (A = 0; A < nn; A++)
 			if (L->nb_cnt[A] > w)
 				w = L->nb_cnt[A];
@@ -611,12 +611,12 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 		fc.lists = nc.lists;
 		fc.w = w;
 		fc.nb = L->nb;
-		parallel_for(nn, 16384, nb_fill, &fc);
+		mclg_parallel_for(nn, 16384, nb_fill, &fc);
 		free(nc.lists);
 		ALLOC(L->kslot, 16L * ne);
 		kc.L = L;
 		kc.bad = 0;
-		parallel_for(ne, 16384, kslot_fill, &kc);
+		mclg_parallel_for(ne, 16384, kslot_fill, &kc);
 		if (kc.bad) {
 			mclg_set_error("internal: neighbour slot not found");
 			return MCLG_BAD_INPUT;

@@ -194,3 +194,21 @@ def test_element_transfer_rejects_mismatched_meshes():
         a.transfer_elem(np.zeros(a.nel), b)                   # different finest level
     with pytest.raises(MclgError):
         a.transfer_elem(np.zeros(a.nel + 1), a)               # wrong field size
+
+
+def test_transfers_on_meshes_split_across_threads():
+    """Both transfers on meshes of over 100 000 nodes and elements (built in
+    chunks on threads): bilinear fields move exactly, element fields by their area
+    mean."""
+    F, base = 9, 6
+    c = cfg(F + 1)
+    a, b = _graded(c, F, base, 31, 0.3), _graded(c, F, base, 32, 0.3)
+    assert min(a.nno, b.nno, a.nel, b.nel) > 2 * 16384
+    X = a.get("X").reshape(2, -1)
+    T = 0.3 + 0.7 * X[0] - 1.1 * X[1] + 0.5 * X[0] * X[1]
+    Y = b.get("X").reshape(2, -1)
+    want = 0.3 + 0.7 * Y[0] - 1.1 * Y[1] + 0.5 * Y[0] * Y[1]
+    assert np.abs(a.transfer(T, b) - want).max() < 1e-13
+    P = np.random.default_rng(7).standard_normal(a.nel)
+    got = a.transfer_elem(P, b)
+    assert np.abs(got - _raster_mean(a, P, b)).max() <= 1e-14 * np.abs(P).max()
