@@ -239,7 +239,8 @@ enum {
 	MCLG_F_TAU1 = 12,    /* [nel] SUPG tau_z                      G.heat[lev].tau[1] */
 	MCLG_F_HEAT_F = 13,  /* [heat neq] heat right-hand side       G.heat[lev].F     */
 	MCLG_F_X0 = 14,      /* [nno] node x                          G.X[lev][0]       */
-	MCLG_F_X1 = 15       /* [nno] node z                          G.X[lev][1]       */
+	MCLG_F_X1 = 15,      /* [nno] node z                          G.X[lev][1]       */
+	MCLG_F_GRAIN = 16    /* [nno] grain size (grain_damage=1; get only)  G.gs[lev]      */
 };
 enum {
 	MCLG_M_SIZES = 0,    /* [8]: nel, nno, neq, heat_neq, nh, gnox, gnoz, max_level */

@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(_PKG, "libmclg.so")
 OK, CAP_REACHED, NAN, BREAKDOWN, BAD_INPUT, CUDA_ERROR, IO_ERROR, NO_DEVICE = range(8)
 
 FIELDS = {"T": 0, "V0": 1, "V1": 2, "P": 3, "d": 4, "stress": 5, "vis": 6, "buoyancy": 7, "F": 8,
-          "Kdiag": 9, "BAB": 10, "tau0": 11, "tau1": 12, "heat_F": 13, "X0": 14, "X1": 15}
+          "Kdiag": 9, "BAB": 10, "tau0": 11, "tau1": 12, "heat_F": 13, "X0": 14, "X1": 15, "gs": 16}
 MESH = {"sizes": 0, "Mcode": 1, "node": 2, "ien": 3, "id": 4, "heat_id": 5, "lm": 6, "hang": 7,
         "v_bc": 8, "T_bc": 9, "interp": 10, "project": 11, "gs_wave": 12, "nb": 13, "kslot": 14}
 NB_WIDTH = 25   # the width of the "nb" lists
@@ -531,7 +531,7 @@ class Model:
         return {"T": self.nno, "V0": self.nno, "V1": self.nno, "P": self.nel, "d": self.neq,
                 "stress": self.nno, "vis": self.nno, "buoyancy": self.nno, "F": self.neq, "Kdiag": self.neq,
                 "BAB": self.nel, "tau0": self.nel, "tau1": self.nel, "heat_F": self.heat_neq,
-                "X0": self.nno, "X1": self.nno}[which]
+                "X0": self.nno, "X1": self.nno, "gs": self.nno}[which]
 
     def get(self, which, lev=-1):
         """A field of the finest level; with solver="mg", T and vis of a coarser level `lev` too."""

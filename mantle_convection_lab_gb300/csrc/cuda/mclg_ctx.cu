@@ -135,6 +135,7 @@ struct mclg_ctx {
 	QtArgs<double> qtd;
 	OutWriter *writer;            // asynchronous output, created on first use
 	struct RemeshJob *rj;         // a remesh begun and not yet finished
+	mclg_grain_state *grain;      // grain_damage=1: the grain-size routine's state (host)
 };
 
 static int cuda_fail(cudaError_t e, const char *what)
@@ -1215,8 +1216,18 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	if (out == NULL || cfg == NULL)
 		return MCLG_BAD_INPUT;
 	*out = NULL;
-	if (cfg->lg_mul != 0 || cfg->grain_damage != 0) {
-		mclg_set_error("lg_mul and grain_damage paths are not part of this engine (set both to 0)");
+	if (cfg->lg_mul != 0) {
+		mclg_set_error("the lg_mul path is not part of this engine (set lg_mul=0)");
+		return MCLG_BAD_INPUT;
+	}
+	// grain-size rheology: the reference evolves the grain size on the first level its
+	// viscosity() visits (mg_min_level); only on a single-level mesh is that the level
+	// solved, and only the FP64 replica runs the reference's iteration on it
+	if (cfg->grain_damage != 0 &&
+	    (cfg->grain_damage != 1 || cfg->mg_min_level != cfg->level - 1 || cfg->precision != 0 ||
+	     (strcmp(cfg->solver, "cg") != 0 && strcmp(cfg->solver, "jc") != 0))) {
+		mclg_set_error("grain_damage=1 needs a single-level mesh (mg_min_level = level-1), precision=fp64 and "
+		               "solver \"cg\" or \"jc\"");
 		return MCLG_BAD_INPUT;
 	}
 	const bool ref_solver = strcmp(cfg->solver, "gs") == 0 || strcmp(cfg->solver, "mg") == 0;
@@ -1328,6 +1339,12 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 	CKD(dalloc(&c->tmpA, 2 * nn + ne));
 	CKD(dalloc(&c->tmpB, 2 * nn + ne));
 	CKD(cudaMallocHost((void **)&c->sc_host, sizeof(StepScalars)));
+	if (cfg->grain_damage == 1 && mclg_grain_new(&c->grain) != MCLG_OK) {
+		mclg_set_error("grain size: out of host memory");
+		mclg_destroy(c);
+		*out = NULL;
+		return MCLG_BAD_INPUT;
+	}
 	CKD(cudaMemsetAsync(c->sc, 0, sizeof(StepScalars), c->st));
 	CKD(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
 	CKD(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
@@ -1405,6 +1422,7 @@ void mclg_destroy(mclg_ctx *c)
 	if (c == NULL)
 		return;
 	writer_free(c->writer);   // pending outputs are written first
+	mclg_grain_delete(c->grain);
 	remesh_job_free(c);
 	if (c->st)
 		cudaStreamSynchronize(c->st);
@@ -1480,11 +1498,39 @@ int mclg_buoyancy_force(mclg_ctx *c)
 	return launch_buoy_vis(c);
 }
 
+// grain_damage=1, after the exponential viscosity (Viscosity.c:19-20): the
+// grain-size routine on the host (mclg_grain.c) with this step's temperature,
+// the last step's nodal stress and the model time; it leaves the viscosity of
+// the nodes it integrates and the stress it scaled.
+static int grain_step(mclg_ctx *c)
+{
+	if (c->grain == NULL)
+		return MCLG_OK;
+	const size_t nn = (size_t)c->L.nno;
+	std::vector<double> T(nn), stress(nn), vis(nn);
+	double mt = 0.0;
+	CK(cudaMemcpyAsync(T.data(), c->T, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(stress.data(), c->stress, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(vis.data(), c->vis, nn * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaMemcpyAsync(&mt, &c->sc->model_time, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	const mclg_config &f = c->cfg;
+	const int rc = mclg_grain_update(c->grain, (int)nn, c->mesh.lev[c->fl].X, T.data(), stress.data(), vis.data(),
+	                                 mt, f.Rayleigh, f.lowest_vis, f.highest_vis, 8);
+	if (rc)
+		return rc;
+	CK(cudaMemcpyAsync(c->vis, vis.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaMemcpyAsync(c->stress, stress.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->st));
+	CK(cudaStreamSynchronize(c->st));
+	return MCLG_OK;
+}
+
 int mclg_viscosity(mclg_ctx *c)
 {
 	if (c == NULL)
 		return MCLG_BAD_INPUT;
-	return launch_buoy_vis(c);
+	const int rc = launch_buoy_vis(c);
+	return rc ? rc : grain_step(c);
 }
 
 int mclg_velocity_pressure_KGF_matrix(mclg_ctx *c)
@@ -1723,7 +1769,7 @@ int mclg_step(mclg_ctx *c, int write_output, mclg_step_stats *st)
 	const long long l0 = c->launches;
 	int rc;
 	CK(cudaEventRecord(c->ev[0], c->st));
-	if ((rc = launch_buoy_vis(c)))
+	if ((rc = launch_buoy_vis(c)) || (rc = grain_step(c)))
 		return rc;
 	if ((rc = mclg_velocity_pressure_KGF_matrix(c)))
 		return rc;
@@ -1833,6 +1879,13 @@ int mclg_get_field(mclg_ctx *c, int which, int lev, double *out, size_t n)
 {
 	if (c == NULL || out == NULL)
 		return MCLG_BAD_INPUT;
+	if (which == MCLG_F_GRAIN) {   // host state of the grain-size routine
+		if (c->grain == NULL || (lev >= 0 && lev != c->fl)) {
+			mclg_set_error("no grain size: grain_damage=1 keeps it for the finest level only");
+			return MCLG_BAD_INPUT;
+		}
+		return mclg_grain_get(c->grain, out, n);
+	}
 	int k;
 	if (coarse_level(c, lev, &k) && (which == MCLG_F_T || which == MCLG_F_VIS)) {   // a coarser level's T, vis
 		const size_t need = (size_t)c->mesh.lev[lev].nno;
@@ -2923,6 +2976,10 @@ int mclg_amr_remesh_begin(mclg_ctx *c, double frac, int base_level, int target_l
 		mclg_set_error("a remesh is already pending: finish it with mclg_amr_remesh_end");
 		return MCLG_BAD_INPUT;
 	}
+	if (c->grain != NULL) {
+		mclg_set_error("grain_damage=1 runs on a fixed single-level mesh: no remeshing");
+		return MCLG_BAD_INPUT;
+	}
 	if (!(frac >= 0.0))
 		return MCLG_BAD_INPUT;
 	// flags and the new tree on the device
@@ -3129,6 +3186,10 @@ extern "C" int mclg_checkpoint_save(mclg_ctx *c, const char *path)
 {
 	if (c == NULL || path == NULL)
 		return MCLG_BAD_INPUT;
+	if (c->grain != NULL) {
+		mclg_set_error("the grain-size state (grain_damage=1) is not part of a checkpoint");
+		return MCLG_BAD_INPUT;
+	}
 	const mclg_level &H = c->mesh.lev[c->fl];
 	CkpHeader hd;
 	memset(&hd, 0, sizeof hd);

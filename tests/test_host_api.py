@@ -64,6 +64,7 @@ def test_defaults_follow_input_c(tmp_path):
     assert (c.cg_precondition, c.accuracy, c.citcom_solver_accu) == (0, 0.001, 0.001)
     assert (c.develop_mode, c.max_citcom_cycle, c.max_cg_cycle, c.zero_P) == (1, 375, 200, 1)
     assert c.precision == 0 and c.warm_start == 0
+    assert (c.grain_damage, c.lowest_vis, c.highest_vis) == (0, 1.0, 1.0)     # Input.c:58-59, 95
 
 
 def test_getpar_tokenisation(tmp_path):
@@ -157,6 +158,27 @@ def test_create_rejects_unsupported_options(tmp_path):
         h = C.c_void_p()
         assert L.mclg_create(C.byref(h), C.byref(c)) == api.BAD_INPUT
         assert needle in L.mclg_last_error()
+
+
+def test_grain_damage_is_accepted_only_where_the_reference_defines_it(tmp_path):
+    """grain_damage=1 runs on a single-level mesh with the FP64 replica and solver cg or
+    jc (the reference evolves only the first level its viscosity() visits); elsewhere
+    it is rejected before any device work.  The accepted case gets as far as the
+    device check."""
+    L = api.lib()
+    base = open(golden_input("gd_l5")).read()
+    for extra in ("mg_min_level=3\n", 'solver="gs"\n', "precision=\"mixed\"\n", "grain_damage=2\n"):
+        c = Config.from_input(write(tmp_path, base + extra))
+        h = C.c_void_p()
+        assert L.mclg_create(C.byref(h), C.byref(c)) == api.BAD_INPUT, extra
+        assert b"grain_damage" in L.mclg_last_error()
+    c = Config.from_input(golden_input("gd_l5"))
+    h = C.c_void_p()
+    rc = L.mclg_create(C.byref(h), C.byref(c))
+    if rc == api.OK:
+        L.mclg_destroy(h)
+        pytest.skip("a CUDA device is visible")
+    assert rc == api.NO_DEVICE, L.mclg_last_error()
 
 
 @pytest.mark.parametrize("step", [0, 1, 2, 3])
