@@ -2,7 +2,7 @@
 
 Single operators (assembled K, F, G, G^T, BAB, heat K and C) must agree to
 1e-12 relative L2; the Stokes solution, stress and temperature after each
-time step to 1e-8 relative L2 (the benchmark spec's bar for velocity, pressure and
+time step to 1e-8 relative L2 (the parity bar for velocity, pressure and
 temperature), with the Uzawa iteration count within one of the reference's.
 """
 import os
