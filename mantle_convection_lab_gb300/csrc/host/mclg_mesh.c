@@ -378,28 +378,135 @@ static void kslot_fill(void *p, long e0, long e1)
 		}
 }
 
+/* the per-element and per-node loops of a level that write only their own item */
+typedef struct {
+	const mclg_mesh *m;
+	const mclg_config *c;
+	mclg_level *L;
+	int lev, fl, gnox, gnoz;
+} lvl_ctx;
+
+static void ien_range(void *p, long e0, long e1)   /* Construct_ien_id_lm.c:3-41 */
+{
+	const lvl_ctx *x = (const lvl_ctx *)p;
+	mclg_level *L = x->L;
+	const long ne = L->nel;
+	for (long e = e0; e < e1; e++) {
+		int level = L->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
+		int loc = L->Mcode[e] >> MCLG_LEVEL_BITS, xx, z, step, node;
+		demorton(loc, &xx, &z);
+		node = z + xx * x->gnoz;
+		step = 1 << (x->fl - level);
+		L->elev[e] = level;
+		L->ien[0L * ne + e] = node;
+		L->ien[1L * ne + e] = node + step;
+		L->ien[2L * ne + e] = node + step + step * x->gnoz;
+		L->ien[3L * ne + e] = node + step * x->gnoz;
+	}
+}
+
+static void ienl_range(void *p, long k0, long k1)
+{
+	mclg_level *L = ((const lvl_ctx *)p)->L;
+	for (long k = k0; k < k1; k++)
+		L->ienl[k] = mclg_node_index(L, L->ien[k]);
+}
+
+/* coordinates (Mesh.c:430-452) and BC codes (Boundary_condition.c:10-110) */
+static void node_range(void *p, long a0, long a1)
+{
+	const lvl_ctx *x = (const lvl_ctx *)p;
+	const mclg_config *c = x->c;
+	mclg_level *L = x->L;
+	const long nn = L->nno;
+	const int gnoz = x->gnoz, gnox = x->gnox;
+	for (long A = a0; A < a1; A++) {
+		const int n = L->node[A], ix = n / gnoz, iz = n - ix * gnoz;
+		L->X[A] = ix * x->m->dx[x->fl];
+		L->X[nn + A] = iz * x->m->dz[x->fl];
+		L->T_bc[A] = 'N';
+		L->T_bc_val[A] = 0.0;
+		if ((n + 1) % gnoz == 0) {
+			L->T_bc[A] = c->top_T_bc;
+			L->T_bc_val[A] = c->top_T_bc_val;
+		} else if (n % gnoz == 0) {
+			L->T_bc[A] = c->bot_T_bc;
+			L->T_bc_val[A] = c->bot_T_bc_val;
+		} else if (n < gnoz) {
+			if (L->T_bc[A] != 'T')
+				L->T_bc[A] = c->lef_T_bc;
+			L->T_bc_val[A] = c->lef_T_bc_val;
+		} else if (n > (gnox - 1) * gnoz - 1) {
+			if (L->T_bc[A] != 'T')
+				L->T_bc[A] = c->rig_T_bc;
+			L->T_bc_val[A] = c->rig_T_bc_val;
+		}
+		for (int d = 0; d < 2; d++) {
+			char *bc = &L->v_bc[d * nn + A];
+			double *bv = &L->v_bc_val[d * nn + A];
+			*bc = 'N';
+			*bv = 0.0;
+			if ((n + 1) % gnoz == 0) {
+				*bc = c->top_v_bc[d];
+				*bv = c->top_v_bc_val[d];
+			} else if (n % gnoz == 0) {
+				*bc = c->bot_v_bc[d];
+				*bv = c->bot_v_bc_val[d];
+			}
+			if (n < gnoz) {
+				if (*bc != 'V')
+					*bc = c->lef_v_bc[d];
+				*bv = c->lef_v_bc_val[d];
+			} else if (n > (gnox - 1) * gnoz - 1) {
+				if (*bc != 'V')
+					*bc = c->rig_v_bc[d];
+				*bv = c->rig_v_bc_val[d];
+			}
+		}
+	}
+}
+
+/* element geometry (Shape_function.c:123-167, Construct_ien_id_lm.c:198-218) */
+static void geom_range(void *p, long e0, long e1)
+{
+	const lvl_ctx *x = (const lvl_ctx *)p;
+	mclg_level *L = x->L;
+	const long ne = L->nel, nn = L->nno;
+	for (long e = e0; e < e1; e++) {
+		int n0 = L->ienl[e], n2 = L->ienl[2L * ne + e];
+		L->dx_dxi[e] = 0.5 * x->m->dx[L->elev[e]];
+		L->dz_deta[e] = 0.5 * x->m->dz[L->elev[e]];
+		L->jacobi[e] = L->dx_dxi[e] * L->dz_deta[e] - 0.0 * 0.0;
+		L->area[e] = (L->X[n2] - L->X[n0]) * (L->X[nn + n2] - L->X[nn + n0]);
+	}
+}
+
+/* fine cell -> covering element (elements cover disjoint cells) */
+static void cell_range(void *p, long e0, long e1)
+{
+	const lvl_ctx *x = (const lvl_ctx *)p;
+	mclg_level *L = x->L;
+	const long ncz = x->gnoz - 1;
+	for (long e = e0; e < e1; e++) {
+		int n0 = L->ien[e], ix0 = n0 / x->gnoz, iz0 = n0 - ix0 * x->gnoz, s = 1 << (x->fl - L->elev[e]), i, j;
+		for (i = 0; i < s; i++)
+			for (j = 0; j < s; j++)
+				L->cell_elem[(long)(ix0 + i) * ncz + iz0 + j] = (int)e;
+	}
+}
+
 static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 {
 	mclg_level *L = &m->lev[lev];
 	int ne = L->nel, e, a, A, d, gnoz = m->gnoz, gnox = m->gnox, fl = m->max_level - 1;
 	long k, nn;
 	ivec nodes = {0};
+	lvl_ctx lc = {m, c, L, lev, fl, gnox, gnoz};
 
 	/* ien (Construct_ien_id_lm.c:3-41) */
 	ALLOC(L->ien, 4L * ne);
 	ALLOC(L->elev, ne);
-	for (e = 0; e < ne; e++) {
-		int level = L->Mcode[e] & ((1 << MCLG_LEVEL_BITS) - 1);
-		int loc = L->Mcode[e] >> MCLG_LEVEL_BITS, x, z, step, node;
-		demorton(loc, &x, &z);
-		node = z + x * gnoz;
-		step = 1 << (fl - level);
-		L->elev[e] = level;
-		L->ien[0L * ne + e] = node;
-		L->ien[1L * ne + e] = node + step;
-		L->ien[2L * ne + e] = node + step + step * gnoz;
-		L->ien[3L * ne + e] = node + step * gnoz;
-	}
+	mclg_parallel_for(ne, 16384, ien_range, &lc);
 	/* node list (Construct_ien_id_lm.c:43-66): the sorted distinct ids of ien.
 	 * Grids of up to 4M node ids keep a direct id -> index table, which also
 	 * serves node_index; larger ones sort and binary-search. */
@@ -432,67 +539,16 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 	L->nno = (int)nn;
 	L->node = nodes.a;
 	ALLOC(L->ienl, 4L * ne);
-	for (k = 0; k < 4L * ne; k++)
-		L->ienl[k] = mclg_node_index(L, L->ien[k]);
+	mclg_parallel_for(4L * ne, 65536, ienl_range, &lc);
 
-	/* coordinates (Mesh.c:430-452) */
+	/* coordinates (Mesh.c:430-452), temperature and velocity BC codes
+	 * (Boundary_condition.c:10-110) */
 	ALLOC(L->X, 2 * nn);
-	for (A = 0; A < nn; A++) {
-		int ix = L->node[A] / gnoz, iz = L->node[A] - ix * gnoz;
-		L->X[A] = ix * m->dx[fl];
-		L->X[nn + A] = iz * m->dz[fl];
-	}
-
-	/* temperature BC codes (Boundary_condition.c:10-56) */
 	ALLOC(L->T_bc, nn);
 	ALLOC(L->T_bc_val, nn);
-	for (A = 0; A < nn; A++) {
-		int n = L->node[A];
-		L->T_bc[A] = 'N';
-		L->T_bc_val[A] = 0.0;
-		if ((n + 1) % gnoz == 0) {
-			L->T_bc[A] = c->top_T_bc;
-			L->T_bc_val[A] = c->top_T_bc_val;
-		} else if (n % gnoz == 0) {
-			L->T_bc[A] = c->bot_T_bc;
-			L->T_bc_val[A] = c->bot_T_bc_val;
-		} else if (n < gnoz) {
-			if (L->T_bc[A] != 'T')
-				L->T_bc[A] = c->lef_T_bc;
-			L->T_bc_val[A] = c->lef_T_bc_val;
-		} else if (n > (gnox - 1) * gnoz - 1) {
-			if (L->T_bc[A] != 'T')
-				L->T_bc[A] = c->rig_T_bc;
-			L->T_bc_val[A] = c->rig_T_bc_val;
-		}
-	}
-	/* velocity BC codes (Boundary_condition.c:58-110) */
 	ALLOC(L->v_bc, 2 * nn);
 	ALLOC(L->v_bc_val, 2 * nn);
-	for (d = 0; d < 2; d++)
-		for (A = 0; A < nn; A++) {
-			int n = L->node[A];
-			char *bc = &L->v_bc[d * nn + A];
-			double *bv = &L->v_bc_val[d * nn + A];
-			*bc = 'N';
-			*bv = 0.0;
-			if ((n + 1) % gnoz == 0) {
-				*bc = c->top_v_bc[d];
-				*bv = c->top_v_bc_val[d];
-			} else if (n % gnoz == 0) {
-				*bc = c->bot_v_bc[d];
-				*bv = c->bot_v_bc_val[d];
-			}
-			if (n < gnoz) {
-				if (*bc != 'V')
-					*bc = c->lef_v_bc[d];
-				*bv = c->lef_v_bc_val[d];
-			} else if (n > (gnox - 1) * gnoz - 1) {
-				if (*bc != 'V')
-					*bc = c->rig_v_bc[d];
-				*bv = c->rig_v_bc_val[d];
-			}
-		}
+	mclg_parallel_for(nn, 16384, node_range, &lc);
 	/* equation numbers (Construct_ien_id_lm.c:79-144) */
 	ALLOC(L->id, 2 * nn);
 	ALLOC(L->heat_id, nn);
@@ -512,13 +568,7 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 	ALLOC(L->dz_deta, ne);
 	ALLOC(L->jacobi, ne);
 	ALLOC(L->area, ne);
-	for (e = 0; e < ne; e++) {
-		int n0 = L->ienl[e], n2 = L->ienl[2L * ne + e];
-		L->dx_dxi[e] = 0.5 * m->dx[L->elev[e]];
-		L->dz_deta[e] = 0.5 * m->dz[L->elev[e]];
-		L->jacobi[e] = L->dx_dxi[e] * L->dz_deta[e] - 0.0 * 0.0;
-		L->area[e] = (L->X[n2] - L->X[n0]) * (L->X[nn + n2] - L->X[nn + n0]);
-	}
+	mclg_parallel_for(ne, 16384, geom_range, &lc);
 	/* node -> element map in ascending element order (Construct_ien_id_lm.c:220-244) */
 	ALLOC(L->p2n_cnt, nn);
 	ALLOC(L->p2n_el, 4 * nn);
@@ -627,12 +677,7 @@ static int build_level_arrays(mclg_mesh *m, const mclg_config *c, int lev)
 	if (lev == fl) {
 		long ncx = gnox - 1, ncz = gnoz - 1;
 		ALLOC(L->cell_elem, ncx * ncz);
-		for (e = 0; e < ne; e++) {
-			int n0 = L->ien[e], ix0 = n0 / gnoz, iz0 = n0 - ix0 * gnoz, s = 1 << (fl - L->elev[e]), i, j;
-			for (i = 0; i < s; i++)
-				for (j = 0; j < s; j++)
-					L->cell_elem[(long)(ix0 + i) * ncz + iz0 + j] = e;
-		}
+		mclg_parallel_for(ne, 16384, cell_range, &lc);
 	}
 	return MCLG_OK;
 oom:
