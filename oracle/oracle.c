@@ -11,6 +11,7 @@
  * every solver is the reference's iteration verbatim:
  *   buoyancy_force          Buoyancy.c:3-22, Parallel.c:354-454
  *   viscosity               Viscosity.c:3-24
+ *   visc_from_grain_size    Grain_size_evolution.c:3-152 (grain_damage=1, single-level meshes)
  *   K / F / G assembly      Build_matrix.c:42-381, 720-744
  *   citcom_solver (Uzawa)   Solver.c:14-249, initial_d_p :251-278
  *   Conj_Grad / jacobi      Solver.c:1589-1864, K_prod_d :360-386

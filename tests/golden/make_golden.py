@@ -12,7 +12,8 @@ this script, together with the .input file of each case.
 Keys in <case>.npz:
     mesh/<array>@<lev>       numbering and geometry (harness dump_mesh)
     ops/<array>@<lev>        assembled K, G (CSR), F, Kdiag, BAB, K x, G p, G^T x
-    step<k>/<array>          fields after the Stokes solve of step k
+    step<k>/<array>          fields after the Stokes solve of step k (with grain_damage=1
+                             also gs, the grain size)
     heat<k>/<array>          fields after update_temperature of step k
     series/<name>            per-step scalars: dt, model_time, uzawa cycles, residuals
 """
