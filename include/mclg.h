@@ -173,7 +173,10 @@ int mclg_solve_velocity_pressure(mclg_ctx *ctx, mclg_step_stats *st); /* Solver.
  * MCLG_NOALLOC_MAX_ELEMS elements (about 3.3 MB, held on every GPU that loads
  * the library until exit); larger meshes get MCLG_BAD_INPUT.  All calls share
  * the array: calls whose GPU work overlaps race.  The first call on a device
- * looks the array's device address up, so make it before any stream capture. */
+ * looks the array's device address up, so make it before any stream capture.
+ * It updates d, P, V and the nodal stress of the context; the element stresses
+ * and the solve counts that the context keeps for the regular solve are left
+ * as they were (the counts come back in *st). */
 #define MCLG_NOALLOC_MAX_NODES 16641
 #define MCLG_NOALLOC_MAX_ELEMS 16384
 int mclg_solve_velocity_pressure_noalloc(mclg_ctx *ctx, mclg_step_stats *st);

@@ -2204,6 +2204,10 @@ extern "C" int mclg_solve_velocity_pressure_noalloc(mclg_ctx *c, mclg_step_stats
 		CK(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
 	c->p_initialized = 1;
 	CK(cudaMemsetAsync(sc, 0, sizeof(StepScalars), c->st));
+	// this solve reports its status through the array's scalars; a status that
+	// an earlier regular solve left in the context's own scalars must not reach
+	// the mclg_update_temperature that follows
+	CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
 	UzawaArgs a;
 	memset(&a, 0, sizeof a);
 	a.L = c->L;

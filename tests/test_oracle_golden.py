@@ -66,6 +66,31 @@ def test_capped_dev14_iterate_is_ill_conditioned():
     assert max(e.values()) < 2e-3, e
 
 
+def test_grain_steps_are_ill_conditioned():
+    """From step 1 on, the grain-size runs solve with the viscosity spread over
+    the clip range [1e-3, 1e3] and about 400 Uzawa cycles of inner CG at its
+    2000-iteration cap.  Moving T by 1e-15 relative -- below the rounding of one
+    summation -- leaves the viscosity unchanged to 1e-15 but moves the oracle's
+    own P by more than 1e-8 (measured 1.3e-8 .. 3.9e-8 over seeds) and V by up
+    to 7e-9.  That envelope, not the grain law, sets the GPU test's bars for
+    these steps (P 1e-7, V/d/stress 3e-8)."""
+    g = golden("gdw_l5")
+    worst = {"P": 0.0, "V": 0.0, "vis": 0.0}
+    for seed in (0, 3):
+        o = oracle_port.Oracle(golden_input("gdw_l5"))
+        T = o.mesh.initial_temperature()
+        o.set_T(T * (1 + 1e-15 * np.random.default_rng(seed).standard_normal(T.size)))
+        o.step()
+        o.step()
+        worst["P"] = max(worst["P"], rel(o.get("P"), g["step0001/p"]))
+        worst["V"] = max(worst["V"], rel(o.get("V0"), g["step0001/V0"]), rel(o.get("V1"), g["step0001/V1"]))
+        worst["vis"] = max(worst["vis"], rel(o.get("vis"), g["step0001/vis"]))
+        o.close()
+    assert worst["vis"] < 1e-15, worst
+    assert 1e-8 < worst["P"] < 1e-7, worst
+    assert worst["V"] < 3e-8, worst
+
+
 @pytest.mark.parametrize("case,steps", [("gd_l5", 2), ("gdw_l5", 2)])
 def test_oracle_grain_size(case, steps):
     """Grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-152) on a
