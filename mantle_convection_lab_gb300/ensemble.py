@@ -59,12 +59,25 @@ def draw(n=256, seed=4, sizes=SIZES):
     return out
 
 
-def configs(n=256, seed=4, sizes=SIZES):
-    return [member_config(*p) for p in draw(n, seed, sizes)]
+def shard(n, rank=0, world=1):
+    """The members rank `rank` of `world` steps: rank, rank + world, ...  Members
+    are independent, so the ranks share no data while stepping; the reference
+    distributes one model's elements over MPI ranks instead (Parallel.c:167-309),
+    which a single device makes unnecessary."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    return list(range(rank, n, world))
 
 
-def make(n=256, seed=4, sizes=SIZES):
-    e = Ensemble(configs(n, seed, sizes))
+def configs(n=256, seed=4, sizes=SIZES, members=None):
+    ps = draw(n, seed, sizes)
+    idx = range(n) if members is None else members
+    return [member_config(*ps[i]) for i in idx]
+
+
+def make(n=256, seed=4, sizes=SIZES, members=None):
+    """The ensemble of members `members` (all n by default) of the n drawn."""
+    e = Ensemble(configs(n, seed, sizes, members))
     e.initial_temperature()
     return e
 
@@ -74,9 +87,9 @@ def amr_levels(n=256, seed=4):
     return np.random.default_rng(seed + 7919).integers(0, 3, n).astype(np.int32)
 
 
-def amr_configs(n=256, seed=4, sizes=SIZES):
+def amr_configs(n=256, seed=4, sizes=SIZES, members=None):
     """Members with the boundary-layer start that |grad T| refinement follows."""
-    out = configs(n, seed, sizes)
+    out = configs(n, seed, sizes, members)
     for c in out:
         c.ic_kind = 2
         c.ic_bl_thickness = 0.02
@@ -85,7 +98,10 @@ def amr_configs(n=256, seed=4, sizes=SIZES):
     return out
 
 
-def make_amr(n=256, seed=4, sizes=SIZES):
-    e = Ensemble(amr_configs(n, seed, sizes), amr_levels(n, seed))
+def make_amr(n=256, seed=4, sizes=SIZES, members=None):
+    lv = amr_levels(n, seed)
+    if members is not None:
+        lv = np.ascontiguousarray(lv[list(members)])
+    e = Ensemble(amr_configs(n, seed, sizes, members), lv)
     e.initial_temperature()
     return e

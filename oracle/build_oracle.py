@@ -10,13 +10,17 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle.c")
+# the seeded initial-temperature header shared with the engine and the dump harness
+IC_DIR = os.path.join(os.path.dirname(HERE), "mantle_convection_lab_gb300", "csrc", "host")
 LIB = os.path.join(HERE, "liboracle.so")
 
 
 def build():
-    if os.path.exists(LIB) and os.path.getmtime(LIB) > os.path.getmtime(SRC):
+    deps = [SRC, os.path.join(IC_DIR, "mclg_ic.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(LIB) > os.path.getmtime(d) for d in deps):
         return LIB
-    base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", SRC, "-o", LIB, "-lm"]
+    base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-I" + IC_DIR, SRC, "-o", LIB,
+            "-lm"]
     p = subprocess.run(base[:1] + ["-fopenmp"] + base[1:], capture_output=True, text=True)
     if p.returncode != 0:
         p = subprocess.run(base, capture_output=True, text=True)

@@ -1340,3 +1340,39 @@ int orc_cg_sample(orc *o, int n)
 	free(x);
 	return c;
 }
+
+/* Seeded initial temperature for T_ini 0, 1 and -2 (Initial_condition.c:3-75
+ * for 0 and 1; the counter-based field of mclg_ic.h for -2) at n nodes, with
+ * the same libm calls as the engine's host code; Dirichlet values are applied
+ * by the caller (apply_T_bc_values, Initial_condition.c:122-136). */
+#include <stdint.h>
+#include "mclg_ic.h"
+void orc_initial_temperature(int T_ini, const double *dpar, const int *ipar, uint64_t seed, int n, const double *X,
+                             const int *gid, double *T)
+{
+	/* dpar: length, height, T_mantle, T_mantle_perturb, ic_noise, ic_bl_thickness, ic_mode_amp
+	 * ipar: T_wave_number, ic_kind, ic_modes */
+	const double pi = M_PI, L = dpar[0], H = dpar[1];
+	int i;
+	mclg_ic_params p;
+	memset(&p, 0, sizeof p);
+	p.kind = ipar[1];
+	p.seed = seed;
+	p.noise = dpar[4];
+	p.perturb = dpar[3];
+	p.wave = ipar[0];
+	p.bl_thickness = dpar[5];
+	p.nmodes = ipar[2];
+	p.mode_amp = dpar[6];
+	p.length = L;
+	p.height = H;
+	for (i = 0; i < n; i++) {
+		double x = X[i], z = X[n + i];
+		if (T_ini == 0)
+			T[i] = H - z + dpar[3] * sin(pi * (H - z) / H) * cos(ipar[0] * pi * x / L);
+		else if (T_ini == 1)
+			T[i] = dpar[2] + dpar[3] * sin(pi * (H - z) / H) * cos(ipar[0] * pi * x / L);
+		else
+			T[i] = mclg_ic_temperature(&p, x, z, (uint32_t)gid[i]);
+	}
+}

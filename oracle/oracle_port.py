@@ -2,7 +2,9 @@
 
 The mesh arrays (ien, node list, BC codes, hanging nodes) come from the host
 mesh builder of the engine, which tests pin bit-exact against the
-reference's own arrays; everything numerical is recomputed here on the CPU.
+reference's own arrays, or -- with standalone=True, for uniform meshes --
+from oracle/mesh_oracle.py, which loads nothing of the engine; everything
+numerical is recomputed here on the CPU.
 
     r = run("case.input", steps=3)      # dict of T, V0, V1, P, d, stress, vis, stats per step
 """
@@ -50,6 +52,8 @@ def lib():
         _L.orc_cg_sample.argtypes = [vp, C.c_int]
         _L.orc_mg_attach.restype = C.c_int
         _L.orc_mg_attach.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+        _L.orc_initial_temperature.restype = None
+        _L.orc_initial_temperature.argtypes = [C.c_int, vp, vp, C.c_uint64, C.c_int, vp, vp, vp]
     return _L
 
 
@@ -67,12 +71,21 @@ class Oracle:
     initial temperature, as in the reference) and the transfer maps of
     oracle/mg_oracle.py."""
 
-    def __init__(self, cfg, threads=1, leaves=None):
-        from mantle_convection_lab_gb300.api import Config, Mesh
-        if isinstance(cfg, (str, os.PathLike)):
-            cfg = Config.from_input(cfg)
+    def __init__(self, cfg, threads=1, leaves=None, standalone=False):
+        if standalone:
+            # uniform meshes from oracle/mesh_oracle.py: the engine's library is not loaded
+            import mesh_oracle
+            if isinstance(cfg, (str, os.PathLike)):
+                cfg = mesh_oracle.read_input(cfg)
+            if leaves is not None or cfg.solver == b"mg":
+                raise ValueError("the standalone oracle covers uniform meshes with the cg/jc/gs solvers")
+            m = mesh_oracle.UniformMesh(cfg)
+        else:
+            from mantle_convection_lab_gb300.api import Config, Mesh
+            if isinstance(cfg, (str, os.PathLike)):
+                cfg = Config.from_input(cfg)
+            m = Mesh(cfg, leaves=leaves)
         self.cfg = cfg
-        m = Mesh(cfg, leaves=leaves)
         self.mesh = m
         self._keep = []
         self._lv = []
