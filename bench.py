@@ -234,69 +234,134 @@ def job_throughput(dist, units, seconds):
     return rsum(dist, units) / rmax(dist, seconds)
 
 
-# ---- CPU oracle samples (the reference's algorithm) --------------------------
-def _oracle(inp, threads):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+# ---- the reference's algorithm on the host cores (the CPU oracle) ---------------
+# Everything here runs oracle/ with its own .input reader and uniform mesh
+# (oracle/mesh_oracle.py): nothing of the engine is loaded in these arms.
+REF_RECORD = os.path.join(ROOT, "oracle", "ref_steps_cfg3_mg_1024.json")
+
+
+def _oracle_mod():
+    p = os.path.join(ROOT, "oracle")
+    if p not in sys.path:
+        sys.path.insert(0, p)
+    import mesh_oracle
     import oracle_port
-    return oracle_port.Oracle(os.path.join(ROOT, inp), threads=threads)
+    return oracle_port, mesh_oracle
 
 
-def cpu_sample(wl, threads, steps=None):
-    """Returns (steps_per_s, cores, description).  Configuration 1 runs whole
-    steps.  At 1024^2 one reference step is thousands of CG solves (its Uzawa
-    loop runs to max_citcom_cycle x max_cg_cycle at this viscosity contrast), so
-    the sample times the assembly and 20 inner CG iterations on the real mesh
-    and scales to that per-step iteration budget."""
+def _oracle(inp, threads, mesh_level=None, cfg=None):
+    oracle_port, mesh_oracle = _oracle_mod()
+    cfg = cfg if cfg is not None else mesh_oracle.read_input(os.path.join(ROOT, inp))
+    return oracle_port.Oracle(cfg, threads=threads, standalone=True, mesh_level=mesh_level)
+
+
+def reference_record():
+    """Whole steps of the reference's algorithm on configuration 3 at 1024^2,
+    measured by oracle/time_reference_steps.py (per step: Uzawa cycles, inner
+    CG iterations, wall time and the host they ran on)."""
+    with open(REF_RECORD) as fh:
+        return json.load(fh)
+
+
+def cpu_sample(wl, threads, samples=3, warmup=0, cycles=1):
+    """Returns (steps_per_s, cores, description, timed_seconds).
+
+    Configuration 1: whole steps of the reference algorithm.
+    Configuration 3 (1024^2): one whole reference step takes minutes (its first
+    step runs Uzawa to max_citcom_cycle with every inner CG at max_cg_cycle), so
+    each sample is a real step truncated after `cycles` Uzawa cycles -- the
+    assembly, the initial inner CG solve, `cycles` Uzawa cycles with their full
+    inner solves, the temperature update -- and the whole steps are rebuilt from
+    the timed parts and the inner-CG iteration counts of whole reference steps
+    recorded in oracle/ref_steps_cfg3_mg_1024.json:
+        t_step = t_assembly + t_heat + C_step * (t_solve / C_sample)."""
     if wl["kind"] == "replica":
         o = _oracle(wl["input"], 1)
-        o.step()
-        n = steps or 10
+        for _ in range(max(warmup, 1)):
+            o.step()
         t0 = time.perf_counter()
-        for _ in range(n):
+        for _ in range(samples):
             o.step()
         el = time.perf_counter() - t0
         o.close()
-        return n / el, 1, f"{n} steady steps of the reference algorithm on 1 core ({el:.1f} s)"
+        return samples / el, 1, f"{samples} whole steps of the reference algorithm on 1 core ({el:.1f} s)", el
+    rec = reference_record()
     o = _oracle(wl["input"], threads)
-    t0 = time.perf_counter()
-    o.assemble()
-    t_asm = time.perf_counter() - t0
-    ncg = 20
-    t0 = time.perf_counter()
-    o.cg_sample(ncg)
-    t_cg = (time.perf_counter() - t0) / ncg
-    budget = o.cfg.max_citcom_cycle * o.cfg.max_cg_cycle
+    t_asm, t_heat, t_cg, timed = [], [], [], 0.0
+    for k in range(warmup + samples):
+        o.set_caps(cycles, o.cfg.max_cg_cycle)
+        t0 = time.perf_counter()
+        st = o.step()
+        el = time.perf_counter() - t0
+        if k >= warmup:
+            timed += el
+            t_asm.append(st["s_assembly"])
+            t_heat.append(st["s_heat"])
+            t_cg.append(st["s_solve"] / max(st["cg_cycles"], 1))
     o.close()
-    per_step = t_asm + budget * t_cg
-    return 1.0 / per_step, threads, (f"assembly ({t_asm:.2f} s) + {ncg} CG iterations ({1e3 * t_cg:.1f} ms each) "
-                                     f"on the 1024^2 mesh with {threads} threads, scaled to the reference's "
-                                     f"per-step budget of {budget} CG iterations (max_citcom_cycle x max_cg_cycle)")
+    a, h, c = statistics.median(t_asm), statistics.median(t_heat), statistics.median(t_cg)
+    steps = rec["steps"]
+    total = sum(a + h + s["cg_iterations"] * c for s in steps)
+    v = len(steps) / total
+    desc = (f"{samples} real steps truncated after {cycles} Uzawa cycle(s) on the 1024^2 mesh with {threads} threads "
+            f"(assembly {a:.2f} s, temperature update {h:.2f} s, {1e3 * c:.2f} ms per inner CG iteration), rebuilt "
+            f"into the reference's first {len(steps)} whole steps with their recorded inner-CG counts "
+            f"{[s['cg_iterations'] for s in steps]} (Uzawa cycles {[s['uzawa_cycles'] for s in steps]}; "
+            f"oracle/ref_steps_cfg3_mg_1024.json, whole steps timed on {rec.get('host', 'a host')} with "
+            f"{rec['threads']} threads: {[round(s['wall_s'], 1) for s in steps]} s)")
+    return v, threads, desc, timed
 
 
-def ensemble_cpu_sample():
-    """The reference's algorithm on one 32x32 member (1 core, a few steps),
-    extrapolated to the whole 256-member mix with a per-step cost growing as
-    (N/32)^3 (Jacobi-PCG iterations grow like N, work per iteration like N^2)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_port
-    from mantle_convection_lab_gb300 import ensemble
+def _member_config(n_side, rayleigh, contrast, seed):
+    """ensemble.member_config on the oracle's own input reader."""
+    import math
+    _, mesh_oracle = _oracle_mod()
+    c = mesh_oracle.read_input(os.path.join(ROOT, "mantle_convection_lab_gb300", "configs", "cfg3_mg_1024.input"))
+    c.level = int(round(math.log2(n_side))) + 1
+    c.mg_min_level = 1
+    c.Rayleigh, c.A, c.refT = rayleigh, math.log(contrast), 0.0
+    c.vis_min, c.vis_max = 1.0 / contrast, 1.0
+    c.ic_kind, c.ic_seed, c.ic_noise, c.T_mantle_perturb, c.T_wave_number = 1, seed, 1e-3, 0.01, 1
+    return c
+
+
+def ensemble_cpu_sample(threads, steps=2):
+    """The reference's algorithm on one member of each size class (its first
+    member in the draw), `steps` whole steps each with all threads; the
+    ensemble's rate rebuilt as 256 / sum over members of the measured step time
+    of the member's size class."""
+    from mantle_convection_lab_gb300 import ensemble   # the draw only (numpy)
     params = ensemble.draw(256, 4)
-    small = next(p for p in params if p[0] == 32)
-    cfg = ensemble.member_config(*small)
-    cfg.precision = 0
-    cfg.warm_start = 0
-    cfg.max_citcom_cycle, cfg.max_cg_cycle, cfg.accuracy, cfg.citcom_solver_accu = 2000, 2000, 1e-8, 1e-8
-    o = oracle_port.Oracle(cfg, threads=1)
-    o.step()
-    n = 3
-    t0 = time.perf_counter()
-    for _ in range(n):
-        o.step()
-    t32 = (time.perf_counter() - t0) / n
-    o.close()
-    total = sum(t32 * (p[0] / 32) ** 3 for p in params)
-    return 256 / total, 1, (f"{n} steps of a 32x32 member on 1 core ({1e3 * t32:.0f} ms/step), extrapolated to the "
-                            f"256-member mix as (N/32)^3 per member")
+    per = {}
+    timed = 0.0
+    for side in ensemble.SIZES:
+        p = next(q for q in params if q[0] == side)
+        o = _oracle(None, threads, cfg=_member_config(*p))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step()
+        el = time.perf_counter() - t0
+        o.close()
+        timed += el
+        per[side] = el / steps
+    total = sum(per[q[0]] for q in params)
+    return 256 / total, threads, (f"{steps} whole steps of the reference algorithm on one member per size class with "
+                                  f"{threads} threads (s/step: " + ", ".join(f"{k}^2 {v:.2f}" for k, v in per.items())
+                                  + "), the 256-member mix rebuilt from the per-class step times"), timed
+
+
+def _ref_line(args, world, metric, v, unit, cores, sample, timed, steps, warmup, extra=None):
+    line = {"metric": metric, "impl": "reference", "value": v, "unit": unit, "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .input)",
+            "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                       "mesh": WORKLOADS[args.workload]["mesh"]},
+            "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+            "timed_s": timed,
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if extra:
+        line.update(extra)
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(args, wl):
@@ -305,58 +370,90 @@ def run_reference(args, wl):
         return 0
     threads = os.cpu_count() or 1
     if wl["kind"] == "amr":
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle_port
-        from mantle_convection_lab_gb300 import Config, amr
-        cfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+        _, mesh_oracle = _oracle_mod()
+        cfg = mesh_oracle.read_input(os.path.join(ROOT, wl["input"]))
         cfg.max_citcom_cycle, cfg.max_cg_cycle = 200, 500
-        o = oracle_port.Oracle(cfg, threads=1, leaves=amr.uniform_leaves(cfg.level - 1, 7))
+        o = _oracle(None, threads, mesh_level=8, cfg=cfg)   # the unrefined 128 x 128 base
         t0 = time.perf_counter()
         o.step()
-        v = 1.0 / (time.perf_counter() - t0)
-        o.close()
-        line = {"metric": "time steps/s including remeshing (configuration 2)", "impl": "reference", "value": v,
-                "unit": "steps/s", "n_gpus": world, "steps": 1, "warmup": 0, "ms_per_step": 1e3 / v,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded .input)", "config": {"workload": args.workload, "desc": wl["desc"]},
-                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": "one step of the reference's algorithm on the unrefined 128x128 base "
-                                           "mesh (a lower bound on a refined step's cost), 1 core"},
-                "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return 0
-    if wl["kind"] == "ensemble":
-        v, cores, sample = ensemble_cpu_sample()
-        line = {"metric": ENSEMBLE_METRIC, "impl": "reference", "value": v, "unit": "model-steps/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 256e3 / v, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded members)",
-                "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"]},
-                "cpu_baseline": {"value": v, "unit": "model-steps/s", "cores": cores, "kind": "port", "sample": sample},
-                "e2e": {"value": v, "unit": "model-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return 0
-    if wl["kind"] == "replica":
-        steps = max(1, args.steps)
-        o = _oracle(wl["input"], 1)
-        for _ in range(max(0, args.warmup)):
-            o.step()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            o.step()
         el = time.perf_counter() - t0
         o.close()
-        v, cores, sample = steps / el, 1, f"{steps} steps after {args.warmup} warm-up steps, 1 core"
-    else:
-        v, cores, sample = cpu_sample(wl, threads)
-        steps = args.steps
-    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "steps/s", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .input)",
-            "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"]},
-            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+        _ref_line(args, world, "time steps/s including remeshing (configuration 2)", 1.0 / el, "steps/s", threads,
+                  f"one whole step of the reference's algorithm (caps 200 x 500) on the unrefined 128x128 base mesh "
+                  f"with {threads} threads: a lower bound on a refined step's cost", el, 1, 0)
+        return 0
+    if wl["kind"] == "ensemble":
+        v, cores, sample, timed = ensemble_cpu_sample(threads)
+        _ref_line(args, world, ENSEMBLE_METRIC, v, "model-steps/s", cores, sample, timed, args.steps, args.warmup)
+        return 0
+    if wl["kind"] == "replica":
+        v, cores, sample, timed = cpu_sample(wl, threads, samples=max(1, args.steps), warmup=max(0, args.warmup))
+        _ref_line(args, world, METRIC, v, "steps/s", cores, sample, timed, max(1, args.steps), args.warmup)
+        return 0
+    # configuration 3: bounded samples of real steps, rebuilt with recorded whole-step counts
+    n = max(1, min(args.steps, 10))
+    v, cores, sample, timed = cpu_sample(wl, threads, samples=n, warmup=1 if args.warmup > 0 else 0)
+    rec = reference_record()
+    _ref_line(args, world, METRIC, v, "steps/s", cores, sample, timed, n, 1 if args.warmup > 0 else 0,
+              {"extrapolated": "whole steps rebuilt from timed parts and recorded iteration counts",
+               "reference_residual": "the reference stops on its own update-size test "
+                                     "(citcom_solver_accu, Solver.c:131); its Stokes residual after a step is "
+                                     + ", ".join(f"{max(s['res_momentum'], s['res_continuity']):.2g}"
+                                                 for s in rec["steps"]) + ", never 1e-8"})
     return 0
+
+
+# ---- FP64 parity of the mixed-precision solvers ----------------------------------
+PARITY_RTOL = 1e-12
+
+
+def fp64_reference_config(cfg):
+    """A copy of `cfg` for the FP64 oracle solve of a step: FP64 operator and
+    multigrid (precision fp64mg), MINRES, cold start, residual 1e-12."""
+    from mantle_convection_lab_gb300 import Config
+    c = Config()
+    C_ = __import__("ctypes")
+    C_.memmove(C_.byref(c), C_.byref(cfg), C_.sizeof(Config))
+    c.precision, c.stokes_method, c.warm_start = 2, 1, 0
+    c.stokes_rtol, c.outer_rtol, c.max_refine, c.max_outer = PARITY_RTOL, 1e-3, 80, 4000
+    return c
+
+
+def leaves_of(model, cfg):
+    """Finest-level Morton start codes of a model's current leaves (its Mcode list)."""
+    import numpy as np
+    mc = model.mesh("Mcode").astype(np.int64)
+    F = cfg.level - 1
+    return ((mc >> 4) << (2 * (F - (mc & 15)))).astype(np.int32)
+
+
+def _rel(a, b):
+    import numpy as np
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b)) / (nb if nb > 0 else 1.0)
+
+
+def step_parity(model, cfg, leaves=None, step=None):
+    """Errors of one mixed-precision step against an FP64 solution of the same
+    step: both start from the model's current temperature; the FP64 model
+    solves to residual 1e-12 (fp64mg, whose solutions are pinned to the
+    reference's fixtures).  Returns relative L2 errors of V (both components),
+    P (mean removed: the constant is the null mode of G on the free-slip box)
+    and T after the step.  `step` steps the mixed model (default model.step)."""
+    from mantle_convection_lab_gb300 import Model
+    T0 = model.get("T")
+    st = (step or model.step)()
+    mine = {k: model.get(k) for k in ("V0", "V1", "P", "T")}
+    with Model(fp64_reference_config(cfg), leaves=leaves) as ref:
+        ref.set("T", T0)
+        rs = ref.step()
+        theirs = {k: ref.get(k) for k in ("V0", "V1", "P", "T")}
+    import numpy as np
+    V = _rel(np.concatenate([mine["V0"], mine["V1"]]), np.concatenate([theirs["V0"], theirs["V1"]]))
+    P = _rel(mine["P"] - mine["P"].mean(), theirs["P"] - theirs["P"].mean())
+    return {"V": V, "P": P, "T": _rel(mine["T"], theirs["T"]),
+            "mixed_residual": max(st.res_momentum, st.res_continuity) if st is not None else None,
+            "fp64_residual": max(rs.res_momentum, rs.res_continuity)}
 
 
 # ---- GPU arm --------------------------------------------------------------------
@@ -446,6 +543,37 @@ def run_ensemble(args, wl):
     done = gather_members(dist, {i: (float(m.get("T").sum()), float(member_res[k]))
                                  for k, (i, m) in enumerate(zip(mine, e.members))})
     res = max(v[1] for v in done.values())
+    # FP64 parity: one more ensemble step; the first member of each size class
+    # (and refinement depth) on this rank against its own FP64 solution
+    picks, seen = [], set()
+    params = ensemble.draw(256, 4)
+    for k, i in enumerate(mine):
+        key = (params[i][0], int(levels[i]) if levels is not None else 0)
+        if key not in seen:
+            seen.add(key)
+            picks.append(k)
+    picks = picks[:6]
+    cfgs = ensemble.amr_configs(256, 4, members=[mine[k] for k in picks]) if amr_run else \
+        ensemble.configs(256, 4, members=[mine[k] for k in picks])
+    T0 = {k: e.members[k].get("T") for k in picks}
+    e.step()
+    member_parity = []
+    for k, cfg_k in zip(picks, cfgs):
+        m = e.members[k]
+        mine_f = {f: m.get(f) for f in ("V0", "V1", "P", "T")}
+        from mantle_convection_lab_gb300 import Model
+        import numpy as np
+        lv = leaves_of(m, cfg_k) if amr_run else None
+        with Model(fp64_reference_config(cfg_k), leaves=lv) as ref:
+            ref.set("T", T0[k])
+            rs = ref.step()
+            th = {f: ref.get(f) for f in ("V0", "V1", "P", "T")}
+        member_parity.append({
+            "member": mine[k], "elements_per_side": params[mine[k]][0],
+            "refinement_levels": int(levels[mine[k]]) if levels is not None else 0,
+            "V": _rel(np.concatenate([mine_f["V0"], mine_f["V1"]]), np.concatenate([th["V0"], th["V1"]])),
+            "P": _rel(mine_f["P"] - mine_f["P"].mean(), th["P"] - th["P"].mean()),
+            "T": _rel(mine_f["T"], th["T"]), "fp64_residual": max(rs.res_momentum, rs.res_continuity)})
     sizes = [p[0] for p in ensemble.draw(256, 4)]
     # algorithmic bytes of the batched solver launch: the per-model MINRES model, summed
     line = {
@@ -467,10 +595,14 @@ def run_ensemble(args, wl):
         "gpu_launches": launches,
         "roofline": None,
         "clocks": clocks,
+        "parity": {"members": member_parity,
+                   "max": {f: max(p[f] for p in member_parity) for f in ("V", "P", "T")},
+                   "against": "one more ensemble step; each listed member's step from the same temperature solved "
+                              "alone in FP64 (fp64mg, MINRES) to residual 1e-12; relative L2, pressure mean-free"},
     }
     e.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, sample = ensemble_cpu_sample()
+        v, cores, sample, _ = ensemble_cpu_sample(os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": "model-steps/s", "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -479,7 +611,7 @@ def run_ensemble(args, wl):
     return 0
 
 
-def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0):
+def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0, parity=False):
     from mantle_convection_lab_gb300 import amr
     run = amr.AmrRun(cfg, lag=lag)
     for _ in range(max(warmup, 0)):
@@ -511,6 +643,9 @@ def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0):
     acc["clocks"] = sampler.stop() if sampler else None
     acc["remeshes"] = run.remeshes - acc["rem0"]
     acc["nh"] = run.model.nh
+    if parity:
+        # one more step on the current refined mesh against its FP64 solution
+        acc["parity"] = step_parity(run.model, cfg, leaves=leaves_of(run.model, cfg))
     run.close()
     return acc
 
@@ -536,7 +671,7 @@ def run_amr(args, wl):
     cfg.mg_eta_avg = 1         # coarse viscosity: full-weighted mean (fewest MINRES iterations here)
     # remeshes after the first are asynchronous: the new mesh is built on a host
     # thread during the next two steps, which run on the old mesh
-    acc = _amr_arm(cfg, args.steps, args.warmup, rank == 0, dist, torch, lag=2)
+    acc = _amr_arm(cfg, args.steps, args.warmup, rank == 0, dist, torch, lag=2, parity=True)
     value = job_throughput(dist, args.steps, acc["wall"])
     line = {
         "metric": "time steps/s including remeshing at Stokes residual 1e-8 (configuration 2)", "value": value,
@@ -557,6 +692,9 @@ def run_amr(args, wl):
                    "roofline": "not reported: assembled-ELL operators on 5 levels, latency-bound at this size"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": acc["launches"], "roofline": None, "clocks": acc["clocks"],
+        "parity": dict(acc["parity"], against="one more step on the last refined mesh from the same temperature, "
+                       "solved in FP64 (fp64mg, MINRES on the conforming system) to residual 1e-12; relative L2, "
+                       "pressure mean-free"),
     }
     if not args.no_plain:
         rcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
@@ -657,6 +795,9 @@ def run_gpu(args, wl):
         "clocks": clocks,
         "wall_s_timed": wall,
     }
+    if wl["kind"] == "converged":
+        line["parity"] = dict(step_parity(model, cfg), against="the same step from the same temperature solved in "
+                              "FP64 (fp64mg, MINRES) to Stokes residual 1e-12; relative L2, pressure mean-free")
     if net is not None:
         line["learned_guess"] = {
             "network": os.path.relpath(GUESS_NET, ROOT), "params": net.nparam, "grid": GUESS_GRID,
@@ -683,6 +824,23 @@ def run_gpu(args, wl):
                                     "inner_cg_per_step": macc["cg"] / args.steps,
                                     "max_stokes_residual": macc["res"]}
     if wl["kind"] == "converged" and not args.no_plain:
+        # FP64 with the same method and warm start as the headline arm: what precision alone buys
+        fcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
+        fcfg.precision = 2
+        fm = Model(fcfg)
+        fm.initial_temperature()
+        for _ in range(max(args.warmup, 0)):
+            fm.step()
+        torch.cuda.synchronize()
+        facc = timed_steps(fm, args.plain_steps, flush, torch)
+        fm.close()
+        fv = job_throughput(dist, args.plain_steps, facc["ms_total"] / 1e3)
+        line["fp64_minres"] = {"value": fv, "unit": "steps/s", "steps": args.plain_steps,
+                               "ms_per_step": facc["ms_total"] / args.plain_steps,
+                               "minres_per_step": facc["uz"] / args.plain_steps,
+                               "max_stokes_residual": facc["res"],
+                               "desc": "FP64 operator and multigrid (fp64mg), MINRES, extrapolated warm start: the "
+                                       "headline arm's method without the mixed precision and the network"}
         pcfg = Config.from_input(os.path.join(ROOT, wl["input"]))
         pcfg.precision = 2
         pcfg.warm_start = 2
@@ -705,8 +863,19 @@ def run_gpu(args, wl):
                               "desc": "the reference's Uzawa outer loop with FP64 multigrid-preconditioned inner CG, "
                                       "d=0 and p kept each step (the reference's start)"}
         line["speedup_vs_plain_fp64"] = value / pv
+        best64 = max(pv, fv)
+        line["ablation"] = {
+            "steps_per_s": {"fp64_uzawa_reference_start": pv, "fp64_minres_extrapolated": fv,
+                            "mixed_minres_extrapolated": line.get("mixed_no_network", {}).get("value"),
+                            "mixed_minres_extrapolated_learned": value},
+            "what_each_buys": {"method_and_warm_start_in_fp64": fv / pv,
+                               "mixed_precision": (line["mixed_no_network"]["value"] / fv
+                                                   if "mixed_no_network" in line else None),
+                               "network": (value / line["mixed_no_network"]["value"]
+                                           if "mixed_no_network" in line else None)},
+            "headline_vs_strongest_fp64": value / best64}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, sample = cpu_sample(wl, os.cpu_count() or 1)
+        v, cores, sample, _ = cpu_sample(wl, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -123,6 +123,9 @@ struct Sync {
 };
 
 // ---- small helpers ----------------------------------------------------------
+// Elements per thread and trip of the FP64 vector loops: their loads are all
+// issued before the arithmetic, so each thread keeps several in flight.
+constexpr int kVecU = 4;
 __device__ __forceinline__ void barrier(Sync &sy, bool grid)
 {
 	if (grid)
@@ -369,9 +372,16 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 			barrier(sy, grid);
 		}
 	} else {
-		// sweep 1 (from zero) fused into sweep 2
+		// sweep 1 (from zero) fused into sweep 2; below the finest level the
+		// right-hand side P^T r of the finer level is formed in the same pass
 		if (active) {
-			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr, XS_ZERO);
+			if (l >= 1)
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, nullptr, L.invD, x, PASS_SMOOTH, H.omega,
+				                nullptr, XS_ZERO_R, H.lv[l - 1].r, H.lv[l - 1].n, nullptr, nullptr, nullptr, nullptr,
+				                nullptr, L.b);
+			else
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr,
+				                XS_ZERO);
 			barrier(sy, grid);
 		}
 		for (int s = 2; s < H.nu; s++) {
@@ -387,16 +397,23 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 	if (active) {
 		tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
 		barrier(sy, grid);
-		restrict_res<T, V>(sy.part(grid), L, H.lv[l + 1]);
-		barrier(sy, grid);
+		// the next level forms its right-hand side from L.r in its first sweep,
+		// except the coarsest (a dense solve) and single-sweep cycles
+		if (H.nu == 1 || l + 1 == H.nlev - 1) {
+			restrict_res<T, V>(sy.part(grid), L, H.lv[l + 1]);
+			barrier(sy, grid);
+		}
 	}
 	xcur[l] = x;
 }
 
+// With dotv (level 0 only), the last sweep also accumulates this thread's
+// share of out0.dotv into *dot and is not followed by a barrier: the caller's
+// reduction provides it.
 template <class T>
 __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
                          const typename V2T<T>::t *rhs0, typename V2T<T>::t *out0, bool grid, bool active,
-                         typename V2T<T>::t **xcur)
+                         typename V2T<T>::t **xcur, const double2 *dotv = nullptr, double *dot = nullptr)
 {
 	typedef typename V2T<T>::t V;
 	const MGLevel<T> &L = H.lv[l];
@@ -406,14 +423,18 @@ __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
 	const MGLevel<T> &C = H.lv[l + 1];
 	// the coarse-grid correction x + P xc is formed inside the first post-smoothing sweep
 	for (int s = 0; s < H.nu; s++) {
-		V *dst = (l == 0 && s == H.nu - 1) ? out0 : xt;
+		const bool last = l == 0 && s == H.nu - 1;
+		V *dst = last ? out0 : xt;
+		double *dp = (last && dotv) ? dot : nullptr;
 		if (active) {
 			if (s == 0)
-				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr,
-				                XS_PROLONG, xcur[l + 1], C.n);
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, dp,
+				                XS_PROLONG, xcur[l + 1], C.n, dotv);
 			else
-				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, nullptr);
-			barrier(sy, grid);
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, dp,
+				                XS_PLAIN, nullptr, 0, dotv);
+			if (!dp)
+				barrier(sy, grid);
 		}
 		xt = x;
 		x = dst;
@@ -421,9 +442,12 @@ __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
 	xcur[l] = x;
 }
 
+// out0 = B rhs0.  With dotv, *dot receives this thread's share of out0.dotv
+// and the cycle ends without a barrier (the caller reduces *dot, which
+// synchronises the team); without it the cycle ends with a barrier.
 template <class T>
 __device__ void vcycle(Sync &sy, unsigned char *sm, const MGHier<T> &H, const typename V2T<T>::t *rhs0,
-                       typename V2T<T>::t *out0)
+                       typename V2T<T>::t *out0, const double2 *dotv = nullptr, double *dot = nullptr)
 {
 	typedef typename V2T<T>::t V;
 	V *xcur[kMaxLev];
@@ -431,6 +455,8 @@ __device__ void vcycle(Sync &sy, unsigned char *sm, const MGHier<T> &H, const ty
 	// first block-local level (the coarsest always is; in a batch all are)
 	const int nb = sy.size > 1 ? (H.nblk < lc ? H.nblk : lc) : 0;
 	const bool b0 = sy.leader();
+	if (dot)
+		*dot = 0.0;
 	for (int l = 0; l < lc; l++)
 		level_down<T>(sy, sm, H, l, rhs0, l < nb, l < nb || b0, xcur);
 	if (b0)
@@ -439,9 +465,9 @@ __device__ void vcycle(Sync &sy, unsigned char *sm, const MGHier<T> &H, const ty
 	for (int l = lc - 1; l >= 0; l--) {
 		if (l == nb - 1)
 			sy.sync();   // block 0's coarse-level results become visible to every block
-		level_up<T>(sy, sm, H, l, rhs0, out0, l < nb, l < nb || b0, xcur);
+		level_up<T>(sy, sm, H, l, rhs0, out0, l < nb, l < nb || b0, xcur, dotv, dot);
 	}
-	if (nb == 0)
+	if (nb == 0 && !dotv)
 		sy.sync();
 }
 
@@ -623,38 +649,234 @@ __device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask
 	return s;
 }
 
+// ---- MINRES vector kernels (FP64), kVecU elements per thread and trip ---------
+// Separate functions so that their registers do not compete with the solver's
+// state; every load of a trip is issued before its arithmetic.
+
+// (G^T u)_e in TI for a TI velocity field (free dofs only), in gtmul64_elem's order.
+template <class TI, class V>
+__device__ __forceinline__ TI gtmul_elem_ti(int N0, const unsigned char *mask, const TI *g0, const TI *g1,
+                                            const V *u, int ex, int ez)
+{
+	const int n = N0 + 1;
+	const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
+	TI s = 0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		const V ua = u[cn[a]];
+		const unsigned m = mask[cn[a]];
+		if (!(m & 1u))
+			s += g0[a] * ua.x;
+		if (!(m & 2u))
+			s += g1[a] * ua.y;
+	}
+	return s;
+}
+
+// Ahp = G^T z_u per element (Morton order), formed in TI like the operator's
+// K z_u; returns this thread's share of Ahp.z_p in FP64.
+template <class TI, class VI>
+__device__ __noinline__ double minres_gt_dot(int N0, const unsigned char *__restrict__ mask, const TI *g0,
+                                             const TI *g1, const VI *__restrict__ zu, const double *__restrict__ zp,
+                                             double *__restrict__ Ahp, int tid, int nth)
+{
+	const int ne = N0 * N0;
+	double acc = 0.0;
+	for (int e0 = tid; e0 < ne; e0 += kVecU * nth) {
+		double t[kVecU], zpe[kVecU];
+		int me[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				const int ex = e / N0, ez = e - ex * N0;
+				me[u] = morton(ex, ez);
+				t[u] = (double)gtmul_elem_ti<TI, VI>(N0, mask, g0, g1, zu, ex, ez);
+				zpe[u] = zp[me[u]];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++)
+			if (e0 + u * nth < ne) {
+				Ahp[me[u]] = t[u];
+				acc += t[u] * zpe[u];
+			}
+	}
+	return acc;
+}
+
+// v_old <- az ig - dg v - gg v_old (velocity, with its TI copy into bI) and the
+// same for the pressure part with Ahp.
+template <class VI>
+__device__ __noinline__ void minres_v_update(int nn, int ne, int tid, int nth, const double2 *__restrict__ az_,
+                                             const double2 *__restrict__ v_, double2 *__restrict__ vo_,
+                                             VI *__restrict__ bI, const double *__restrict__ ah_,
+                                             const double *__restrict__ p0_, double *__restrict__ p1_, double ig,
+                                             double dg, double gg)
+{
+	typedef decltype(VI().x) TI;
+	for (int A0 = tid; A0 < nn; A0 += kVecU * nth) {
+		double2 az[kVecU], v[kVecU], vo[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int A = A0 + u * nth;
+			if (A < nn) {
+				az[u] = az_[A];
+				v[u] = v_[A];
+				vo[u] = vo_[A];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int A = A0 + u * nth;
+			if (A < nn) {
+				const double2 vn = make_double2(az[u].x * ig - dg * v[u].x - gg * vo[u].x,
+				                                az[u].y * ig - dg * v[u].y - gg * vo[u].y);
+				vo_[A] = vn;
+				VI w;
+				w.x = (TI)vn.x;
+				w.y = (TI)vn.y;
+				bI[A] = w;
+			}
+		}
+	}
+	for (int e0 = tid; e0 < ne; e0 += kVecU * nth) {
+		double ah[kVecU], p0[kVecU], p1[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				ah[u] = ah_[e];
+				p0[u] = p0_[e];
+				p1[u] = p1_[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne)
+				p1_[e] = ah[u] * ig - dg * p0[u] - gg * p1[u];
+		}
+	}
+}
+
+// w_old <- (z ig - a3 w_old - a2 w) ia1 and x += step w_old, for the velocity
+// (z in TI) and the pressure parts.
+template <class VI>
+__device__ __noinline__ void minres_w_update(int nn, int ne, int tid, int nth, const VI *__restrict__ z_,
+                                             double2 *__restrict__ wo_, const double2 *__restrict__ w_,
+                                             double2 *__restrict__ x_, const double *__restrict__ zp_,
+                                             double *__restrict__ wpo_, const double *__restrict__ wp_,
+                                             double *__restrict__ xp_, double ig, double a3, double a2, double ia1,
+                                             double step)
+{
+	for (int A0 = tid; A0 < nn; A0 += kVecU * nth) {
+		VI z[kVecU];
+		double2 wo[kVecU], w[kVecU], x[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int A = A0 + u * nth;
+			if (A < nn) {
+				z[u] = z_[A];
+				wo[u] = wo_[A];
+				w[u] = w_[A];
+				x[u] = x_[A];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int A = A0 + u * nth;
+			if (A < nn) {
+				const double2 wn = make_double2(((double)z[u].x * ig - a3 * wo[u].x - a2 * w[u].x) * ia1,
+				                                ((double)z[u].y * ig - a3 * wo[u].y - a2 * w[u].y) * ia1);
+				wo_[A] = wn;
+				x_[A] = make_double2(x[u].x + step * wn.x, x[u].y + step * wn.y);
+			}
+		}
+	}
+	for (int e0 = tid; e0 < ne; e0 += kVecU * nth) {
+		double zz[kVecU], wo[kVecU], w[kVecU], x[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				zz[u] = zp_[e];
+				wo[u] = wpo_[e];
+				w[u] = wp_[e];
+				x[u] = xp_[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				const double wn = (zz[u] * ig - a3 * wo[u] - a2 * w[u]) * ia1;
+				wpo_[e] = wn;
+				xp_[e] = x[u] + step * wn;
+			}
+		}
+	}
+}
+
+// z_p = v_p / BAB (ibab = 1/BAB), also into zpt in TI; returns this thread's
+// share of z_p.v_p.
+template <class TI>
+__device__ __noinline__ double precond_pressure(int ne, int tid, int nth, const double *__restrict__ vp,
+                                                const double *__restrict__ ibab, double *zp, TI *zpt)
+{
+	double acc = 0.0;
+	for (int e0 = tid; e0 < ne; e0 += kVecU * nth) {
+		double v[kVecU], ib[kVecU];
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				v[u] = vp[e];
+				ib[u] = ibab[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kVecU; u++) {
+			const int e = e0 + u * nth;
+			if (e < ne) {
+				const double z = v[u] * ib[u];
+				zp[e] = z;
+				zpt[e] = (TI)z;
+				acc += z * v[u];
+			}
+		}
+	}
+	return acc;
+}
+
 // z = M^-1 v for M = diag(one V-cycle of K, BAB): the velocity part goes
-// through the TI hierarchy (z_u stays in TI), the pressure part is divided by
-// BAB.  Returns <z, v> over the grid.
+// through the TI hierarchy (z_u stays in TI), the pressure part is multiplied
+// by 1/BAB (a.bab holds the reciprocal).  Returns <z, v> over the team.  With
+// converted, the caller has already written v_u in TI to the finest level's
+// right-hand side (H.lv[0].b) and synchronised.
 template <class TI>
 __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, const double2 *vu, const double *vp,
-                                typename V2T<TI>::t *zu, double *zp)
+                                typename V2T<TI>::t *zu, double *zp, TI *zpt, bool converted = false)
 {
 	typedef typename V2T<TI>::t VI;
 	const MGHier<TI> &H = a.H;
 	const int tid = sy.tid, nth = sy.nth;
 	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
 	VI *bI = H.lv[0].b;
-	for (int A = tid; A < nn; A += nth) {
-		const double2 v = vu[A];
-		VI w;
-		w.x = (TI)v.x;
-		w.y = (TI)v.y;
-		bI[A] = w;
+	if (!converted) {
+		for (int A = tid; A < nn; A += nth) {
+			const double2 v = vu[A];
+			VI w;
+			w.x = (TI)v.x;
+			w.y = (TI)v.y;
+			bI[A] = w;
+		}
+		sy.sync();
 	}
-	sy.sync();
-	vcycle<TI>(sy, sm, H, bI, zu);
 	double dot[1] = {0.0};
-	for (int A = tid; A < nn; A += nth) {
-		const VI z = zu[A];
-		const double2 v = vu[A];
-		dot[0] += (double)z.x * v.x + (double)z.y * v.y;
-	}
-	for (int e = tid; e < ne; e += nth) {
-		const double z = vp[e] / a.bab[e];
-		zp[e] = z;
-		dot[0] += z * vp[e];
-	}
+	vcycle<TI>(sy, sm, H, bI, zu, vu, &dot[0]);   // the last sweep forms <z_u, v_u>
+	dot[0] += precond_pressure<TI>(ne, tid, nth, vp, a.bab, zp, zpt);
 	sy.reduce<1>(dot);
 	return dot[0];
 }
@@ -696,7 +918,7 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		a.dpv[e] = 0.0;
 	}
 	sy.sync();
-	double gam2 = block_precond(a, sm, sy, vu[0], vp[0], zu[0], zp[0]);
+	double gam2 = block_precond(a, sm, sy, vu[0], vp[0], zu[0], zp[0], a.mzpt[0]);
 	if (!(gam2 > 0.0))
 		return 0;
 	double gam = sqrt(gam2), gam_prev = 1.0;
@@ -704,37 +926,21 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 	double eta = gam, c_prev = 1.0, c_cur = 1.0, s_prev = 0.0, s_cur = 0.0;
 	int cv = 0, cw = 0, it = 0;   // index cv: z(j), v(j); 1-cv: v(j-1).  cw: w(j); 1-cw: w(j-1)
 	while (it < maxit) {
-		// A z(j), unscaled (z~ = z / gam): K z_u + G z_p, and G^T z_u per element
-		tile_pass<TI, VI>(sm, sy.part(true), L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_MATVEC, TI(0), nullptr);
-		gmul64(N0, a.mask0, gt, zp[cv], a.u1, tid, nth);
-		sy.sync();
+		// A z(j), unscaled (z~ = z / gam): K z_u + G z_p into a.Kd with its
+		// product with z_u formed in the same pass, and G^T z_u per element
 		double dl[1] = {0.0};
-		for (int A = tid; A < nn; A += nth) {
-			const VI k = kz[A], z = zu[cv][A];
-			const double2 q = a.u1[A];
-			const double2 az = make_double2((double)k.x + q.x, (double)k.y + q.y);
-			a.Kd[A] = az;
-			dl[0] += az.x * (double)z.x + az.y * (double)z.y;
-		}
-		for (int e = tid; e < ne; e += nth) {
-			const int ex = e / N0, ez = e - ex * N0;
-			const int me = morton(ex, ez);
-			const double t = gtmul_elem_t(N0, a.mask0, gt, zu[cv], ex, ez);
-			a.Ahp[me] = t;
-			dl[0] += t * zp[cv][me];
-		}
+		tile_pass<TI, VI>(sm, sy.part(true), L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_STOKES, TI(0),
+		                  &dl[0], XS_PLAIN, nullptr, 0, nullptr, a.mzpt[cv], a.gti0, a.gti1, a.Kd);
+		dl[0] += minres_gt_dot<TI, VI>(N0, a.mask0, a.gti0, a.gti1, zu[cv], zp[cv], a.Ahp, tid, nth);
 		sy.reduce<1>(dl);
 		const double delta = dl[0] / (gam * gam);
-		// v(j+1) = A z~ - (delta/gam) v(j) - (gam/gam_prev) v(j-1), into v(j-1)'s buffer
+		// v(j+1) = A z~ - (delta/gam) v(j) - (gam/gam_prev) v(j-1), into v(j-1)'s
+		// buffer, and its TI copy as the V-cycle's right-hand side
 		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
-		for (int A = tid; A < nn; A += nth) {
-			const double2 az = a.Kd[A], v = vu[cv][A], vo = vu[1 - cv][A];
-			vu[1 - cv][A] = make_double2(az.x * ig - dg * v.x - gg * vo.x, az.y * ig - dg * v.y - gg * vo.y);
-		}
-		for (int e = tid; e < ne; e += nth)
-			vp[1 - cv][e] = a.Ahp[e] * ig - dg * vp[cv][e] - gg * vp[1 - cv][e];
+		minres_v_update<VI>(nn, ne, tid, nth, a.Kd, vu[cv], vu[1 - cv], H.lv[0].b, a.Ahp, vp[cv], vp[1 - cv], ig, dg, gg);
 		sy.sync();
-		const double gn2 = block_precond(a, sm, sy, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv]);
+		const double gn2 = block_precond(a, sm, sy, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv], a.mzpt[1 - cv],
+		                                 true);
 		const double gam_next = sqrt(fmax(gn2, 0.0));
 		// Givens rotations
 		const double a0 = c_cur * delta - c_prev * s_cur * gam;
@@ -749,22 +955,8 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		const double c_next = a0 / a1, s_next = gam_next / a1;
 		// w(j+1) = (z~(j) - a3 w(j-1) - a2 w(j)) / a1 into w(j-1)'s buffer; x += c_next eta w(j+1)
 		const double ia1 = 1.0 / a1, step = c_next * eta;
-		for (int A = tid; A < nn; A += nth) {
-			const VI z = zu[cv][A];
-			const double2 wo = wu[1 - cw][A], w = wu[cw][A];
-			const double2 wn = make_double2(((double)z.x * ig - a3 * wo.x - a2 * w.x) * ia1,
-			                                ((double)z.y * ig - a3 * wo.y - a2 * w.y) * ia1);
-			wu[1 - cw][A] = wn;
-			double2 x = a.dd[A];
-			x.x += step * wn.x;
-			x.y += step * wn.y;
-			a.dd[A] = x;
-		}
-		for (int e = tid; e < ne; e += nth) {
-			const double wn = (zp[cv][e] * ig - a3 * wp[1 - cw][e] - a2 * wp[cw][e]) * ia1;
-			wp[1 - cw][e] = wn;
-			a.dpv[e] += step * wn;
-		}
+		minres_w_update<VI>(nn, ne, tid, nth, zu[cv], wu[1 - cw], wu[cw], a.dd, zp[cv], wp[1 - cw], wp[cw], a.dpv, ig,
+		                    a3, a2, ia1, step);
 		eta = -s_next * eta;
 		it++;
 		cv = 1 - cv;
@@ -782,7 +974,9 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		}
 		if (!(fabs(eta) > rtol * eta0) || !(gam > 0.0))
 			break;
-		sy.sync();
+		// no barrier here: the next operator pass reads z(j+1) and z_p(j+1),
+		// complete since the reduction in block_precond, and touches none of
+		// the vectors the updates above wrote
 	}
 	sy.sync();
 	return it;
@@ -850,7 +1044,7 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 			if (!(m & 2u))
 				s += g1 * g1 / kd.y;
 		}
-		a.bab[morton(ex, ez)] = s;
+		a.bab[morton(ex, ez)] = 1.0 / s;   // the solvers multiply by 1/BAB
 	}
 	if (sy.leader())
 		coarse_build<TI>(H);
@@ -957,7 +1151,7 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 		while (cycle < a.max_outer && rnorm > a.outer_rtol * rnorm0 && rnorm > 0.0) {
 			double rz[2] = {0.0, 0.0};
 			for (int e = tid; e < ne; e += nth) {
-				const double z = r1[e] / a.bab[e];
+				const double z = r1[e] * a.bab[e];
 				z1[e] = z;
 				rz[0] += r1[e] * z;
 				if (cycle > 0)

@@ -31,23 +31,50 @@ struct TileSmem {
 constexpr int kSmemBytes = sizeof(TileSmem<double>) > sizeof(TileSmem<float>) ? sizeof(TileSmem<double>)
                                                                                 : sizeof(TileSmem<float>);
 
-enum { PASS_MATVEC = 0, PASS_RESID = 1, PASS_SMOOTH = 2 };
+enum { PASS_MATVEC = 0, PASS_RESID = 1, PASS_SMOOTH = 2, PASS_STOKES = 3 };
 
 // How a tile pass forms its input x at a node:
 //   XS_PLAIN    x
 //   XS_ZERO     omega D^-1 b         (the first Jacobi sweep from a zero guess)
 //   XS_PROLONG  x + P xc             (coarse-grid correction, bilinear P)
-// Fusing the last two into the next tile pass saves a grid barrier and a
-// pass over memory on every multigrid level.
-enum { XS_PLAIN = 0, XS_ZERO = 1, XS_PROLONG = 2 };
+//   XS_ZERO_R   omega D^-1 b with b = P^T r_f formed from the finer level's
+//               residual (xc = r_f, nc = its nodes per side); the pass also
+//               writes b for its own nodes (bout), for the level's later passes
+// Fusing these into the next tile pass saves a grid barrier and a pass over
+// memory on every multigrid level.
+enum { XS_PLAIN = 0, XS_ZERO = 1, XS_PROLONG = 2, XS_ZERO_R = 3 };
+
+// (P^T r_f) at coarse node (cx, cz): full weighting 1, 1/2, 1/4 over the 3 x 3
+// fine nodes around (2 cx, 2 cz), in restrict_res's order; unmasked.
+template <class T, class V>
+__device__ __forceinline__ V restrict_at(const V *__restrict__ rf, int nf, int cx, int cz)
+{
+	T su = 0, sw = 0;
+#pragma unroll
+	for (int dx = -1; dx <= 1; dx++)
+#pragma unroll
+		for (int dz = -1; dz <= 1; dz++) {
+			const int fx = 2 * cx + dx, fz = 2 * cz + dz;
+			if (fx < 0 || fx >= nf || fz < 0 || fz >= nf)
+				continue;
+			const T wgt = (dx == 0 ? T(1) : T(0.5)) * (dz == 0 ? T(1) : T(0.5));
+			const V r = rf[fz + fx * nf];
+			su += wgt * r.x;
+			sw += wgt * r.y;
+		}
+	V o;
+	o.x = su;
+	o.y = sw;
+	return o;
+}
 
 template <class T, class V>
 __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__restrict__ x, const V *__restrict__ b,
                                    const V *__restrict__ invD, T omega, const V *__restrict__ xc, int nc)
 {
 	V v;
-	if (xs == XS_ZERO) {
-		const V bv = b[A], dv = invD[A];
+	if (xs == XS_ZERO || xs == XS_ZERO_R) {
+		const V bv = xs == XS_ZERO ? b[A] : restrict_at<T, V>(xc, nc, gx, gz), dv = invD[A];
 		v.x = omega * dv.x * bv.x;
 		v.y = omega * dv.y * bv.y;
 	} else {
@@ -66,13 +93,23 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 //   MATVEC: out = A x            (*dot = this thread's share of x.(A x) when dot != nullptr)
 //   RESID:  out = b - A x
 //   SMOOTH: out = x + omega D^-1 (b - A x)
+//           (*dot = this thread's share of out.dotv when dot != nullptr)
+//   STOKES: out64 = A x + G gp, formed in T and widened to FP64, G from the
+//           element pressures gp (Morton order, in T) and the corner
+//           coefficients (gt0, gt1) of the fine uniform mesh; *dot = this
+//           thread's share of x.out64 in FP64 (the velocity rows of the Stokes
+//           operator applied to (x, gp), and their product with x)
 // x at Dirichlet dofs is read as 0 and out is 0 there.
 template <class T, class V>
 __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, const unsigned char *__restrict__ mask,
                                        const T *__restrict__ eta, const V *__restrict__ x,
                                        const V *__restrict__ b, const V *__restrict__ invD, V *__restrict__ out,
                                        int mode, T omega, double *dot, int xs = XS_PLAIN,
-                                       const V *__restrict__ xc = nullptr, int nc = 0)
+                                       const V *__restrict__ xc = nullptr, int nc = 0,
+                                       const double2 *__restrict__ dotv = nullptr,
+                                       const T *__restrict__ gp = nullptr, const T *gt0 = nullptr,
+                                       const T *gt1 = nullptr, double2 *__restrict__ out64 = nullptr,
+                                       V *__restrict__ bout = nullptr)
 {
 	typedef TileSmem<T> SM;
 	constexpr int TX = SM::TX, PX = SM::PX, PZ = SM::PZ, EX = SM::EX, EZ = SM::EZ;
@@ -131,9 +168,18 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 #pragma unroll
 		for (int j = 0; j < NPT; j++) {
 			const int gx = ix0 + lx0 + 8 * j, gz = iz0 + lz;
-			if (gx < n && gz < n && mode != PASS_MATVEC) {
+			if (gx < n && gz < n && (mode == PASS_RESID || mode == PASS_SMOOTH)) {
 				const int A = gz + gx * n;
-				eb[j] = b[A];
+				if (xs == XS_ZERO_R) {
+					const unsigned m = mask[A];
+					V bv = restrict_at<T, V>(xc, nc, gx, gz);
+					bv.x = (m & 1u) ? T(0) : bv.x;
+					bv.y = (m & 2u) ? T(0) : bv.y;
+					eb[j] = bv;
+					bout[A] = bv;
+				} else {
+					eb[j] = b[A];
+				}
 				if (mode == PASS_SMOOTH)
 					ed[j] = invD[A];
 			}
@@ -199,6 +245,23 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 				fw = 0;
 			const T xu = S.u[px][pz], xw = S.w[px][pz];   // x as this pass formed it (0 on Dirichlet dofs)
 			V o;
+			if (mode == PASS_STOKES) {
+				// (G gp) at this node: its up to 4 elements, in gmul64's order
+				const int eox[4] = {gx - 1, gx - 1, gx, gx}, eoz[4] = {gz - 1, gz, gz, gz - 1};
+#pragma unroll
+				for (int q = 0; q < 4; q++) {
+					const int ex = eox[q], ez = eoz[q];
+					if (ex < 0 || ex >= N || ez < 0 || ez >= N)
+						continue;
+					const T se = gp[morton(ex, ez)];
+					fu += gt0[ea[q]] * se;
+					fw += gt1[ea[q]] * se;
+				}
+				const double2 az = make_double2((m & 1u) ? 0.0 : (double)fu, (m & 2u) ? 0.0 : (double)fw);
+				out64[A] = az;
+				dacc += az.x * (double)xu + az.y * (double)xw;
+				continue;
+			}
 			if (mode == PASS_MATVEC) {
 				o.x = fu;
 				o.y = fw;
@@ -210,6 +273,10 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 			} else {
 				o.x = (m & 1u) ? T(0) : xu + omega * ed[j].x * (eb[j].x - fu);
 				o.y = (m & 2u) ? T(0) : xw + omega * ed[j].y * (eb[j].y - fw);
+				if (dot) {
+					const double2 v = dotv[A];
+					dacc += (double)o.x * v.x + (double)o.y * v.y;
+				}
 			}
 			out[A] = o;
 		}

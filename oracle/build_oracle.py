@@ -19,13 +19,17 @@ def build():
     deps = [SRC, os.path.join(IC_DIR, "mclg_ic.h")]
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) > os.path.getmtime(d) for d in deps):
         return LIB
-    base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-I" + IC_DIR, SRC, "-o", LIB,
+    # built beside the library and renamed over it, so that a process that has
+    # the old one loaded keeps a consistent file
+    tmp = LIB + f".{os.getpid()}.tmp"
+    base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-I" + IC_DIR, SRC, "-o", tmp,
             "-lm"]
     p = subprocess.run(base[:1] + ["-fopenmp"] + base[1:], capture_output=True, text=True)
     if p.returncode != 0:
         p = subprocess.run(base, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError("oracle build failed:\n" + p.stderr)
+    os.replace(tmp, LIB)
     return LIB
 
 

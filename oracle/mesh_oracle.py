@@ -134,14 +134,23 @@ def _compact(v):
 
 
 class UniformMesh:
-    """Finest level of the uniform mesh of `cfg` (develop_mode=0, one rank)."""
+    """Finest level of the uniform mesh of `cfg` (develop_mode=0, one rank).
 
-    def __init__(self, cfg):
+    With `level` below cfg.level the mesh is the uniform grid of that level
+    (2**(level-1) elements per side) and the seeded initial temperature is
+    drawn with the node ids of cfg.level's grid, as the engine draws it for a
+    coarse uniform base inside a finer tree."""
+
+    def __init__(self, cfg, level=None):
         if cfg.develop_mode != 0 or cfg.nprox * cfg.nproz != 1 or cfg.AMR != 0:
             raise ValueError("UniformMesh covers develop_mode=0 on one rank without AMR")
         self.cfg = cfg
-        self.max_level = cfg.level
-        fl = cfg.level - 1
+        level = cfg.level if level is None else level
+        if not 1 <= level <= cfg.level:
+            raise ValueError(f"level {level} outside 1..{cfg.level}")
+        self.max_level = level
+        self._ic_scale = 1 << (cfg.level - level)
+        fl = level - 1
         N = 1 << fl
         self.N = N
         self.gnox = self.gnoz = N + 1
@@ -201,6 +210,9 @@ class UniformMesh:
         X = np.ascontiguousarray(self._arr["X"])
         node = self._arr["node"]
         nn = node.size
+        if self._ic_scale > 1:            # the node ids of the finer grid the field is keyed by
+            n, k, nf = self.N + 1, self._ic_scale, self.N * self._ic_scale + 1
+            node = np.ascontiguousarray(((node % n) * k + (node // n) * k * nf).astype(np.int32))
         T = np.zeros(nn)
         dpar = np.array([cfg.model_length, cfg.model_height, cfg.T_mantle, cfg.T_mantle_perturb, cfg.ic_noise,
                          cfg.ic_bl_thickness, cfg.ic_mode_amp])

@@ -32,6 +32,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1262,18 +1263,39 @@ static void assemble_coarse(orc *o)
 	}
 }
 
+static double wall_s(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 /* One time step of Main.c:58-64 (no output).  stats: uzawa, cg, heat cycles,
- * dt, model_time, residual momentum, residual continuity. */
+ * dt, model_time, residual momentum, residual continuity, then the wall
+ * seconds of the assembly (buoyancy .. K/F/G), of the Stokes solve and of the
+ * temperature update. */
 void orc_step(orc *o, double *stats)
 {
+	double t0 = wall_s(), t1, t2;
 	buoyancy_force(o);
 	viscosity_step(o);
 	assemble_stokes(o);
 	assemble_coarse(o);
+	t1 = wall_s();
 	solve_velocity_pressure(o);
+	t2 = wall_s();
 	update_temperature(o);
 	stats[0] = o->uzawa_cycles; stats[1] = o->cg_cycles; stats[2] = o->heat_cycles;
 	stats[3] = o->dt; stats[4] = o->model_time; stats[5] = o->res_m; stats[6] = o->res_c;
+	stats[7] = t1 - t0; stats[8] = t2 - t1; stats[9] = wall_s() - t2;
+}
+
+/* The caps of the Uzawa loop and of its inner CG (max_citcom_cycle,
+ * max_cg_cycle); for bounded timing samples of the CPU baseline. */
+void orc_set_caps(orc *o, int max_citcom, int max_cg)
+{
+	o->max_citcom = max_citcom;
+	o->max_cg = max_cg;
 }
 
 /* The Stokes half only (buoyancy .. solve), for operator-level checks. */

@@ -52,6 +52,8 @@ def lib():
         _L.orc_cg_sample.argtypes = [vp, C.c_int]
         _L.orc_mg_attach.restype = C.c_int
         _L.orc_mg_attach.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+        _L.orc_set_caps.restype = None
+        _L.orc_set_caps.argtypes = [vp, C.c_int, C.c_int]
         _L.orc_initial_temperature.restype = None
         _L.orc_initial_temperature.argtypes = [C.c_int, vp, vp, C.c_uint64, C.c_int, vp, vp, vp]
     return _L
@@ -71,15 +73,16 @@ class Oracle:
     initial temperature, as in the reference) and the transfer maps of
     oracle/mg_oracle.py."""
 
-    def __init__(self, cfg, threads=1, leaves=None, standalone=False):
+    def __init__(self, cfg, threads=1, leaves=None, standalone=False, mesh_level=None):
         if standalone:
-            # uniform meshes from oracle/mesh_oracle.py: the engine's library is not loaded
+            # uniform meshes from oracle/mesh_oracle.py: the engine's library is not loaded;
+            # mesh_level < cfg.level gives the uniform grid of that level (seeded T keyed by cfg.level's grid)
             import mesh_oracle
             if isinstance(cfg, (str, os.PathLike)):
                 cfg = mesh_oracle.read_input(cfg)
             if leaves is not None or cfg.solver == b"mg":
                 raise ValueError("the standalone oracle covers uniform meshes with the cg/jc/gs solvers")
-            m = mesh_oracle.UniformMesh(cfg)
+            m = mesh_oracle.UniformMesh(cfg, level=mesh_level)
         else:
             from mantle_convection_lab_gb300.api import Config, Mesh
             if isinstance(cfg, (str, os.PathLike)):
@@ -180,13 +183,18 @@ class Oracle:
         lib().orc_set_T(self._o, _p(self._T))
 
     def step(self):
-        st = np.zeros(7)
+        st = np.zeros(10)
         lib().orc_step(self._o, _p(st))
         return {"uzawa_cycles": int(st[0]), "cg_cycles": int(st[1]), "heat_cg_cycles": int(st[2]),
-                "dt": st[3], "model_time": st[4], "res_m": st[5], "res_c": st[6]}
+                "dt": st[3], "model_time": st[4], "res_m": st[5], "res_c": st[6], "s_assembly": st[7],
+                "s_solve": st[8], "s_heat": st[9]}
+
+    def set_caps(self, max_citcom, max_cg):
+        """max_citcom_cycle and max_cg_cycle of the following steps."""
+        lib().orc_set_caps(self._o, int(max_citcom), int(max_cg))
 
     def stokes(self):
-        st = np.zeros(7)
+        st = np.zeros(10)
         lib().orc_stokes(self._o, _p(st))
         return {"uzawa_cycles": int(st[0]), "cg_cycles": int(st[1]), "res_m": st[5], "res_c": st[6]}
 
