@@ -77,8 +77,10 @@ typedef struct mclg_config {
 	int max_citcom_cycle;    /* (375) */
 	int max_cg_cycle;        /* (200) */
 	int zero_P;              /* (1) */
-	int lg_mul, grain_damage; /* must be 0: the Lagrange path is out of scope; the grain-size
-	                             path is in the CPU oracle, not yet on the device */
+	int lg_mul, grain_damage; /* lg_mul must be 0 (the Lagrange-multiplier path is out of scope);
+	                             grain_damage=1 runs the grain-size rheology after the viscosity,
+	                             accepted on single-level meshes with precision=fp64 and solver
+	                             "cg" or "jc" (Grain_size_evolution.c:3-152) */
 	char old_T_file[1024];
 	int old_T_timestep;
 	/* seeded synthetic initial temperature (T_ini=-2), see mclg_ic.h */
@@ -113,7 +115,7 @@ typedef struct mclg_config {
 	int mg_finest_iteration; /* Gauss-Seidel sweeps before restriction (4)  Input.c:65 */
 	int mg_coarse_iteration; /* Gauss-Seidel sweeps after prolongation (4)  Input.c:64 */
 	/* grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-123): the clip of
-	 * the viscosity it sets; read for the CPU oracle, the engine rejects grain_damage=1 */
+	 * the viscosity it sets */
 	double lowest_vis, highest_vis;   /* (1.0, 1.0)  Input.c:58-59 */
 } mclg_config;
 

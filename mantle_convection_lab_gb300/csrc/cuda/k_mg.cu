@@ -378,7 +378,7 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 			if (l >= 1)
 				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, nullptr, L.invD, x, PASS_SMOOTH, H.omega,
 				                nullptr, XS_ZERO_R, H.lv[l - 1].r, H.lv[l - 1].n, nullptr, nullptr, nullptr, nullptr,
-				                nullptr, L.b);
+				                L.b);
 			else
 				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr,
 				                XS_ZERO);
@@ -653,32 +653,11 @@ __device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask
 // Separate functions so that their registers do not compete with the solver's
 // state; every load of a trip is issued before its arithmetic.
 
-// (G^T u)_e in TI for a TI velocity field (free dofs only), in gtmul64_elem's order.
-template <class TI, class V>
-__device__ __forceinline__ TI gtmul_elem_ti(int N0, const unsigned char *mask, const TI *g0, const TI *g1,
-                                            const V *u, int ex, int ez)
-{
-	const int n = N0 + 1;
-	const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
-	TI s = 0;
-#pragma unroll
-	for (int c = 0; c < 4; c++) {
-		const int a = kSortedCorner[c];
-		const V ua = u[cn[a]];
-		const unsigned m = mask[cn[a]];
-		if (!(m & 1u))
-			s += g0[a] * ua.x;
-		if (!(m & 2u))
-			s += g1[a] * ua.y;
-	}
-	return s;
-}
-
-// Ahp = G^T z_u per element (Morton order), formed in TI like the operator's
-// K z_u; returns this thread's share of Ahp.z_p in FP64.
-template <class TI, class VI>
-__device__ __noinline__ double minres_gt_dot(int N0, const unsigned char *__restrict__ mask, const TI *g0,
-                                             const TI *g1, const VI *__restrict__ zu, const double *__restrict__ zp,
+// Ahp = G^T z_u per element (Morton order), in FP64; returns this thread's
+// share of Ahp.z_p.
+template <class VI>
+__device__ __noinline__ double minres_gt_dot(int N0, const unsigned char *__restrict__ mask, const GTab &gt,
+                                             const VI *__restrict__ zu, const double *__restrict__ zp,
                                              double *__restrict__ Ahp, int tid, int nth)
 {
 	const int ne = N0 * N0;
@@ -692,7 +671,7 @@ __device__ __noinline__ double minres_gt_dot(int N0, const unsigned char *__rest
 			if (e < ne) {
 				const int ex = e / N0, ez = e - ex * N0;
 				me[u] = morton(ex, ez);
-				t[u] = (double)gtmul_elem_ti<TI, VI>(N0, mask, g0, g1, zu, ex, ez);
+				t[u] = gtmul_elem_t(N0, mask, gt, zu, ex, ez);
 				zpe[u] = zp[me[u]];
 			}
 		}
@@ -819,11 +798,9 @@ __device__ __noinline__ void minres_w_update(int nn, int ne, int tid, int nth, c
 	}
 }
 
-// z_p = v_p / BAB (ibab = 1/BAB), also into zpt in TI; returns this thread's
-// share of z_p.v_p.
-template <class TI>
+// z_p = v_p / BAB (ibab = 1/BAB); returns this thread's share of z_p.v_p.
 __device__ __noinline__ double precond_pressure(int ne, int tid, int nth, const double *__restrict__ vp,
-                                                const double *__restrict__ ibab, double *zp, TI *zpt)
+                                                const double *__restrict__ ibab, double *__restrict__ zp)
 {
 	double acc = 0.0;
 	for (int e0 = tid; e0 < ne; e0 += kVecU * nth) {
@@ -842,7 +819,6 @@ __device__ __noinline__ double precond_pressure(int ne, int tid, int nth, const 
 			if (e < ne) {
 				const double z = v[u] * ib[u];
 				zp[e] = z;
-				zpt[e] = (TI)z;
 				acc += z * v[u];
 			}
 		}
@@ -857,7 +833,7 @@ __device__ __noinline__ double precond_pressure(int ne, int tid, int nth, const 
 // right-hand side (H.lv[0].b) and synchronised.
 template <class TI>
 __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, const double2 *vu, const double *vp,
-                                typename V2T<TI>::t *zu, double *zp, TI *zpt, bool converted = false)
+                                typename V2T<TI>::t *zu, double *zp, bool converted = false)
 {
 	typedef typename V2T<TI>::t VI;
 	const MGHier<TI> &H = a.H;
@@ -876,7 +852,7 @@ __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, Sync &sy
 	}
 	double dot[1] = {0.0};
 	vcycle<TI>(sy, sm, H, bI, zu, vu, &dot[0]);   // the last sweep forms <z_u, v_u>
-	dot[0] += precond_pressure<TI>(ne, tid, nth, vp, a.bab, zp, zpt);
+	dot[0] += precond_pressure(ne, tid, nth, vp, a.bab, zp);
 	sy.reduce<1>(dot);
 	return dot[0];
 }
@@ -918,7 +894,7 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		a.dpv[e] = 0.0;
 	}
 	sy.sync();
-	double gam2 = block_precond(a, sm, sy, vu[0], vp[0], zu[0], zp[0], a.mzpt[0]);
+	double gam2 = block_precond(a, sm, sy, vu[0], vp[0], zu[0], zp[0]);
 	if (!(gam2 > 0.0))
 		return 0;
 	double gam = sqrt(gam2), gam_prev = 1.0;
@@ -930,8 +906,8 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		// product with z_u formed in the same pass, and G^T z_u per element
 		double dl[1] = {0.0};
 		tile_pass<TI, VI>(sm, sy.part(true), L0.N, L0.mask, L0.eta, zu[cv], nullptr, nullptr, kz, PASS_STOKES, TI(0),
-		                  &dl[0], XS_PLAIN, nullptr, 0, nullptr, a.mzpt[cv], a.gti0, a.gti1, a.Kd);
-		dl[0] += minres_gt_dot<TI, VI>(N0, a.mask0, a.gti0, a.gti1, zu[cv], zp[cv], a.Ahp, tid, nth);
+		                  &dl[0], XS_PLAIN, nullptr, 0, nullptr, zp[cv], &gt, a.Kd);
+		dl[0] += minres_gt_dot<VI>(N0, a.mask0, gt, zu[cv], zp[cv], a.Ahp, tid, nth);
 		sy.reduce<1>(dl);
 		const double delta = dl[0] / (gam * gam);
 		// v(j+1) = A z~ - (delta/gam) v(j) - (gam/gam_prev) v(j-1), into v(j-1)'s
@@ -939,8 +915,7 @@ __device__ int minres_correction(const MGArgs<TI> &a, unsigned char *sm, Sync &s
 		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
 		minres_v_update<VI>(nn, ne, tid, nth, a.Kd, vu[cv], vu[1 - cv], H.lv[0].b, a.Ahp, vp[cv], vp[1 - cv], ig, dg, gg);
 		sy.sync();
-		const double gn2 = block_precond(a, sm, sy, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv], a.mzpt[1 - cv],
-		                                 true);
+		const double gn2 = block_precond(a, sm, sy, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv], true);
 		const double gam_next = sqrt(fmax(gn2, 0.0));
 		// Givens rotations
 		const double a0 = c_cur * delta - c_prev * s_cur * gam;

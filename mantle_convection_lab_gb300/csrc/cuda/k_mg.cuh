@@ -66,8 +66,6 @@ struct MGArgs {
 	int method;                  // correction solve: 0 Uzawa with inner MG-PCG, 1 MINRES (block-diagonal preconditioner)
 	double2 *mv[2], *mw[2];      // MINRES Lanczos and direction vectors, velocity part (z_u lives in TI)
 	double *mvp[2], *mzp[2], *mwp[2]; // Lanczos, preconditioned and direction vectors, pressure part (Morton)
-	TI *mzpt[2];                 // MINRES: the preconditioned pressure z_p in TI, for G z_p inside the TI operator
-	TI gti0[4], gti1[4];         // the G coefficients of gt in TI
 	const double2 *d_alt;        // second candidate guess (previous solution) or null
 	const double *p_alt;
 	int guess_force;             // keep (d, p) without judging it against (d_alt, p_alt)

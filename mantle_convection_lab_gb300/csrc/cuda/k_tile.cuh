@@ -94,11 +94,12 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 //   RESID:  out = b - A x
 //   SMOOTH: out = x + omega D^-1 (b - A x)
 //           (*dot = this thread's share of out.dotv when dot != nullptr)
-//   STOKES: out64 = A x + G gp, formed in T and widened to FP64, G from the
-//           element pressures gp (Morton order, in T) and the corner
-//           coefficients (gt0, gt1) of the fine uniform mesh; *dot = this
-//           thread's share of x.out64 in FP64 (the velocity rows of the Stokes
-//           operator applied to (x, gp), and their product with x)
+//   STOKES: out64 = A x + G gp, with G gp in FP64 from the element pressures
+//           gp (Morton order) and the corner coefficients gt of the fine
+//           uniform mesh; *dot = this thread's share of x.out64 (the velocity
+//           rows of the Stokes operator applied to (x, gp), and their product
+//           with x).  G stays in FP64: applied in FP32 as well, it raised the
+//           MINRES iterations per step by half.
 // x at Dirichlet dofs is read as 0 and out is 0 there.
 template <class T, class V>
 __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, const unsigned char *__restrict__ mask,
@@ -107,9 +108,8 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
                                        int mode, T omega, double *dot, int xs = XS_PLAIN,
                                        const V *__restrict__ xc = nullptr, int nc = 0,
                                        const double2 *__restrict__ dotv = nullptr,
-                                       const T *__restrict__ gp = nullptr, const T *gt0 = nullptr,
-                                       const T *gt1 = nullptr, double2 *__restrict__ out64 = nullptr,
-                                       V *__restrict__ bout = nullptr)
+                                       const double *__restrict__ gp = nullptr, const GTab *gt = nullptr,
+                                       double2 *__restrict__ out64 = nullptr, V *__restrict__ bout = nullptr)
 {
 	typedef TileSmem<T> SM;
 	constexpr int TX = SM::TX, PX = SM::PX, PZ = SM::PZ, EX = SM::EX, EZ = SM::EZ;
@@ -246,18 +246,19 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 			const T xu = S.u[px][pz], xw = S.w[px][pz];   // x as this pass formed it (0 on Dirichlet dofs)
 			V o;
 			if (mode == PASS_STOKES) {
-				// (G gp) at this node: its up to 4 elements, in gmul64's order
+				// (G gp) at this node: its up to 4 elements, as gmul64
+				double s0 = 0.0, s1 = 0.0;
 				const int eox[4] = {gx - 1, gx - 1, gx, gx}, eoz[4] = {gz - 1, gz, gz, gz - 1};
 #pragma unroll
 				for (int q = 0; q < 4; q++) {
 					const int ex = eox[q], ez = eoz[q];
 					if (ex < 0 || ex >= N || ez < 0 || ez >= N)
 						continue;
-					const T se = gp[morton(ex, ez)];
-					fu += gt0[ea[q]] * se;
-					fw += gt1[ea[q]] * se;
+					const double se = gp[morton(ex, ez)];
+					s0 += gt->g0[ea[q]] * se;
+					s1 += gt->g1[ea[q]] * se;
 				}
-				const double2 az = make_double2((m & 1u) ? 0.0 : (double)fu, (m & 2u) ? 0.0 : (double)fw);
+				const double2 az = make_double2((m & 1u) ? 0.0 : (double)fu + s0, (m & 2u) ? 0.0 : (double)fw + s1);
 				out64[A] = az;
 				dacc += az.x * (double)xu + az.y * (double)xw;
 				continue;

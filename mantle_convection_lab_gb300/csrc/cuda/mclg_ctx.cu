@@ -407,8 +407,6 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 			}
 			a.gt.g0[k] = g0;
 			a.gt.g1[k] = g1;
-			a.gti0[k] = (TI)g0;
-			a.gti1[k] = (TI)g1;
 		}
 	}
 	a.vis = c->vis;
@@ -434,7 +432,6 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 			CK(mg_alloc(c, &a.mvp[k], ne));
 			CK(mg_alloc(c, &a.mzp[k], ne));
 			CK(mg_alloc(c, &a.mwp[k], ne));
-			CK(mg_alloc(c, &a.mzpt[k], ne));
 		}
 	}
 	a.red.part = c->red_part;
