@@ -117,6 +117,9 @@ typedef struct mclg_config {
 	/* grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-123): the clip of
 	 * the viscosity it sets */
 	double lowest_vis, highest_vis;   /* (1.0, 1.0)  Input.c:58-59 */
+	/* converged solvers on uniform meshes: damped-Jacobi sweeps per V-cycle side
+	 * on the levels below the two finest (0: mg_smooth) */
+	int mg_smooth_coarse;
 } mclg_config;
 
 typedef struct mclg_step_stats {

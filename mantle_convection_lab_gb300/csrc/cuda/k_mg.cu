@@ -247,21 +247,6 @@ __device__ void prolong_add(Part pt, const MGLevel<T> &F, const V *xf, V *out, c
 	}
 }
 
-// x = omega D^-1 b (first smoothing sweep from a zero guess).
-template <class T, class V>
-__device__ void jacobi_first(Part pt, int n, const V *b, const V *invD, V *x, T omega)
-{
-	int i0, st;
-	span(pt, i0, st);
-	for (int A = i0; A < n * n; A += st) {
-		const V bv = b[A], dv = invD[A];
-		V o;
-		o.x = omega * dv.x * bv.x;
-		o.y = omega * dv.y * bv.y;
-		x[A] = o;
-	}
-}
-
 // ---- coarsest grid: dense inverse -------------------------------------------
 // Assemble the coarsest operator densely (FP64), put identity rows on the
 // Dirichlet dofs and invert it by Gauss-Jordan; block 0 only.
@@ -365,26 +350,29 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 	typedef typename V2T<T>::t V;
 	const MGLevel<T> &L = H.lv[l];
 	const V *b = (l == 0) ? rhs0 : L.b;
+	const int nu = l < H.lfine ? H.nu : H.nu_c;
+	// below the finest level the right-hand side P^T r of the finer level is
+	// formed in this level's first pass (and stored for its later passes)
+	const int xs0 = l >= 1 ? XS_ZERO_R : XS_ZERO;
+	const V *rf = l >= 1 ? H.lv[l - 1].r : nullptr;
+	const int nf = l >= 1 ? H.lv[l - 1].n : 0;
+	V *bo = l >= 1 ? L.b : nullptr;
 	V *x = L.xa, *xt = L.xb;
-	if (H.nu == 1) {
+	if (nu == 1) {
+		// one sweep from zero, x = omega D^-1 b, formed inside the residual pass
 		if (active) {
-			jacobi_first<T, V>(sy.part(grid), L.n, b, L.invD, x, H.omega);
+			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, L.r, PASS_RESID, H.omega, nullptr,
+			                xs0, rf, nf, nullptr, nullptr, nullptr, nullptr, bo, x);
 			barrier(sy, grid);
 		}
 	} else {
-		// sweep 1 (from zero) fused into sweep 2; below the finest level the
-		// right-hand side P^T r of the finer level is formed in the same pass
+		// sweep 1 (from zero) fused into sweep 2
 		if (active) {
-			if (l >= 1)
-				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, nullptr, L.invD, x, PASS_SMOOTH, H.omega,
-				                nullptr, XS_ZERO_R, H.lv[l - 1].r, H.lv[l - 1].n, nullptr, nullptr, nullptr, nullptr,
-				                L.b);
-			else
-				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr,
-				                XS_ZERO);
+			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr,
+			                xs0, rf, nf, nullptr, nullptr, nullptr, nullptr, bo);
 			barrier(sy, grid);
 		}
-		for (int s = 2; s < H.nu; s++) {
+		for (int s = 2; s < nu; s++) {
 			if (active) {
 				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, xt, PASS_SMOOTH, H.omega, nullptr);
 				barrier(sy, grid);
@@ -393,16 +381,16 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 			x = xt;
 			xt = tmp;
 		}
-	}
-	if (active) {
-		tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
-		barrier(sy, grid);
-		// the next level forms its right-hand side from L.r in its first sweep,
-		// except the coarsest (a dense solve) and single-sweep cycles
-		if (H.nu == 1 || l + 1 == H.nlev - 1) {
-			restrict_res<T, V>(sy.part(grid), L, H.lv[l + 1]);
+		if (active) {
+			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, L.r, PASS_RESID, H.omega, nullptr);
 			barrier(sy, grid);
 		}
+	}
+	// the next level forms its right-hand side from L.r in its first pass,
+	// except the coarsest (a dense solve)
+	if (active && l + 1 == H.nlev - 1) {
+		restrict_res<T, V>(sy.part(grid), L, H.lv[l + 1]);
+		barrier(sy, grid);
 	}
 	xcur[l] = x;
 }
@@ -421,9 +409,10 @@ __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
 	V *x = xcur[l];
 	V *xt = (x == L.xa) ? L.xb : L.xa;
 	const MGLevel<T> &C = H.lv[l + 1];
+	const int nu = l < H.lfine ? H.nu : H.nu_c;
 	// the coarse-grid correction x + P xc is formed inside the first post-smoothing sweep
-	for (int s = 0; s < H.nu; s++) {
-		const bool last = l == 0 && s == H.nu - 1;
+	for (int s = 0; s < nu; s++) {
+		const bool last = l == 0 && s == nu - 1;
 		V *dst = last ? out0 : xt;
 		double *dp = (last && dotv) ? dot : nullptr;
 		if (active) {

@@ -35,7 +35,8 @@ struct MGHier {
 	double *cwork;               // [cnd * 2*cnd] scratch for the inversion
 	int cnd;                     // 2 * n_coarsest^2
 	T omega;
-	int nu;
+	int nu;                      // Jacobi sweeps per side on levels below lfine
+	int nu_c, lfine;             // ... and on levels lfine and coarser
 	int eta_avg;                 // coarse viscosity: 0 injection, 1 full-weighted mean, 2 full-weighted log-mean
 	// inner CG vectors on level 0
 	typename V2T<T>::t *px, *pr, *pz, *pp, *pq;

@@ -91,7 +91,7 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 
 // One pass of y = A x over a level, with a fused epilogue:
 //   MATVEC: out = A x            (*dot = this thread's share of x.(A x) when dot != nullptr)
-//   RESID:  out = b - A x
+//   RESID:  out = b - A x        (with xout, x as formed is stored there too)
 //   SMOOTH: out = x + omega D^-1 (b - A x)
 //           (*dot = this thread's share of out.dotv when dot != nullptr)
 //   STOKES: out64 = A x + G gp, with G gp in FP64 from the element pressures
@@ -109,7 +109,8 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
                                        const V *__restrict__ xc = nullptr, int nc = 0,
                                        const double2 *__restrict__ dotv = nullptr,
                                        const double *__restrict__ gp = nullptr, const GTab *gt = nullptr,
-                                       double2 *__restrict__ out64 = nullptr, V *__restrict__ bout = nullptr)
+                                       double2 *__restrict__ out64 = nullptr, V *__restrict__ bout = nullptr,
+                                       V *__restrict__ xout = nullptr)
 {
 	typedef TileSmem<T> SM;
 	constexpr int TX = SM::TX, PX = SM::PX, PZ = SM::PZ, EX = SM::EX, EZ = SM::EZ;
@@ -271,6 +272,12 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 			} else if (mode == PASS_RESID) {
 				o.x = (m & 1u) ? T(0) : eb[j].x - fu;
 				o.y = (m & 2u) ? T(0) : eb[j].y - fw;
+				if (xout) {   // x as this pass formed it (the first sweep from zero)
+					V xv;
+					xv.x = xu;
+					xv.y = xw;
+					xout[A] = xv;
+				}
 			} else {
 				o.x = (m & 1u) ? T(0) : xu + omega * ed[j].x * (eb[j].x - fu);
 				o.y = (m & 2u) ? T(0) : xw + omega * ed[j].y * (eb[j].y - fw);

@@ -385,6 +385,8 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	CK(mg_alloc(c, &a.H.cwork, (size_t)a.H.cnd * 2 * a.H.cnd));
 	a.H.omega = (TI)c->cfg.mg_omega;
 	a.H.nu = c->cfg.mg_smooth < 1 ? 1 : c->cfg.mg_smooth;
+	a.H.nu_c = c->cfg.mg_smooth_coarse < 1 ? a.H.nu : c->cfg.mg_smooth_coarse;
+	a.H.lfine = 2;
 	a.H.eta_avg = c->cfg.mg_eta_avg;
 	const size_t nn0 = (size_t)n0 * n0, ne = (size_t)N0 * N0;
 	CK(mg_alloc(c, &a.H.px, nn0));

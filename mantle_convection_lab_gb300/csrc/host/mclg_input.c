@@ -320,6 +320,7 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_int(&pl, "mg_coarse_iteration", &c->mg_coarse_iteration, 4);
 	get_double(&pl, "lowest_vis", &c->lowest_vis, 1.0);
 	get_double(&pl, "highest_vis", &c->highest_vis, 1.0);
+	get_int(&pl, "mg_smooth_coarse", &c->mg_smooth_coarse, 0);
 	free(pl.e);
 	return MCLG_OK;
 }
