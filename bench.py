@@ -563,7 +563,10 @@ def run_ensemble(args, wl):
         mine_f = {f: m.get(f) for f in ("V0", "V1", "P", "T")}
         from mantle_convection_lab_gb300 import Model
         import numpy as np
-        lv = leaves_of(m, cfg_k) if amr_run else None
+        lv = None
+        if amr_run:   # a refined member's configuration names its base grid; its tree is levels deeper
+            cfg_k.level += int(levels[mine[k]])
+            lv = leaves_of(m, cfg_k)
         with Model(fp64_reference_config(cfg_k), leaves=lv) as ref:
             ref.set("T", T0[k])
             rs = ref.step()

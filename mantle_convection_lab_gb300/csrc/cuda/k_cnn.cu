@@ -7,12 +7,17 @@
 // Precision: BF16 weights (rounded from FP32 master copies after every Adam
 // step), FP32 activations, biases and accumulation.
 //
-// Tensors are [B][C][H][W] with W contiguous.  A convolution block covers a
-// 16 x 16 output tile with one thread per pixel; input channels stream
-// through shared memory in chunks of 16 together with their weights, stored
-// [ci][k][co] so that the weights of one tap load as float4 broadcasts.
-// The weight gradient is reduced in two deterministic stages (per-block
-// partials, then a fixed-order sum over blocks).
+// Tensors are [B][C][H][W] with W contiguous.  The convolutions (forward, and
+// backward-data with flipped weights) run on the tensor cores: a block covers a
+// 16 x 16 output tile as an implicit GEMM, M = 256 pixels, N = the output
+// channels, K = 9 taps x the input channels, in mma.sync.m16n8k16 steps with
+// BF16 operands and FP32 accumulation.  The input tile (with its halo) is
+// staged in shared memory as BF16, channels innermost, and the weights as
+// [tap][out][in]; both are padded so that the fragment loads of a warp fall
+// in 32 different banks.  So the convolution inputs (activations forward,
+// gradients backward) are rounded to BF16 as the weights are.
+// The weight gradient (FP32 inputs) is reduced in two deterministic stages
+// (per-block partials, then a fixed-order sum over blocks).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
@@ -29,8 +34,8 @@ struct mclg_cnn {
 	size_t off[mclg::kCnnMaxLayers];        // start of layer l in the flat parameter array: W[co][ci][9], b[co]
 	size_t nparam;
 	float *master, *grad, *m, *v;           // device, [nparam]
-	__nv_bfloat16 *wf[mclg::kCnnMaxLayers]; // forward weights  [ci][9][pad(cout)]
-	__nv_bfloat16 *wb[mclg::kCnnMaxLayers]; // backward weights [co][9 flipped][pad(cin)]
+	__nv_bfloat16 *wf[mclg::kCnnMaxLayers]; // forward weights  [9][co_pad(cout)][ci_pad(cin)]
+	__nv_bfloat16 *wb[mclg::kCnnMaxLayers]; // backward weights [9 flipped][co_pad(cin)][ci_pad(cout)]
 	long long adam_t;
 	float *part;                            // weight-gradient partials
 	size_t part_cap;
@@ -49,6 +54,11 @@ static int pad_channels(int c)
 	return c <= 4 ? 4 : c <= 8 ? 8 : c <= 16 ? 16 : c <= 32 ? 32 : 48;
 }
 
+// channel padding of the tensor-core convolution: K steps of 16 input
+// channels, N tiles of 8 output channels
+static int ci_pad(int c) { return c <= 16 ? 16 : 32; }
+static int co_pad(int c) { return c <= 8 ? 8 : c <= 16 ? 16 : 32; }
+
 static int cnn_fail(cudaError_t e, const char *what)
 {
 	mclg_set_error("%s: %s", what, cudaGetErrorString(e));
@@ -63,68 +73,104 @@ static int cnn_fail(cudaError_t e, const char *what)
 	} while (0)
 
 // ---- convolution (forward, and backward-data with flipped weights) -----------
-// out[b][o][y][x] = bias[o] + sum_c sum_k w[c][k][o] * in[b][c][y+ky-1][x+kx-1]
-// then ReLU (relu != 0) and/or a multiply by (mask > 0) (mask != null).
-template <int CO>
+// out[b][o][y][x] = bias[o] + sum_c sum_k w[k][o][c] * in[b][c][y+ky-1][x+kx-1]
+// (w and in rounded to BF16, FP32 accumulation), then ReLU (relu != 0) and/or
+// a multiply by (mask > 0) (mask != null).  CI >= Cin input channels (a
+// multiple of 16), CO >= Cout output channels (a multiple of 8).
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                               unsigned b0, unsigned b1)
+{
+	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+	             "{%0,%1,%2,%3};\n"
+	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	             : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int CI, int CO>
 __global__ void __launch_bounds__(256) k_conv3x3(const float *__restrict__ in, int Cin,
                                                  const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
                                                  float *__restrict__ out, int Cout, int H, int W, int relu,
                                                  const float *__restrict__ mask)
 {
-	__shared__ __align__(16) float s_in[kChunk * kHalo * kHalo];
-	__shared__ __align__(16) float s_w[kChunk * 9 * CO];
-	const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
+	// channel stride of a pixel (and of an output channel's weights) in shared
+	// memory: CI + 8 BF16 puts the 8 rows of a fragment in distinct banks
+	constexpr int SI = CI + 8, NT = CO / 8;
+	__shared__ __align__(16) __nv_bfloat16 s_in[kHalo * kHalo * SI];
+	__shared__ __align__(16) __nv_bfloat16 s_w[9 * CO * SI];
 	const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile, b = blockIdx.z;
-	float acc[CO];
+	for (int i = threadIdx.x; i < CI * kHalo * kHalo; i += blockDim.x) {
+		const int c = i / (kHalo * kHalo), r = i - c * kHalo * kHalo;
+		const int yy = r / kHalo, xx = r - yy * kHalo;
+		const int gy = y0 + yy - 1, gx = x0 + xx - 1;
+		float v = 0.f;
+		if (c < Cin && gy >= 0 && gy < H && gx >= 0 && gx < W)
+			v = in[((size_t)(b * Cin + c) * H + gy) * W + gx];
+		s_in[r * SI + c] = __float2bfloat16_rn(v);
+	}
+	for (int i = threadIdx.x; i < 9 * CO * CI; i += blockDim.x) {
+		const int kc = i / CI, c = i - kc * CI;
+		s_w[kc * SI + c] = w[i];
+	}
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int g = lane >> 2, t2 = (lane & 3) * 2;
+	float acc[2][NT][4];
 #pragma unroll
-	for (int j = 0; j < CO; j++)
-		acc[j] = 0.f;
-	for (int c0 = 0; c0 < Cin; c0 += kChunk) {
-		const int nc = min(kChunk, Cin - c0);
-		__syncthreads();
-		for (int i = threadIdx.x; i < nc * kHalo * kHalo; i += blockDim.x) {
-			const int ci = i / (kHalo * kHalo), r = i - ci * kHalo * kHalo;
-			const int yy = r / kHalo, xx = r - yy * kHalo;
-			const int gy = y0 + yy - 1, gx = x0 + xx - 1;
-			float v = 0.f;
-			if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-				v = in[((size_t)(b * Cin + c0 + ci) * H + gy) * W + gx];
-			s_in[i] = v;
-		}
-		for (int i = threadIdx.x; i < nc * 9 * CO; i += blockDim.x)
-			s_w[i] = __bfloat162float(w[(size_t)c0 * 9 * CO + i]);
-		__syncthreads();
-		for (int ci = 0; ci < nc; ci++) {
+	for (int m = 0; m < 2; m++)
 #pragma unroll
-			for (int k = 0; k < 9; k++) {
-				const int ky = k / 3, kx = k - 3 * (k / 3);
-				const float xv = s_in[ci * kHalo * kHalo + (ty + ky) * kHalo + tx + kx];
-				const float4 *wr = reinterpret_cast<const float4 *>(s_w + (ci * 9 + k) * CO);
+		for (int j = 0; j < NT; j++)
 #pragma unroll
-				for (int j = 0; j < CO / 4; j++) {
-					const float4 wv = wr[j];
-					acc[4 * j + 0] = fmaf(wv.x, xv, acc[4 * j + 0]);
-					acc[4 * j + 1] = fmaf(wv.y, xv, acc[4 * j + 1]);
-					acc[4 * j + 2] = fmaf(wv.z, xv, acc[4 * j + 2]);
-					acc[4 * j + 3] = fmaf(wv.w, xv, acc[4 * j + 3]);
-				}
+			for (int q = 0; q < 4; q++)
+				acc[m][j][q] = 0.f;
+	// warp w: output rows 2w and 2w+1, each an M tile of 16 pixels
+#pragma unroll 1
+	for (int k = 0; k < 9; k++) {
+		const int ky = k / 3, kx = k - 3 * (k / 3);
+#pragma unroll
+		for (int cb = 0; cb < CI; cb += 16) {
+			unsigned bfr[NT][2];
+#pragma unroll
+			for (int j = 0; j < NT; j++) {
+				const __nv_bfloat16 *wr = s_w + (k * CO + j * 8 + g) * SI + cb + t2;
+				bfr[j][0] = *reinterpret_cast<const unsigned *>(wr);
+				bfr[j][1] = *reinterpret_cast<const unsigned *>(wr + 8);
+			}
+#pragma unroll
+			for (int m = 0; m < 2; m++) {
+				const int py = 2 * warp + m;
+				const __nv_bfloat16 *r0 = s_in + ((py + ky) * kHalo + g + kx) * SI + cb + t2;
+				const __nv_bfloat16 *r1 = r0 + 8 * SI;
+				const unsigned a0 = *reinterpret_cast<const unsigned *>(r0);
+				const unsigned a1 = *reinterpret_cast<const unsigned *>(r1);
+				const unsigned a2 = *reinterpret_cast<const unsigned *>(r0 + 8);
+				const unsigned a3 = *reinterpret_cast<const unsigned *>(r1 + 8);
+#pragma unroll
+				for (int j = 0; j < NT; j++)
+					mma_bf16_16816(acc[m][j], a0, a1, a2, a3, bfr[j][0], bfr[j][1]);
 			}
 		}
 	}
-	const int x = x0 + tx, y = y0 + ty;
-	if (x >= W || y >= H)
-		return;
+	// D fragment: rows g (pixels x0+g) and g+8, columns t2, t2+1 of the N tile
 #pragma unroll
-	for (int j = 0; j < CO; j++) {
-		if (j < Cout) {
-			const size_t o = ((size_t)(b * Cout + j) * H + y) * W + x;
-			float v = acc[j] + (bias ? bias[j] : 0.f);
-			if (relu)
-				v = fmaxf(v, 0.f);
-			if (mask && !(mask[o] > 0.f))
-				v = 0.f;
-			out[o] = v;
-		}
+	for (int m = 0; m < 2; m++) {
+		const int y = y0 + 2 * warp + m;
+		if (y >= H)
+			continue;
+#pragma unroll
+		for (int j = 0; j < NT; j++)
+#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				const int x = x0 + g + (q >= 2 ? 8 : 0), o = j * 8 + t2 + (q & 1);
+				if (x >= W || o >= Cout)
+					continue;
+				const size_t idx = ((size_t)(b * Cout + o) * H + y) * W + x;
+				float v = acc[m][j][q] + (bias ? bias[o] : 0.f);
+				if (relu)
+					v = fmaxf(v, 0.f);
+				if (mask && !(mask[idx] > 0.f))
+					v = 0.f;
+				out[idx] = v;
+			}
 	}
 }
 
@@ -283,35 +329,38 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
 	}
 }
 
-// wf[c][k][o] = bf16(W[o][c][k]); wb[o][8-k][c] = bf16(W[o][c][k]); zero padding.
-__global__ void k_pack(const float *__restrict__ W, int Cin, int Cout, int COp, int CIp, __nv_bfloat16 *__restrict__ wf,
-                       __nv_bfloat16 *__restrict__ wb)
+// Weights of the tensor-core convolutions, zero padded:
+//   wf[k][o][c] = bf16(W[o][c][k])      o < co_pad(Cout) = NO, c < ci_pad(Cin) = NC
+//   wb[k][c][o] = bf16(W[o][c][8 - k])  c < co_pad(Cin) = BO,  o < ci_pad(Cout) = BC
+__global__ void k_pack(const float *__restrict__ W, int Cin, int Cout, int NO, int NC, int BO, int BC,
+                       __nv_bfloat16 *__restrict__ wf, __nv_bfloat16 *__restrict__ wb)
 {
-	const int nf = Cin * 9 * COp, nb = Cout * 9 * CIp;
+	const int nf = 9 * NO * NC, nb = 9 * BO * BC;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf + nb; i += gridDim.x * blockDim.x) {
 		if (i < nf) {
-			const int c = i / (9 * COp), r = i - c * 9 * COp, k = r / COp, o = r - k * COp;
-			wf[i] = __float2bfloat16_rn(o < Cout ? W[(o * Cin + c) * 9 + k] : 0.f);
+			const int k = i / (NO * NC), r = i - k * NO * NC, o = r / NC, c = r - o * NC;
+			wf[i] = __float2bfloat16_rn(o < Cout && c < Cin ? W[(o * Cin + c) * 9 + k] : 0.f);
 		} else {
 			const int j = i - nf;
-			const int o = j / (9 * CIp), r = j - o * 9 * CIp, kf = r / CIp, c = r - kf * CIp;
-			wb[j] = __float2bfloat16_rn(c < Cin ? W[(o * Cin + c) * 9 + (8 - kf)] : 0.f);
+			const int k = j / (BO * BC), r = j - k * BO * BC, c = r / BC, o = r - c * BC;
+			wb[j] = __float2bfloat16_rn(o < Cout && c < Cin ? W[(o * Cin + c) * 9 + (8 - k)] : 0.f);
 		}
 	}
 }
 
 // ---- launch helpers -----------------------------------------------------------
-static void conv_launch(const float *in, int Cin, const __nv_bfloat16 *w, int CO, const float *bias, float *out,
-                        int Cout, int B, int H, int W, int relu, const float *mask, cudaStream_t st)
+// w is packed for (ci_pad(Cin), co_pad(Cout)) as k_pack lays it out.
+static void conv_launch(const float *in, int Cin, const __nv_bfloat16 *w, const float *bias, float *out, int Cout,
+                        int B, int H, int W, int relu, const float *mask, cudaStream_t st)
 {
 	dim3 grid((W + kTile - 1) / kTile, (H + kTile - 1) / kTile, B);
-	switch (CO) {
-	case 4: k_conv3x3<4><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask); break;
-	case 8: k_conv3x3<8><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask); break;
-	case 16: k_conv3x3<16><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask); break;
-	case 32: k_conv3x3<32><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask); break;
-	default: k_conv3x3<48><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask); break;
-	}
+	const int ci = ci_pad(Cin), co = co_pad(Cout);
+#define CONV_TC(CI_, CO_) k_conv3x3<CI_, CO_><<<grid, 256, 0, st>>>(in, Cin, w, bias, out, Cout, H, W, relu, mask)
+	if (ci == 16)
+		co == 8 ? CONV_TC(16, 8) : co == 16 ? CONV_TC(16, 16) : CONV_TC(16, 32);
+	else
+		co == 8 ? CONV_TC(32, 8) : co == 16 ? CONV_TC(32, 16) : CONV_TC(32, 32);
+#undef CONV_TC
 }
 
 static size_t wgrad_smem(int Cin, int CO)
@@ -352,10 +401,10 @@ static cudaError_t wgrad_launch(const float *in, int Cin, const float *g, int Co
 static int pack_all(mclg_cnn *n)
 {
 	for (int l = 0; l < n->nl; l++) {
-		const int nb = n->cin[l] * 9 * pad_channels(n->cout[l]) + n->cout[l] * 9 * pad_channels(n->cin[l]);
-		k_pack<<<(nb + 255) / 256, 256, 0, n->st>>>(n->master + n->off[l], n->cin[l], n->cout[l],
-		                                            pad_channels(n->cout[l]), pad_channels(n->cin[l]), n->wf[l],
-		                                            n->wb[l]);
+		const int NO = co_pad(n->cout[l]), NC = ci_pad(n->cin[l]), BO = co_pad(n->cin[l]), BC = ci_pad(n->cout[l]);
+		const int nb = 9 * (NO * NC + BO * BC);
+		k_pack<<<(nb + 255) / 256, 256, 0, n->st>>>(n->master + n->off[l], n->cin[l], n->cout[l], NO, NC, BO, BC,
+		                                            n->wf[l], n->wb[l]);
 	}
 	CKC(cudaGetLastError());
 	return MCLG_OK;
@@ -404,9 +453,8 @@ int cnn_forward_dev(const mclg_cnn *net, CnnWork &w, const float *x, cudaStream_
 {
 	w.act[0] = const_cast<float *>(x);
 	for (int l = 0; l < net->nl; l++)
-		conv_launch(w.act[l], net->cin[l], net->wf[l], pad_channels(net->cout[l]),
-		            net->master + net->off[l] + (size_t)net->cout[l] * net->cin[l] * 9, w.act[l + 1], net->cout[l],
-		            w.B, w.H, w.W, l + 1 < net->nl, nullptr, st);
+		conv_launch(w.act[l], net->cin[l], net->wf[l], net->master + net->off[l] + (size_t)net->cout[l] * net->cin[l] * 9,
+		            w.act[l + 1], net->cout[l], w.B, w.H, w.W, l + 1 < net->nl, nullptr, st);
 	CKC(cudaGetLastError());
 	return MCLG_OK;
 }
@@ -434,7 +482,7 @@ static int cnn_backward_dev(mclg_cnn *net, CnnWork &w, const float *gy, float *g
 		if (l > 0) {
 			// d loss / d z_{l-1} = (W_l^T g_l) masked by ReLU'(z_{l-1}) = (act_l > 0)
 			float *gin = bufs[l & 1];
-			conv_launch(gz, Cout, net->wb[l], pad_channels(Cin), nullptr, gin, Cin, w.B, w.H, w.W, 0, w.act[l], st);
+			conv_launch(gz, Cout, net->wb[l], nullptr, gin, Cin, w.B, w.H, w.W, 0, w.act[l], st);
 			gz = gin;
 		}
 	}
@@ -731,9 +779,9 @@ int mclg_cnn_create(mclg_cnn **out, int cin, int width, int depth, int cout, uns
 	if (e == cudaSuccess) e = cudaMalloc((void **)&n->m, off * sizeof(float));
 	if (e == cudaSuccess) e = cudaMalloc((void **)&n->v, off * sizeof(float));
 	for (int l = 0; l < depth && e == cudaSuccess; l++) {
-		e = cudaMalloc((void **)&n->wf[l], (size_t)n->cin[l] * 9 * pad_channels(n->cout[l]) * sizeof(__nv_bfloat16));
+		e = cudaMalloc((void **)&n->wf[l], (size_t)9 * co_pad(n->cout[l]) * ci_pad(n->cin[l]) * sizeof(__nv_bfloat16));
 		if (e == cudaSuccess)
-			e = cudaMalloc((void **)&n->wb[l], (size_t)n->cout[l] * 9 * pad_channels(n->cin[l]) * sizeof(__nv_bfloat16));
+			e = cudaMalloc((void **)&n->wb[l], (size_t)9 * co_pad(n->cin[l]) * ci_pad(n->cout[l]) * sizeof(__nv_bfloat16));
 	}
 	if (e == cudaSuccess) e = cudaMemcpyAsync(n->master, h, off * sizeof(float), cudaMemcpyHostToDevice, n->st);
 	if (e == cudaSuccess) e = cudaMemsetAsync(n->m, 0, off * sizeof(float), n->st);

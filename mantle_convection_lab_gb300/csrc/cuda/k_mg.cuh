@@ -1,16 +1,10 @@
 // Types shared by the converged-solve kernel (k_mg.cu) and its host launcher.
 #pragma once
-#include "mclg_dev.cuh"
+#include "team.cuh"
 
 namespace mclg {
 
 constexpr int kMaxLev = 14;
-
-// The blocks that share a pass over a level: block `rank` of `size` (the
-// whole grid, a thread-block cluster, or one block alone).
-struct Part {
-	int rank, size;
-};
 
 template <class T> struct V2T;
 template <> struct V2T<float> { typedef float2 t; };

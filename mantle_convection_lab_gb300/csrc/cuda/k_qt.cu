@@ -238,16 +238,17 @@ __device__ __forceinline__ void qt_sweep(const QtLevel<TI> &L, TI omega, const t
 	qt_sweep_src(L, omega, src, xo, tid, nth);
 }
 
-// The team running a part of the V-cycle: the whole grid, or block 0 alone
-// for the smallest levels (block barriers instead of grid barriers).
+// The part of the solve's team running a part of the V-cycle: the whole team,
+// or its leading block alone for the smallest levels (block barriers instead
+// of team barriers).
 struct QtTeam {
-	cg::grid_group *g;
-	bool grid;
+	Sync *sy;
+	bool wide;
 	int tid, nth;
 	__device__ void sync()
 	{
-		if (grid)
-			g->sync();
+		if (wide)
+			sy->sync();
 		else
 			__syncthreads();
 	}
@@ -362,27 +363,27 @@ __device__ void qt_coarse_solve(const QtHier<TI> &H, QtTeam &t)
 
 // z = V-cycle(b) with b in the finest level's b; returns the buffer holding z.
 template <class TI>
-__device__ const typename Q2T<TI>::t *qt_vcycle(cg::grid_group &g, const QtHier<TI> &H, int tid, int nth)
+__device__ const typename Q2T<TI>::t *qt_vcycle(Sync &sy, const QtHier<TI> &H)
 {
-	const int top = H.nlev - 1, nb = H.nblk < top ? H.nblk : top;   // the finest level always runs on the grid
-	QtTeam grid{&g, true, tid, nth};
+	const int top = H.nlev - 1, nb = H.nblk < top ? H.nblk : top;   // the finest level always runs on the team
+	QtTeam team{&sy, true, sy.tid, sy.nth};
 	for (int l = top; l >= (nb > 1 ? nb : 1); l--)
-		qt_down(H, l, grid);
+		qt_down(H, l, team);
 	if (nb > 0) {
-		if (blockIdx.x == 0) {
-			QtTeam blk{&g, false, (int)threadIdx.x, (int)blockDim.x};
+		if (sy.leader()) {
+			QtTeam blk{&sy, false, (int)threadIdx.x, (int)blockDim.x};
 			for (int l = nb - 1; l >= 1; l--)
 				qt_down(H, l, blk);
 			qt_coarse_solve(H, blk);
 			for (int l = 1; l < nb; l++)
 				qt_up(H, l, blk);
 		}
-		g.sync();
+		sy.sync();
 	} else {
-		qt_coarse_solve(H, grid);
+		qt_coarse_solve(H, team);
 	}
 	for (int l = nb > 1 ? nb : 1; l <= top; l++)
-		qt_up(H, l, grid);
+		qt_up(H, l, team);
 	return H.lv[top].x[qt_final(H, top)];
 }
 
@@ -443,9 +444,9 @@ __device__ void qt_coarse_build(const QtHier<TI> &H)
 // ---- FP64 residual and the preconditioner ------------------------------------------
 // R = [C^T (F - K d - G p) ; G^T C d] (FP64); rs = |R_m|^2, |R_c|^2, |C^T F|^2.
 template <class TI>
-__device__ void qt_residual(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, const double2 *d, const double *p,
-                            double (&rs)[3], int tid, int nth)
+__device__ void qt_residual(Sync &sy, const QtArgs<TI> &a, const double2 *d, const double *p, double (&rs)[3])
 {
+	const int tid = sy.tid, nth = sy.nth;
 	const DevLevel &L = a.L;
 	const QtLevel<TI> &Q = a.H.lv[a.H.nlev - 1];
 	const double *df = reinterpret_cast<const double *>(d);
@@ -475,14 +476,15 @@ __device__ void qt_residual(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a
 		a.Rc[e] = c;
 		rs[1] += c * c;
 	}
-	grid_reduce<3>(g, red, rs, 0u);
+	sy.reduce<3>(rs);
 }
 
 // z = M^-1 v, M = diag(V-cycle, BAB); returns <z, v>.
 template <class TI>
-__device__ double qt_precond(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, const double2 *vu, const double *vp,
-                             typename Q2T<TI>::t *zu, double *zp, int tid, int nth)
+__device__ double qt_precond(Sync &sy, const QtArgs<TI> &a, const double2 *vu, const double *vp,
+                             typename Q2T<TI>::t *zu, double *zp)
 {
+	const int tid = sy.tid, nth = sy.nth;
 	typedef typename Q2T<TI>::t V;
 	const QtHier<TI> &H = a.H;
 	const QtLevel<TI> &Q = H.lv[H.nlev - 1];
@@ -493,8 +495,8 @@ __device__ double qt_precond(cg::grid_group &g, GridRed &red, const QtArgs<TI> &
 		w.y = (TI)v.y;
 		Q.b[A] = w;
 	}
-	g.sync();
-	const V *x = qt_vcycle(g, H, tid, nth);
+	sy.sync();
+	const V *x = qt_vcycle(sy, H);
 	double dot[1] = {0.0};
 	for (int A = tid; A < Q.nno; A += nth) {
 		const V z = x[A];
@@ -507,7 +509,7 @@ __device__ double qt_precond(cg::grid_group &g, GridRed &red, const QtArgs<TI> &
 		zp[e] = z;
 		dot[0] += z * vp[e];
 	}
-	grid_reduce<1>(g, red, dot, 0u);
+	sy.reduce<1>(dot);
 	return dot[0];
 }
 
@@ -516,9 +518,9 @@ __device__ double qt_precond(cg::grid_group &g, GridRed &red, const QtArgs<TI> &
 // system [C^T K C, C^T G; G^T C, 0][x_u; x_p] = [R_m; -R_c] from zero; K in TI,
 // G in FP64, Lanczos and direction vectors FP64; x into a.dd, a.dpv.
 template <class TI>
-__device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, double rtol, int maxit, int *status,
-                         int tid, int nth)
+__device__ int qt_minres(Sync &sy, const QtArgs<TI> &a, double rtol, int maxit, int *status)
 {
+	const int tid = sy.tid, nth = sy.nth;
 	typedef typename Q2T<TI>::t V;
 	const DevLevel &L = a.L;
 	const QtLevel<TI> &Q = a.H.lv[a.H.nlev - 1];
@@ -541,8 +543,8 @@ __device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, d
 		wp[1][e] = 0.0;
 		a.dpv[e] = 0.0;
 	}
-	g.sync();
-	double gam2 = qt_precond(g, red, a, vu[0], vp[0], zu[0], zp[0], tid, nth);
+	sy.sync();
+	double gam2 = qt_precond(sy, a, vu[0], vp[0], zu[0], zp[0]);
 	if (!(gam2 > 0.0))
 		return 0;
 	double gam = sqrt(gam2), gam_prev = 1.0;
@@ -567,7 +569,7 @@ __device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, d
 			a.Ahp[e] = t;
 			dl[0] += t * zp[cv][e];
 		}
-		grid_reduce<1>(g, red, dl, 0u);
+		sy.reduce<1>(dl);
 		const double delta = dl[0] / (gam * gam);
 		const double ig = 1.0 / gam, dg = delta / gam, gg = gam / gam_prev;
 		for (int A = tid; A < nn; A += nth) {
@@ -576,8 +578,8 @@ __device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, d
 		}
 		for (int e = tid; e < ne; e += nth)
 			vp[1 - cv][e] = a.Ahp[e] * ig - dg * vp[cv][e] - gg * vp[1 - cv][e];
-		g.sync();
-		const double gn2 = qt_precond(g, red, a, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv], tid, nth);
+		sy.sync();
+		const double gn2 = qt_precond(sy, a, vu[1 - cv], vp[1 - cv], zu[1 - cv], zp[1 - cv]);
 		const double gam_next = sqrt(fmax(gn2, 0.0));
 		const double a0 = c_cur * delta - c_prev * s_cur * gam;
 		const double a1 = sqrt(a0 * a0 + gam_next * gam_next);
@@ -623,21 +625,19 @@ __device__ int qt_minres(cg::grid_group &g, GridRed &red, const QtArgs<TI> &a, d
 		}
 		if (!(fabs(eta) > rtol * eta0) || !(gam > 0.0))
 			break;
-		g.sync();
+		sy.sync();
 	}
-	g.sync();
+	sy.sync();
 	return it;
 }
 
+// The whole converged solve of one refined model on the team `sy`.
 template <class TI>
-__global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
+__device__ void qt_solve(const QtArgs<TI> &a, Sync &sy)
 {
-	typedef typename V4T<TI>::t K4;
-	cg::grid_group g = cg::this_grid();
-	const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+	const int tid = sy.tid, nth = sy.nth;
 	const QtHier<TI> &H = a.H;
 	const DevLevel &L = a.L;
-	GridRed red = a.red;
 	int *status = &a.sc->status;
 
 	// -- per step: every level's reduced operator C^T K C in TI, and its diagonal
@@ -670,16 +670,16 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 				Q.invD[2 * A + c] = Q.kind[2 * A + c] == 1 && dgl[c] > 0.0 ? (TI)(1.0 / dgl[c]) : TI(0);
 		}
 	}
-	g.sync();
-	if (blockIdx.x == 0)
+	sy.sync();
+	if (sy.leader())
 		qt_coarse_build(H);
-	g.sync();
+	sy.sync();
 
 	int refine = 0, minres_total = 0, vcycles = 0, capped = 0;
 	double res_m = 0.0, res_c = 0.0;
 	while (true) {
 		double rs[3];
-		qt_residual(g, red, a, a.d, a.p, rs, tid, nth);
+		qt_residual(sy, a, a.d, a.p, rs);
 		// a zero load (|C^T F| = 0): the residual is measured absolutely
 		const double fnorm = rs[2] > 0.0 ? sqrt(rs[2]) : 1.0;
 		res_m = sqrt(rs[0]) / fnorm;
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 		// far from the target a pass reduces by 1e-2, close to it by what is
 		// left (factor 2 margin), not below outer_rtol
 		const double prt = res > 1e4 * a.rtol ? 1e-2 : fmax(a.outer_rtol, 0.5 * a.rtol / res);
-		const int it = qt_minres(g, red, a, prt, a.max_outer, status, tid, nth);
+		const int it = qt_minres(sy, a, prt, a.max_outer, status);
 		minres_total += it;
 		vcycles += it + 1;
 		for (int A = tid; A < L.nno; A += nth) {
@@ -712,7 +712,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 		}
 		for (int e = tid; e < L.nel; e += nth)
 			a.p[e] += a.dpv[e];
-		g.sync();
+		sy.sync();
 	}
 	if (capped && tid == 0)
 		atomicOr(status, kStatCap);
@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 			v[c] = qt_val(Q, (const double *)df, 2 * A + c);
 		a.V[A] = make_double2(vfree(L, A, 0) ? v[0] : L.vbcval[A], vfree(L, A, 1) ? v[1] : L.vbcval[L.nno + A]);
 	}
-	g.sync();
+	sy.sync();
 	for (int A = tid; A < L.nno; A += nth)
 		for (int c = 0; c < 2; c++)
 			if (Q.kind[2 * A + c] == 2)
@@ -739,6 +739,76 @@ __global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
 		sc->res_c = res_c;
 		sc->dv = 0.0;
 		sc->dp = 0.0;
+	}
+}
+
+// One refined model on the whole cooperative grid.
+template <class TI>
+__global__ void __launch_bounds__(kBlock) k_stokes_qt(QtArgs<TI> a)
+{
+	cg::grid_group g = cg::this_grid();
+	Sync sy;
+	sy.mode = SYNC_GRID;
+	sy.g = &g;
+	sy.red = a.red;
+	sy.cpart = nullptr;
+	sy.cflip = 0;
+	sy.rank = blockIdx.x;
+	sy.size = gridDim.x;
+	sy.tid = blockIdx.x * blockDim.x + threadIdx.x;
+	sy.nth = gridDim.x * blockDim.x;
+	qt_solve<TI>(a, sy);
+}
+
+// A batch of independent refined models, launched with clusters of `cs`
+// blocks (cs = 1: plain blocks).  Each cluster takes the next model from the
+// queue (ordered largest first by the host) and solves it alone with cluster
+// barriers, so clusters never wait on one another.  The rank-0 block draws and
+// every block reads the draw from its shared memory.
+template <class TI>
+__global__ void __launch_bounds__(kBlock) k_stokes_qt_batch(const QtArgs<TI> *models, int nmodels, int *queue)
+{
+	__shared__ int next;
+	__shared__ double cpart[2 * kRedWidth];
+	cg::cluster_group cl = cg::this_cluster();
+	const int cs = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+	for (;;) {
+		if (rank == 0 && threadIdx.x == 0)
+			next = atomicAdd(queue, 1);
+		Sync sy;
+		sy.g = nullptr;
+		sy.cflip = 0;
+		if (cs > 1) {
+			cl.sync();
+			const int m = *cl.map_shared_rank(&next, 0);
+			cl.sync();   // every block has read the draw before the next one
+			if (m >= nmodels)
+				break;
+			sy.mode = SYNC_CLUSTER;
+			sy.red = models[m].red;
+			sy.cpart = cpart;
+			sy.rank = rank;
+			sy.size = cs;
+			sy.tid = rank * blockDim.x + threadIdx.x;
+			sy.nth = cs * blockDim.x;
+			qt_solve<TI>(models[m], sy);
+			cl.sync();   // no block starts the next model (or leaves) while another reads its partials
+		} else {
+			__syncthreads();
+			const int m = next;
+			__syncthreads();
+			if (m >= nmodels)
+				break;
+			sy.mode = SYNC_BLOCK;
+			sy.red = models[m].red;
+			sy.cpart = nullptr;
+			sy.rank = 0;
+			sy.size = 1;
+			sy.tid = threadIdx.x;
+			sy.nth = blockDim.x;
+			qt_solve<TI>(models[m], sy);
+			__syncthreads();
+		}
 	}
 }
 
@@ -795,5 +865,9 @@ __global__ void __launch_bounds__(kBlock) k_qt_inject(int n, const int *map, con
 }
 
 void *qt_kernel(int fp64) { return fp64 ? (void *)k_stokes_qt<double> : (void *)k_stokes_qt<float>; }
+void *qt_batch_kernel(int fp64)
+{
+	return fp64 ? (void *)k_stokes_qt_batch<double> : (void *)k_stokes_qt_batch<float>;
+}
 
 }  // namespace mclg

@@ -7,7 +7,7 @@
 // (Connection.c:708-930), its transpose as restriction, damped Jacobi on the
 // constrained operator and a dense solve on the coarsest level.
 #pragma once
-#include "mclg_dev.cuh"
+#include "team.cuh"
 
 namespace mclg {
 
@@ -82,5 +82,9 @@ struct QtArgs {
 };
 
 void *qt_kernel(int fp64);
+// Refined members of an ensemble solved in one launch: each thread-block
+// cluster (or block) takes the next model from a queue (QtArgs<TI>[n] on the
+// device, largest first) and solves it with team barriers only.
+void *qt_batch_kernel(int fp64);
 
 }  // namespace mclg

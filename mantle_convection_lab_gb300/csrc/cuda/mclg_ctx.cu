@@ -927,9 +927,10 @@ static int qt_setup(mclg_ctx *c, QtArgs<TI> &a, Prebuilt *pre)
 }
 
 // One converged solve on a refined mesh: warm start, the coarse levels'
-// viscosity (the finer level's value at the same node) and K, the kernel,
-// the warm-start history.
-static int launch_stokes_qt(mclg_ctx *c)
+// viscosity (the finer level's value at the same node) and K, then the
+// solver (one cooperative launch here; a batched launch for ensemble members,
+// see stokes_qt_finish), the warm-start history.
+static int stokes_qt_prepare(mclg_ctx *c)
 {
 	const mclg_config &f = c->cfg;
 	const size_t nn = c->L.nno, ne = c->L.nel;
@@ -985,6 +986,22 @@ static int launch_stokes_qt(mclg_ctx *c)
 		if ((rc = check_launch(c, "k_assemble_stokes")))
 			return rc;
 	}
+	(void)track;
+	return MCLG_OK;
+}
+
+// after the solve: the warm-start history counts one more solution
+static void stokes_qt_finish(mclg_ctx *c)
+{
+	if (c->d_h1 != NULL)
+		c->ghist++;
+}
+
+static int launch_stokes_qt(mclg_ctx *c)
+{
+	int rc = stokes_qt_prepare(c);
+	if (rc)
+		return rc;
 	if (c->cfg.precision == 2) {
 		void *args[] = {&c->qtd};
 		CK(cudaLaunchCooperativeKernel(qt_kernel(1), dim3(c->coop_qt), dim3(kBlock), args, 0, c->st));
@@ -993,8 +1010,7 @@ static int launch_stokes_qt(mclg_ctx *c)
 		CK(cudaLaunchCooperativeKernel(qt_kernel(0), dim3(c->coop_qt), dim3(kBlock), args, 0, c->st));
 	}
 	c->launches++;
-	if (track)
-		c->ghist++;
+	stokes_qt_finish(c);
 	return MCLG_OK;
 }
 
@@ -2379,15 +2395,41 @@ struct mclg_ensemble {
 	int cs_cand[kCand], grid_cand[kCand];
 	float cand_cost[kCand];
 	int cs, grid;          // chosen cluster size and grid
+	int qcs, qgrid;        // ... and those of the refined members' batched launch
 	long long steps;
 	int nbatch;            // members in the batched launch (uniform meshes)
-	int *amr, namr;        // members on refined meshes, solved one launch each
+	// refined members of at most kQtBatchNodes nodes: a second batched launch
+	// of the refined-mesh solver (a model per cluster, largest first)
+	static const int kQtBatchNodes = 32768;
+	int *qorder, nqt;
+	void *dargs_qt;        // device QtArgs<TI>[nqt], queue order
+	int *queue_qt;
+	int qcs_cand[kCand], qgrid_cand[kCand];
+	int *amr, namr;        // larger refined members, solved one cooperative launch each
 	// the whole step as a CUDA graph, captured once the autotuner has chosen and
 	// every member's warm start is in its steady form, replayed afterwards
 	cudaGraphExec_t graph;
 	int graph_failed;
 	long long graph_launches;   // kernels one replay launches
 };
+
+static cudaError_t launch_qt_batch(mclg_ensemble *e, int cs, int grid)
+{
+	cudaLaunchConfig_t lc;
+	memset(&lc, 0, sizeof lc);
+	lc.gridDim = dim3(grid);
+	lc.blockDim = dim3(kBlock);
+	lc.stream = e->st;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeClusterDimension;
+	at[0].val.clusterDim.x = cs;
+	at[0].val.clusterDim.y = 1;
+	at[0].val.clusterDim.z = 1;
+	lc.attrs = at;
+	lc.numAttrs = 1;
+	void *kargs[] = {&e->dargs_qt, &e->nqt, &e->queue_qt};
+	return cudaLaunchKernelExC(&lc, qt_batch_kernel(e->fp64), kargs);
+}
 
 static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
 {
@@ -2407,9 +2449,9 @@ static cudaError_t launch_batch(mclg_ensemble *e, int cs, int grid)
 	return cudaLaunchKernelExC(&lc, stokes_mg_batch_kernel(e->fp64), kargs);
 }
 
-// Blocks of a batched launch with clusters of cs: as many clusters as can be
-// resident at once, but no more than there are models.
-static int batch_grid(mclg_ensemble *e, int cs)
+// Blocks of a batched launch of `kern` with clusters of cs: as many clusters
+// as can be resident at once, but no more than there are models (nmodels).
+static int batch_grid(mclg_ensemble *e, int cs, void *kern, int nmodels)
 {
 	cudaLaunchConfig_t lc;
 	memset(&lc, 0, sizeof lc);
@@ -2423,14 +2465,14 @@ static int batch_grid(mclg_ensemble *e, int cs)
 	lc.attrs = at;
 	lc.numAttrs = 1;
 	int nc = 0;
-	if (cudaOccupancyMaxActiveClusters(&nc, stokes_mg_batch_kernel(e->fp64), &lc) != cudaSuccess) {
+	if (cudaOccupancyMaxActiveClusters(&nc, kern, &lc) != cudaSuccess) {
 		cudaGetLastError();
 		nc = cs <= 8 ? 2 * e->m[0]->num_sms / cs : 0;
 	}
 	if (nc < 1)
 		return 0;
-	if (nc > e->nbatch)
-		nc = e->nbatch;
+	if (nc > nmodels)
+		nc = nmodels;
 	return (nc < 1 ? 1 : nc) * cs;
 }
 
@@ -2450,10 +2492,15 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 	free(e->m);
 	free(e->order);
 	free(e->amr);
+	free(e->qorder);
 	if (e->dargs)
 		cudaFree(e->dargs);
 	if (e->queue)
 		cudaFree(e->queue);
+	if (e->dargs_qt)
+		cudaFree(e->dargs_qt);
+	if (e->queue_qt)
+		cudaFree(e->queue_qt);
 	for (int i = 0; i < 4; i++)
 		if (e->ev[i])
 			cudaEventDestroy(e->ev[i]);
@@ -2494,7 +2541,8 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 		return MCLG_BAD_INPUT;
 	}
 	e->amr = (int *)calloc((size_t)n, sizeof(int));
-	if (e->amr == NULL) {
+	e->qorder = (int *)calloc((size_t)n, sizeof(int));
+	if (e->amr == NULL || e->qorder == NULL) {
 		mclg_ensemble_destroy(e);
 		return MCLG_BAD_INPUT;
 	}
@@ -2529,8 +2577,12 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 			mclg_ensemble_destroy(e);
 			return rc;
 		}
-		if (e->m[i]->qt_on)
-			e->amr[e->namr++] = i;
+		if (e->m[i]->qt_on) {
+			if (e->m[i]->L.nno <= mclg_ensemble::kQtBatchNodes)
+				e->qorder[e->nqt++] = i;
+			else
+				e->amr[e->namr++] = i;
+		}
 	}
 	CKE(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
 	for (int i = 0; i < 4; i++)
@@ -2550,8 +2602,8 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 			mclg_ensemble_destroy(e);
 			return MCLG_BAD_INPUT;
 		}
-		if (c->qt_on)   // refined members keep their own stream: their steps run concurrently
-			continue;
+		if (c->qt_on && c->L.nno > mclg_ensemble::kQtBatchNodes)
+			continue;   // large refined members keep their own stream: their steps run concurrently
 		CKE(cudaStreamSynchronize(c->st));
 		CKE(cudaStreamDestroy(c->st));
 		c->st = e->st;
@@ -2576,21 +2628,51 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 	CKE(cudaMemcpyAsync(e->dargs, h.data(), asz * (size_t)(e->nbatch > 0 ? e->nbatch : 1), cudaMemcpyHostToDevice,
 	                    e->st));
 	CKE(cudaMalloc((void **)&e->queue, sizeof(int)));
+	// the batched refined members, largest first
+	std::stable_sort(e->qorder, e->qorder + e->nqt,
+	                 [&](int a, int b) { return e->m[a]->L.nno > e->m[b]->L.nno; });
+	if (e->nqt > 0) {
+		const size_t qsz = e->fp64 ? sizeof(QtArgs<double>) : sizeof(QtArgs<float>);
+		std::vector<unsigned char> hq(qsz * (size_t)e->nqt);
+		for (int k = 0; k < e->nqt; k++) {
+			mclg_ctx *c = e->m[e->qorder[k]];
+			if (e->fp64)
+				memcpy(&hq[qsz * k], &c->qtd, qsz);
+			else
+				memcpy(&hq[qsz * k], &c->qtf, qsz);
+		}
+		CKE(cudaMalloc(&e->dargs_qt, hq.size()));
+		CKE(cudaMemcpyAsync(e->dargs_qt, hq.data(), hq.size(), cudaMemcpyHostToDevice, e->st));
+		CKE(cudaMalloc((void **)&e->queue_qt, sizeof(int)));
+	}
 	// 16 blocks per cluster is beyond the portable 8: allowed by an opt-in
 	// attribute, dropped from the candidates where the device refuses it
 	const bool allow16 = cudaFuncSetAttribute(stokes_mg_batch_kernel(e->fp64),
 	                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
 	cudaGetLastError();
+	const bool allow16q = cudaFuncSetAttribute(qt_batch_kernel(e->fp64),
+	                                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+	cudaGetLastError();
 	for (int k = 0; k < mclg_ensemble::kCand; k++) {
 		e->cs_cand[k] = 1 << k;
-		e->grid_cand[k] = (k < 4 || allow16) ? batch_grid(e, e->cs_cand[k]) : 0;
+		e->grid_cand[k] = (k < 4 || allow16) ? batch_grid(e, e->cs_cand[k], stokes_mg_batch_kernel(e->fp64),
+		                                                  e->nbatch) : 0;
 		if (e->grid_cand[k] < e->cs_cand[k]) {   // not launchable: fall back to the previous size
 			e->cs_cand[k] = e->cs_cand[k - 1];
 			e->grid_cand[k] = e->grid_cand[k - 1];
 		}
+		e->qcs_cand[k] = 1 << k;
+		e->qgrid_cand[k] = (k < 4 || allow16q) ? batch_grid(e, e->qcs_cand[k], qt_batch_kernel(e->fp64), e->nqt)
+		                                       : 0;
+		if (e->qgrid_cand[k] < e->qcs_cand[k] && k > 0) {
+			e->qcs_cand[k] = e->qcs_cand[k - 1];
+			e->qgrid_cand[k] = e->qgrid_cand[k - 1];
+		}
 	}
 	e->cs = 1;
 	e->grid = e->grid_cand[0];
+	e->qcs = e->qcs_cand[0];
+	e->qgrid = e->qgrid_cand[0];
 	CKE(cudaStreamSynchronize(e->st));
 #undef CKE
 	*out = e;
@@ -2641,11 +2723,11 @@ int mclg_ensemble_initial_temperature(mclg_ensemble *e)
 
 // The work of one ensemble step, issued on the ensemble's stream (refined
 // members fork onto their own streams and join back).
-static int ensemble_issue(mclg_ensemble *e, int cs, int grid)
+static int ensemble_issue(mclg_ensemble *e, int cs, int grid, int qcs, int qgrid)
 {
 	int rc;
-	// refined members: the whole step on the member's own stream, concurrent with
-	// one another and with the batched members
+	// large refined members: the whole step on the member's own stream, concurrent
+	// with one another and with the batched members
 	for (int k = 0; k < e->namr; k++) {
 		mclg_ctx *c = e->m[e->amr[k]];
 		CK(cudaStreamWaitEvent(c->st, e->ev[0], 0));
@@ -2662,17 +2744,30 @@ static int ensemble_issue(mclg_ensemble *e, int cs, int grid)
 		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_mg_prepare(c)))
 			return rc;
 	}
+	for (int k = 0; k < e->nqt; k++) {
+		mclg_ctx *c = e->m[e->qorder[k]];
+		if ((rc = launch_buoy_vis(c)) || (rc = mclg_velocity_pressure_KGF_matrix(c)) || (rc = stokes_qt_prepare(c)))
+			return rc;
+	}
 	CK(cudaEventRecord(e->ev[1], e->st));
 	if (e->nbatch > 0) {
 		CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
 		CK(launch_batch(e, cs, grid));
 	}
+	if (e->nqt > 0) {
+		CK(cudaMemsetAsync(e->queue_qt, 0, sizeof(int), e->st));
+		CK(launch_qt_batch(e, qcs, qgrid));
+	}
 	CK(cudaEventRecord(e->ev[2], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
-		if (c->qt_on)
+		if (c->qt_on && c->L.nno > mclg_ensemble::kQtBatchNodes)
 			continue;
-		if ((rc = stokes_mg_finish(c)) || (rc = launch_stress(c)) || (rc = launch_heat(c)))
+		if (c->qt_on)
+			stokes_qt_finish(c);
+		else if ((rc = stokes_mg_finish(c)))
+			return rc;
+		if ((rc = launch_stress(c)) || (rc = launch_heat(c)))
 			return rc;
 		CK(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, e->st));
 	}
@@ -2710,6 +2805,8 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		tune = (int)(e->steps - 2);
 	const int cs = tune >= 0 ? e->cs_cand[tune] : e->cs;
 	const int grid = tune >= 0 ? e->grid_cand[tune] : e->grid;
+	const int qcs = tune >= 0 ? e->qcs_cand[tune] : e->qcs;
+	const int qgrid = tune >= 0 ? e->qgrid_cand[tune] : e->qgrid;
 	// capture the step once the tuning is over and the warm starts are steady
 	if (tune < 0 && e->steps >= 2 + mclg_ensemble::kCand && e->graph == NULL && !e->graph_failed &&
 	    ensemble_steady(e)) {
@@ -2723,7 +2820,7 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 		cudaError_t ce = cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal);
 		if (ce == cudaSuccess) {
 			ce = cudaEventRecord(e->ev[0], e->st);
-			rc = ce == cudaSuccess ? ensemble_issue(e, cs, grid) : MCLG_CUDA_ERROR;
+			rc = ce == cudaSuccess ? ensemble_issue(e, cs, grid, qcs, qgrid) : MCLG_CUDA_ERROR;
 			const cudaError_t ee = cudaStreamEndCapture(e->st, &g);   // always ends the capture
 			if (ce == cudaSuccess)
 				ce = ee;
@@ -2757,7 +2854,7 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 				c->ghist++;
 		}
 		e->m[0]->launches += e->graph_launches;
-	} else if ((rc = ensemble_issue(e, cs, grid))) {
+	} else if ((rc = ensemble_issue(e, cs, grid, qcs, qgrid))) {
 		return rc;
 	}
 	CK(cudaEventRecord(e->ev[3], e->st));
@@ -2780,6 +2877,8 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 					best = k;
 			e->cs = e->cs_cand[best];
 			e->grid = e->grid_cand[best];
+			e->qcs = e->qcs_cand[best];
+			e->qgrid = e->qgrid_cand[best];
 		}
 	}
 	long long l1 = 0;
@@ -2800,7 +2899,7 @@ int mclg_ensemble_step(mclg_ensemble *e, mclg_step_stats *st, int *grid_used)
 				s->status = s2;
 			s->ms_total = ms_total;
 			s->solver_kernel_ms = ms_solver;
-			s->solver_kernel_launches = (e->nbatch > 0) + e->namr;
+			s->solver_kernel_launches = (e->nbatch > 0) + (e->nqt > 0) + e->namr;
 			s->kernel_launches = (l1 - l0) + 1;
 		}
 		c->timestep++;
