@@ -76,8 +76,8 @@ WORKLOADS["cfg4_ensemble_amr_256"] = {
     "kind": "ensemble", "amr": True,
     "desc": "configuration 4 with refinement: the 256 members of cfg4_ensemble_256 starting from tanh boundary "
             "layers with seeded modes, each base grid refined 0-2 levels (seeded) by |grad T| > 0.2 max (2:1, "
-            "hanging nodes); uniform members in one batched launch, refined members by the refined-mesh solver one "
-            "launch each; every member to Stokes residual < 1e-8 every step",
+            "hanging nodes); uniform members in one batched launch, refined members in one batched launch of the "
+            "refined-mesh solver; every member to Stokes residual < 1e-8 every step",
     "mesh": "256 models, 32^2..256^2 bases + 0-2 levels",
 }
 WORKLOADS["cfg2_amr_128"] = {
@@ -420,11 +420,10 @@ def fp64_reference_config(cfg):
 
 
 def leaves_of(model, cfg):
-    """Finest-level Morton start codes of a model's current leaves (its Mcode list)."""
+    """Finest-level Morton start codes of a model's current leaves: its Mcode
+    list without the level bits."""
     import numpy as np
-    mc = model.mesh("Mcode").astype(np.int64)
-    F = cfg.level - 1
-    return ((mc >> 4) << (2 * (F - (mc & 15)))).astype(np.int32)
+    return np.ascontiguousarray(model.mesh("Mcode") >> 4, np.int32)
 
 
 def _rel(a, b):

@@ -2399,11 +2399,14 @@ struct mclg_ensemble {
 	long long steps;
 	int nbatch;            // members in the batched launch (uniform meshes)
 	// refined members of at most kQtBatchNodes nodes: a second batched launch
-	// of the refined-mesh solver (a model per cluster, largest first)
-	static const int kQtBatchNodes = 32768;
+	// of the refined-mesh solver (a model per cluster, largest first); larger
+	// ones keep a cooperative launch of their own
+	static const int kQtBatchNodes = 1 << 20;
 	int *qorder, nqt;
 	void *dargs_qt;        // device QtArgs<TI>[nqt], queue order
 	int *queue_qt;
+	cudaStream_t st_qt;    // the refined batch runs beside the uniform one
+	cudaEvent_t ev_qt[2];
 	int qcs_cand[kCand], qgrid_cand[kCand];
 	int *amr, namr;        // larger refined members, solved one cooperative launch each
 	// the whole step as a CUDA graph, captured once the autotuner has chosen and
@@ -2419,7 +2422,7 @@ static cudaError_t launch_qt_batch(mclg_ensemble *e, int cs, int grid)
 	memset(&lc, 0, sizeof lc);
 	lc.gridDim = dim3(grid);
 	lc.blockDim = dim3(kBlock);
-	lc.stream = e->st;
+	lc.stream = e->st_qt;
 	cudaLaunchAttribute at[1];
 	at[0].id = cudaLaunchAttributeClusterDimension;
 	at[0].val.clusterDim.x = cs;
@@ -2504,6 +2507,13 @@ void mclg_ensemble_destroy(mclg_ensemble *e)
 	for (int i = 0; i < 4; i++)
 		if (e->ev[i])
 			cudaEventDestroy(e->ev[i]);
+	for (int i = 0; i < 2; i++)
+		if (e->ev_qt[i])
+			cudaEventDestroy(e->ev_qt[i]);
+	if (e->st_qt) {
+		cudaStreamSynchronize(e->st_qt);
+		cudaStreamDestroy(e->st_qt);
+	}
 	if (e->st)
 		cudaStreamDestroy(e->st);
 	free(e);
@@ -2585,8 +2595,11 @@ static int ensemble_create(mclg_ensemble **out, const mclg_config *cfgs, const i
 		}
 	}
 	CKE(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+	CKE(cudaStreamCreateWithFlags(&e->st_qt, cudaStreamNonBlocking));
 	for (int i = 0; i < 4; i++)
 		CKE(cudaEventCreate(&e->ev[i]));
+	for (int i = 0; i < 2; i++)
+		CKE(cudaEventCreateWithFlags(&e->ev_qt[i], cudaEventDisableTiming));
 	// one stream for all members; the solver's element tables are shared
 	// constants, so every member must have the same element aspect ratio
 	int first = 0;
@@ -2750,14 +2763,20 @@ static int ensemble_issue(mclg_ensemble *e, int cs, int grid, int qcs, int qgrid
 			return rc;
 	}
 	CK(cudaEventRecord(e->ev[1], e->st));
+	// the refined batch on its own stream, beside the uniform batch
+	if (e->nqt > 0) {
+		CK(cudaEventRecord(e->ev_qt[0], e->st));
+		CK(cudaStreamWaitEvent(e->st_qt, e->ev_qt[0], 0));
+		CK(cudaMemsetAsync(e->queue_qt, 0, sizeof(int), e->st_qt));
+		CK(launch_qt_batch(e, qcs, qgrid));
+		CK(cudaEventRecord(e->ev_qt[1], e->st_qt));
+	}
 	if (e->nbatch > 0) {
 		CK(cudaMemsetAsync(e->queue, 0, sizeof(int), e->st));
 		CK(launch_batch(e, cs, grid));
 	}
-	if (e->nqt > 0) {
-		CK(cudaMemsetAsync(e->queue_qt, 0, sizeof(int), e->st));
-		CK(launch_qt_batch(e, qcs, qgrid));
-	}
+	if (e->nqt > 0)
+		CK(cudaStreamWaitEvent(e->st, e->ev_qt[1], 0));
 	CK(cudaEventRecord(e->ev[2], e->st));
 	for (int i = 0; i < e->n; i++) {
 		mclg_ctx *c = e->m[i];
