@@ -90,6 +90,9 @@ WORKLOADS["cfg2_amr_128"] = {
     "mesh": "128^2 base + 3 levels",
 }
 ENSEMBLE_METRIC = "aggregate model-steps/s at Stokes residual 1e-8"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one steady launch
+# of the workload's solver kernel, from the ncu capture summarised in profiles/
+TRAFFIC = {"cfg3_mg_1024": (57.07e9, "profiles/k_stokes_mg_f32_1024.md (one steady launch, ncu --set full)")}
 DEFAULT_WORKLOAD = "cfg3_mg_1024"
 GUESS_NET = os.path.join(ROOT, "mantle_convection_lab_gb300", "weights", "guess_cfg3.bin")
 GUESS_GRID = 128
@@ -792,7 +795,9 @@ def run_gpu(args, wl):
                 "d2h_bytes_per_step": 8 * (3 * nno + nel)},
         "gpu_launches": acc["launches"],
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": TRAFFIC.get(args.workload, (None, None))[0],
+                     "traffic_source": TRAFFIC.get(args.workload, (None, None))[1],
                      "alg_bytes_per_launch": alg, "ms_per_launch": ms_launch},
         "clocks": clocks,
         "wall_s_timed": wall,
