@@ -97,7 +97,10 @@ typedef struct mclg_config {
 	                            2 "fp64mg": the same converged solver with FP64 inner solves */
 	double stokes_rtol;      /* converged solvers: stop when |[F-Kd-Gp; G^T d]| / |F| < rtol (1e-8) */
 	int warm_start;          /* converged solvers: 0 zero, 1 the previous step's (d,p), 2 d=0 and p kept
-	                            (the reference's start), 3 linear extrapolation of the last two steps */
+	                            (the reference's start), 3 linear extrapolation of the last two steps,
+	                            4 (uniform meshes, stokes_method=1) the start of least FP64 residual in
+	                            h1 + a (h1 - h2) + b (h1 - 2 h2 + h3) over the last three solutions
+	                            (refined meshes treat 4 as 3) */
 	double vis_min, vis_max; /* viscosity clip, applied when vis_max > 0 */
 	int mg_smooth;           /* damped-Jacobi sweeps per V-cycle side (2) */
 	double mg_omega;         /* Jacobi damping (0.6) */
@@ -140,6 +143,7 @@ typedef struct mclg_step_stats {
 	int guess_used;          /* learned guess: 1 network, 0 previous solution, -1 not judged this step */
 	double res_guess_learned, res_guess_prev;   /* relative FP64 residuals of the two candidate guesses */
 	double ms_guess;         /* device time of the network and its feature kernels this step */
+	double warm_alpha, warm_beta;   /* warm_start=4: the start h1 + alpha (h1-h2) + beta (h1-2h2+h3) chosen */
 } mclg_step_stats;
 
 typedef struct mclg_ctx mclg_ctx;

@@ -93,7 +93,7 @@ class StepStats(C.Structure):
         ("kernel_launches", C.c_longlong), ("solver_kernel_ms", C.c_double),
         ("solver_kernel_launches", C.c_longlong), ("refine_passes", C.c_int),
         ("guess_used", C.c_int), ("res_guess_learned", C.c_double), ("res_guess_prev", C.c_double),
-        ("ms_guess", C.c_double),
+        ("ms_guess", C.c_double), ("warm_alpha", C.c_double), ("warm_beta", C.c_double),
     ]
 
     def as_dict(self):

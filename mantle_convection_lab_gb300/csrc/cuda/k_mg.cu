@@ -778,6 +778,138 @@ __device__ double block_precond(const MGArgs<TI> &a, unsigned char *sm, Sync &sy
 	return dot[0];
 }
 
+// Y = K u + G p and Yc = G^T u in FP64 (the Stokes operator applied to (u, p));
+// a.Kd is scratch.  Ends with a team barrier: Yc is written at Morton indices,
+// which other threads read.
+template <class TI>
+__device__ void stokes_apply(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, const double2 *u, const double *p,
+                             double2 *Y, double *Yc)
+{
+	const int tid = sy.tid, nth = sy.nth;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	tile_pass<double, double2>(sm, sy.part(true), N0, a.mask0, a.vis, u, nullptr, nullptr, Y, PASS_MATVEC, 0.0, nullptr);
+	gmul64(N0, a.mask0, a.gt, p, a.Kd, tid, nth);
+	sy.sync();
+	for (int A = tid; A < nn; A += nth) {
+		const double2 y = Y[A], g = a.Kd[A];
+		Y[A] = make_double2(y.x + g.x, y.y + g.y);
+	}
+	for (int e = tid; e < ne; e += nth) {
+		const int ex = e / N0, ez = e - ex * N0;
+		Yc[morton(ex, ez)] = gtmul64_elem(N0, a.mask0, a.gt, u, ex, ez);
+	}
+	sy.sync();
+}
+
+// warm_start=4: the start of the solve is the member of
+//     x(alpha, beta) = h1 + alpha (h1 - h2) + beta (h1 - 2 h2 + h3)
+// (h1, h2, h3 the last three solutions) whose residual under this step's
+// operator is smallest in the norm the MINRES correction works in,
+// |r|_M^2 = <r, M^-1 r> with M = diag(V-cycle, BAB): a least-squares problem in
+// (alpha, beta) from the residual r0 at h1 and the operator applied to the two
+// differences, a_k = A D_k; with M symmetric only M^-1 a_1 and M^-1 a_2 are
+// needed.  The family holds the previous solution (0, 0), the linear (1, 0)
+// and the quadratic (1, 1) extrapolation in time.  (In the plain L2 norm the
+// minimiser chose coefficients of 10^5 along the second difference, whose
+// operator image is tiny, and the solves diverged.)  ndir = 1 uses h1, h2 only
+// (beta = 0).  Coefficients outside [-4, 8] fall back to the linear
+// extrapolation.  Scratch: the MINRES and inner-CG vectors, free until the
+// correction solve starts.
+// Measured on the 1024^2 viscosity-contrast workload: the minimiser picks the
+// quadratic member, MINRES needs about half the iterations of the linear start
+// for some ten steps, then more and more (the error the solves leave behind is
+// carried on and amplified from step to step), 111 against 100 per step over
+// 30 steps; warm_start=3 stays the default there.
+template <class TI>
+__device__ void warm_guess(const MGArgs<TI> &a, unsigned char *sm, Sync &sy, int ndir)
+{
+	typedef typename V2T<TI>::t VI;
+	const int tid = sy.tid, nth = sy.nth;
+	const int N0 = a.N0, n0 = N0 + 1, nn = n0 * n0, ne = N0 * N0;
+	double2 *U1 = a.mw[0], *U2 = a.mw[1], *Y1 = a.mv[0], *Y2 = a.mv[1];
+	double *P1 = a.mwp[0], *P2 = a.mwp[1], *Yc1 = a.mvp[0], *Yc2 = a.mvp[1];
+	VI *Z1 = a.H.px, *Z2 = a.H.pr;
+	double *Zp1 = a.mzp[0], *Zp2 = a.mzp[1];
+	double rs[3];
+	stokes_residual(a, sm, sy, a.h1d, a.h1p, rs);   // a.R = F - K h1 - G p1, a.Rc = G^T h1
+	for (int A = tid; A < nn; A += nth) {
+		const double2 x1 = a.h1d[A], x2 = a.h2d[A];
+		U1[A] = make_double2(x1.x - x2.x, x1.y - x2.y);
+		if (ndir == 2) {
+			const double2 x3 = a.h3d[A];
+			U2[A] = make_double2(x1.x - 2.0 * x2.x + x3.x, x1.y - 2.0 * x2.y + x3.y);
+		}
+	}
+	for (int e = tid; e < ne; e += nth) {
+		P1[e] = a.h1p[e] - a.h2p[e];
+		if (ndir == 2)
+			P2[e] = a.h1p[e] - 2.0 * a.h2p[e] + a.h3p[e];
+	}
+	sy.sync();
+	stokes_apply(a, sm, sy, U1, P1, Y1, Yc1);
+	if (ndir == 2)
+		stokes_apply(a, sm, sy, U2, P2, Y2, Yc2);
+	// M^-1 a_k (the preconditioner's pressure part divides by BAB); the signs of
+	// the continuity parts follow r = [F - K d - G p ; -G^T d]
+	double q[5];   // <a1, M^-1 a1>, <a2, M^-1 a1>, <a2, M^-1 a2>, <r0, M^-1 a1>, <r0, M^-1 a2>
+	q[0] = block_precond(a, sm, sy, Y1, Yc1, Z1, Zp1);
+	q[2] = ndir == 2 ? block_precond(a, sm, sy, Y2, Yc2, Z2, Zp2) : 0.0;
+	double c[3] = {0.0, 0.0, 0.0};
+	for (int A = tid; A < nn; A += nth) {
+		const double2 r = a.R[A];
+		const VI z1 = Z1[A];
+		c[1] += (double)z1.x * r.x + (double)z1.y * r.y;
+		if (ndir == 2) {
+			const double2 y2 = Y2[A];
+			const VI z2 = Z2[A];
+			c[0] += (double)z1.x * y2.x + (double)z1.y * y2.y;
+			c[2] += (double)z2.x * r.x + (double)z2.y * r.y;
+		}
+	}
+	for (int e = tid; e < ne; e += nth) {
+		const double rc = -a.Rc[e];
+		c[1] += Zp1[e] * rc;
+		if (ndir == 2) {
+			c[0] += Zp1[e] * Yc2[e];
+			c[2] += Zp2[e] * rc;
+		}
+	}
+	sy.reduce<3>(c);
+	q[1] = c[0];
+	q[3] = c[1];
+	q[4] = c[2];
+	// every thread holds the same q: the same coefficients and branches
+	double al = q[0] > 0.0 ? q[3] / q[0] : 1.0, be = 0.0;
+	if (ndir == 2) {
+		const double det = q[0] * q[2] - q[1] * q[1];
+		if (det > 1e-12 * q[0] * q[2]) {
+			al = (q[3] * q[2] - q[4] * q[1]) / det;
+			be = (q[4] * q[0] - q[3] * q[1]) / det;
+		}
+	}
+	if (!isfinite(al) || !isfinite(be) || al < -4.0 || al > 8.0 || be < -4.0 || be > 8.0) {
+		al = 1.0;
+		be = 0.0;
+	}
+	for (int A = tid; A < nn; A += nth) {
+		const double2 x1 = a.h1d[A], u1 = U1[A];
+		double2 d = make_double2(x1.x + al * u1.x, x1.y + al * u1.y);
+		if (ndir == 2) {
+			const double2 u2 = U2[A];
+			d.x += be * u2.x;
+			d.y += be * u2.y;
+		}
+		a.d[A] = d;
+	}
+	for (int e = tid; e < ne; e += nth)
+		a.p[e] = a.h1p[e] + al * P1[e] + (ndir == 2 ? be * P2[e] : 0.0);
+	if (tid == 0) {
+		a.sc->warm_a = al;
+		a.sc->warm_b = be;
+	}
+	sy.sync();
+}
+
 // Correction solve by preconditioned MINRES (the Lanczos-based algorithm of
 // Elman, Silvester and Wathen, "Finite Elements and Fast Iterative Solvers",
 // Alg. 4.1) on [K G; G^T 0][x_u; x_p] = [R_m; -R_c] from a zero start, with
@@ -948,6 +1080,11 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 
 	int refine = 0, outer_total = 0, inner_total = 0, capped = 0;
 	double res_m = 0.0, res_c = 0.0, fnorm = 1.0;
+	if (a.method == 1 && a.h1d != nullptr) {
+		const int nh = a.sc->nsolved < 3 ? a.sc->nsolved : 3;   // solutions in the history
+		if (nh >= 2)
+			warm_guess<TI>(a, sm, sy, nh - 1);
+	}
 	if (a.d_alt != nullptr) {
 		// Two candidate guesses: (d, p) from the network and (d_alt, p_alt),
 		// the previous step's solution.  Keep the one with the smaller FP64
@@ -1134,6 +1271,8 @@ __device__ void stokes_solve(const MGArgs<TI> &a, unsigned char *sm, Sync &sy)
 		a.sc->uzawa_cycles = outer_total;
 		a.sc->cg_cycles = inner_total;
 		a.sc->refine_passes = refine;
+		if (a.sc->nsolved < 1000000)
+			a.sc->nsolved++;
 		a.sc->res_m = res_m;
 		a.sc->res_c = res_c;
 		a.sc->dv = 0.0;

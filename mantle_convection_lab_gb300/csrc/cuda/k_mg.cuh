@@ -61,6 +61,9 @@ struct MGArgs {
 	int method;                  // correction solve: 0 Uzawa with inner MG-PCG, 1 MINRES (block-diagonal preconditioner)
 	double2 *mv[2], *mw[2];      // MINRES Lanczos and direction vectors, velocity part (z_u lives in TI)
 	double *mvp[2], *mzp[2], *mwp[2]; // Lanczos, preconditioned and direction vectors, pressure part (Morton)
+	// warm_start=4: the last three solutions (h1 the most recent), or null
+	const double2 *h1d, *h2d, *h3d;
+	const double *h1p, *h2p, *h3p;
 	const double2 *d_alt;        // second candidate guess (previous solution) or null
 	const double *p_alt;
 	int guess_force;             // keep (d, p) without judging it against (d_alt, p_alt)

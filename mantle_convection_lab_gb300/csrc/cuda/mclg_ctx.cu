@@ -110,6 +110,8 @@ struct mclg_ctx {
 	int gsample, gtimed;          // a sample from the last solve exists; ev[6] was recorded
 	double2 *d_h1, *d_h2, *d_cand;   // last two solutions, second candidate guess
 	double *p_h1, *p_h2, *p_cand, *gscale;
+	double2 *d_h3;                // warm_start=4: the solution before d_h2
+	double *p_h3;
 	float *gX, *gYt, *gYs;        // features, target and filter scratch on the coarse node grid
 	CnnWork gw;
 	int goff, gbad;               // steps left with the network off; consecutive steps it did not pay
@@ -935,7 +937,7 @@ static int stokes_qt_prepare(mclg_ctx *c)
 	const mclg_config &f = c->cfg;
 	const size_t nn = c->L.nno, ne = c->L.nel;
 	int rc;
-	if (f.warm_start != 1 && f.warm_start != 3)
+	if (f.warm_start != 1 && f.warm_start != 3 && f.warm_start != 4)
 		CK(cudaMemsetAsync(c->d, 0, nn * sizeof(double2), c->st));
 	if (f.warm_start == 0)
 		CK(cudaMemsetAsync(c->p, 0, ne * sizeof(double), c->st));
@@ -944,7 +946,7 @@ static int stokes_qt_prepare(mclg_ctx *c)
 	const bool track = c->d_h1 != NULL;
 	if (track) {   // history: d_h2 <- d_h1, d_h1 <- d (the last two solutions)
 		const size_t n = 2 * nn > ne ? 2 * nn : ne;
-		if (c->hist_shift == 1 && f.warm_start == 3 && c->ghist >= 2) {
+		if (c->hist_shift == 1 && (f.warm_start == 3 || f.warm_start == 4) && c->ghist >= 2) {
 			// the second step after a remesh: d_h1, d_h2 are the last two solutions of
 			// the old mesh interpolated, d the first solution on the new one.  Their
 			// extrapolation 2 d - d_h1 would add the interpolation error of d_h1 once
@@ -962,7 +964,7 @@ static int stokes_qt_prepare(mclg_ctx *c)
 		CK(cudaMemcpyAsync(c->p_h2, c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h1, c->p, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-		if (f.warm_start == 3 && c->ghist >= 2) {
+		if ((f.warm_start == 3 || f.warm_start == 4) && c->ghist >= 2) {
 			k_qt_extrapolate<<<blocks_for(n), kBlock, 0, c->st>>>((int)(2 * nn), (int)ne, (const double *)c->d_h1,
 			                                                       (const double *)c->d_h2, c->p_h1, c->p_h2,
 			                                                       (double *)c->d, c->p);
@@ -1026,6 +1028,18 @@ static int alloc_history(mclg_ctx *c)
 	CK(dalloc(&c->p_h2, ne));
 	CK(dalloc(&c->p_cand, ne));
 	CK(dalloc(&c->gscale, 4));
+	if (c->cfg.warm_start == 4) {
+		CK(dalloc(&c->d_h3, nn));
+		CK(dalloc(&c->p_h3, ne));
+		const MGArgs<float> &mf = c->mgf;
+		(void)mf;
+		c->mgf.h1d = c->mgd.h1d = c->d_h1;
+		c->mgf.h2d = c->mgd.h2d = c->d_h2;
+		c->mgf.h3d = c->mgd.h3d = c->d_h3;
+		c->mgf.h1p = c->mgd.h1p = c->p_h1;
+		c->mgf.h2p = c->mgd.h2p = c->p_h2;
+		c->mgf.h3p = c->mgd.h3p = c->p_h3;
+	}
 	c->ghist = 0;
 	return MCLG_OK;
 }
@@ -1041,7 +1055,7 @@ static int stokes_mg_prepare(mclg_ctx *c)
 	// policy for zero_P=0 (initial_d_p, Solver.c:251-278): d zeroed, p kept;
 	// 3 = linear extrapolation in time of the last two solutions (previous
 	// solution until two exist)
-	if (f.warm_start != 1 && f.warm_start != 3)
+	if (f.warm_start != 1 && f.warm_start != 3 && f.warm_start != 4)
 		CK(cudaMemsetAsync(c->d, 0, c->L.nno * sizeof(double2), c->st));
 	if (f.warm_start == 0)
 		CK(cudaMemsetAsync(c->p, 0, c->L.nel * sizeof(double), c->st));
@@ -1065,7 +1079,12 @@ static int stokes_mg_prepare(mclg_ctx *c)
 		if (feat)
 			guess_features(c->st, N0, c->gs, c->T, c->vis, c->d, c->p, c->d_h1, c->p_h1, c->gX, c->gscale);
 		// history: d_h2 <- d_h1, d_h1 <- d (the last two solutions; device copies,
-		// so that a captured step replays unchanged)
+		// so that a captured step replays unchanged), and d_h3 <- d_h2 before them
+		// for warm_start=4, whose start the solver kernel forms from the three
+		if (c->d_h3 != NULL) {
+			CK(cudaMemcpyAsync(c->d_h3, c->d_h2, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
+			CK(cudaMemcpyAsync(c->p_h3, c->p_h2, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+		}
 		CK(cudaMemcpyAsync(c->d_h2, c->d_h1, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->p_h2, c->p_h1, ne * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
 		CK(cudaMemcpyAsync(c->d_h1, c->d, nn * sizeof(double2), cudaMemcpyDeviceToDevice, c->st));
@@ -1384,7 +1403,7 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 			mclg_set_error("cooperative occupancy query failed");
 			rc = MCLG_CUDA_ERROR;
 		}
-		if (rc == MCLG_OK && cfg->warm_start == 3)
+		if (rc == MCLG_OK && (cfg->warm_start == 3 || cfg->warm_start == 4))   // 4 acts as 3 here
 			rc = alloc_history(c);
 		if (rc != MCLG_OK) {
 			mclg_destroy(c);
@@ -1404,7 +1423,7 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 			return rc;
 		}
 		c->coop_mg = coop_blocks(stokes_mg_kernel(cfg->precision == 2), c->num_sms, 1 << 30);
-		if (cfg->warm_start == 3 && (rc = alloc_history(c)) != MCLG_OK) {
+		if ((cfg->warm_start == 3 || cfg->warm_start == 4) && (rc = alloc_history(c)) != MCLG_OK) {
 			mclg_destroy(c);
 			*out = NULL;
 			return rc;
@@ -1467,7 +1486,8 @@ void mclg_destroy(mclg_ctx *c)
 	for (int i = 0; i < 7; i++)
 		if (c->ev[i])
 			cudaEventDestroy(c->ev[i]);
-	void *gptrs[] = {c->d_h1, c->d_h2, c->d_cand, c->p_h1, c->p_h2, c->p_cand, c->gscale, c->gX, c->gYt, c->gYs};
+	void *gptrs[] = {c->d_h1, c->d_h2, c->d_h3, c->d_cand, c->p_h1, c->p_h2, c->p_h3, c->p_cand, c->gscale, c->gX,
+	                 c->gYt, c->gYs};
 	for (void *q : gptrs)
 		if (q)
 			cudaFree(q);
@@ -1669,6 +1689,8 @@ static void fill_stats_stokes(mclg_ctx *c, mclg_step_stats *st)
 	st->guess_used = c->cfg.precision != 0 ? s.guess_used : -1;
 	st->res_guess_learned = st->guess_used >= 0 ? s.res_learned : 0.0;
 	st->res_guess_prev = st->guess_used >= 0 ? s.res_prev : 0.0;
+	st->warm_alpha = c->cfg.warm_start == 4 ? s.warm_a : 0.0;
+	st->warm_beta = c->cfg.warm_start == 4 ? s.warm_b : 0.0;
 }
 
 int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
@@ -3448,6 +3470,13 @@ extern "C" int mclg_checkpoint_load(mclg_ctx *c, const char *path)
 	c->p_initialized = hd.p_initialized;
 	if (c->d_h1 != NULL)
 		c->ghist = hist ? hd.ghist : 0;
+	if (c->d_h3 != NULL) {
+		// warm_start=4: the checkpoint holds the last two solutions, not a third;
+		// the next solve starts from one difference, the one after from two
+		const int ns = c->ghist < 2 ? c->ghist : 2;
+		CK(cudaMemcpyAsync(&c->sc->nsolved, &ns, sizeof(int), cudaMemcpyHostToDevice, c->st));
+		CK(cudaStreamSynchronize(c->st));
+	}
 	c->goff = hd.goff;
 	c->gbad = hd.gbad;
 	c->git_prev = hd.git_prev;

@@ -79,6 +79,8 @@ struct StepScalars {
 	double res_m, res_c, fnorm;
 	int uzawa_cycles, cg_cycles, heat_cycles, status;
 	int refine_passes;
+	int nsolved;                // converged solves since the warm-start history began (warm_start=4)
+	double warm_a, warm_b;      // warm_start=4: the coefficients of the chosen start
 	int guess_used;             // learned guess: 1 network, 0 previous solution, -1 not judged
 	double res_learned, res_prev;   // relative FP64 residuals of the two candidates
 };

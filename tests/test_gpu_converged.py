@@ -17,7 +17,7 @@ from mantle_convection_lab_gb300 import Config, Model
 pytestmark = pytest.mark.gpu
 
 VARIANTS = [  # precision, stokes_method, warm_start
-    (1, 0, 1), (1, 1, 1), (1, 1, 3), (1, 1, 0), (2, 0, 2), (2, 1, 3)]
+    (1, 0, 1), (1, 1, 1), (1, 1, 3), (1, 1, 0), (2, 0, 2), (2, 1, 3), (1, 1, 4), (2, 1, 4)]
 
 
 def make(case, precision, method, warm, rtol=1e-8):
