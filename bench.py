@@ -617,6 +617,7 @@ def run_ensemble(args, wl):
 
 
 def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0, parity=False):
+    import numpy as np
     from mantle_convection_lab_gb300 import amr
     run = amr.AmrRun(cfg, lag=lag)
     for _ in range(max(warmup, 0)):
@@ -641,6 +642,8 @@ def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0, parity=False):
         acc["minres"] += st.uzawa_cycles
         acc["vcycles"] += st.cg_cycles
         acc["nel"].append(run.model.nel)
+        acc["remesh_ms"] = {k: round(getattr(st, "remesh_ms_" + k), 2)
+                            for k in ("numbering", "lists", "state", "wait", "carry")}
     torch.cuda.synchronize()
     acc["wall"] = time.perf_counter() - t0
     if dist:
@@ -648,6 +651,8 @@ def _amr_arm(cfg, steps, warmup, sampler_on, dist, torch, lag=0, parity=False):
     acc["clocks"] = sampler.stop() if sampler else None
     acc["remeshes"] = run.remeshes - acc["rem0"]
     acc["nh"] = run.model.nh
+    acc["ms_remesh_begin"] = float(np.mean(run.ms_begin)) if run.ms_begin else None
+    acc["ms_remesh_end"] = float(np.mean(run.ms_end)) if run.ms_end else None
     if parity:
         # one more step on the current refined mesh against its FP64 solution
         acc["parity"] = step_parity(run.model, cfg, leaves=leaves_of(run.model, cfg))
@@ -686,14 +691,17 @@ def run_amr(args, wl):
         "config": {"workload": args.workload, "desc": wl["desc"], "mesh": wl["mesh"],
                    "elements_per_step": acc["nel"], "hanging_nodes_last": acc["nh"],
                    "remeshes_timed": acc["remeshes"], "device_ms_per_step": acc["ms"] / args.steps,
+                   "ms_per_remesh_begin": acc["ms_remesh_begin"], "ms_per_remesh_end": acc["ms_remesh_end"],
+                   "last_remesh_ms": acc.get("remesh_ms"),
                    "solver_kernel_ms_per_step": acc["ms_solver"] / args.steps,
                    "refine_passes_per_step": acc["passes"] / args.steps,
                    "minres_iterations_per_step": acc["minres"] / args.steps,
                    "steps_at_iteration_cap": acc["capped"], "max_stokes_residual": acc["res"],
                    "residual": "conforming: |[C^T(F - K d - G p); G^T C d]| / |C^T F|, C the hanging-node expansion",
                    "residual_1e-8_met": bool(acc["res"] < 1e-8), "parallelism": f"replicas x{world}",
-                   "remesh": "every 10 steps from the T of that step; the mesh built on a host thread during the "
-                             "next 2 steps, swapped in before the third",
+                   "remesh": "every 10 steps from the T of that step: flags, tree and numbering on the device, "
+                             "the solver's lists and the new device state built on a host thread during the next "
+                             "2 steps, swapped in before the third",
                    "roofline": "not reported: assembled-ELL operators on 5 levels, latency-bound at this size"},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": acc["launches"], "roofline": None, "clocks": acc["clocks"],

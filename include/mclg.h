@@ -144,6 +144,11 @@ typedef struct mclg_step_stats {
 	double res_guess_learned, res_guess_prev;   /* relative FP64 residuals of the two candidate guesses */
 	double ms_guess;         /* device time of the network and its feature kernels this step */
 	double warm_alpha, warm_beta;   /* warm_start=4: the start h1 + alpha (h1-h2) + beta (h1-2h2+h3) chosen */
+	/* the last remesh of this model (host wall clock, 0 before the first): the new
+	 * mesh's numbering on the device (in begin), the refined-mesh solver's lists
+	 * and the new device state (on the worker), the wait for the worker and the
+	 * field carry-over (in end) */
+	double remesh_ms_numbering, remesh_ms_lists, remesh_ms_state, remesh_ms_wait, remesh_ms_carry;
 } mclg_step_stats;
 
 typedef struct mclg_ctx mclg_ctx;
@@ -349,14 +354,23 @@ int mclg_amr_leaves(mclg_ctx *ctx, const unsigned char *flags, size_t n, int bas
                     size_t cap, size_t *nleaves);
 int mclg_amr_remesh(mclg_ctx *ctx, double frac, int base_level, int target_level, size_t *nel);
 /* The same in two halves, so that the host work overlaps the GPU's: begin takes
- * the flags of the current T and the new tree (device), then builds the new
- * mesh, the refined-mesh solver's lists and the new device state on a worker
- * thread and returns; the caller may go on stepping the old mesh; end waits
+ * the flags of the current T, the new tree and the new mesh's numbering and
+ * hanging nodes (device, on the model's stream), then builds the refined-mesh
+ * solver's lists and the new device state on a worker thread and returns; the
+ * caller may go on stepping the old mesh; end waits
  * for the worker and carries the current fields over (as mclg_amr_remesh).
  * One remesh may be pending at a time; mclg_destroy finishes a pending one. */
 int mclg_amr_remesh_begin(mclg_ctx *ctx, double frac, int base_level, int target_level);
 int mclg_amr_remesh_end(mclg_ctx *ctx, size_t *nel);
 int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n);
+/* The same mesh numbered on the current CUDA device (k_mesh.cu: ien, node list,
+ * BC codes, equation numbers, geometry, node->element map, hanging nodes,
+ * neighbour lists), copied into host arrays equal to mclg_mesh_new_leaves's
+ * byte for byte.  Rejects leaf lists that are not quadtree cells. */
+int mclg_mesh_new_leaves_device(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n);
+/* 0 when every array of every level of a and b is equal byte for byte, else 1
+ * and the first differing array's name in what[cap]. */
+int mclg_mesh_diff(const mclg_mesh_handle *a, const mclg_mesh_handle *b, char *what, size_t cap);
 int mclg_mesh_amr_leaves(const mclg_mesh_handle *h, const unsigned char *flags, size_t nflags, int base_level,
                          int target_level, int *leaves, size_t cap, size_t *n);
 int mclg_mesh_transfer(const mclg_mesh_handle *from, const double *T_from, size_t n_from,

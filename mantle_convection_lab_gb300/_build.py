@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas"
 CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
 HOST_SRCS = ["host/mclg_input.c", "host/mclg_mesh.c", "host/mclg_output.c", "host/mclg_mesh_api.c", "host/mclg_amr.c", "host/mclg_refmg.c", "host/mclg_qtmg.c", "host/mclg_grain.c"]
-CUDA_SRCS = ["cuda/k_elem.cu", "cuda/k_uzawa.cu", "cuda/k_heat.cu", "cuda/k_mg.cu", "cuda/k_cnn.cu", "cuda/k_amr.cu", "cuda/k_qt.cu", "cuda/mclg_writer.cu", "cuda/mclg_ctx.cu"]
+CUDA_SRCS = ["cuda/k_elem.cu", "cuda/k_uzawa.cu", "cuda/k_heat.cu", "cuda/k_mg.cu", "cuda/k_cnn.cu", "cuda/k_amr.cu", "cuda/k_qt.cu", "cuda/k_mesh.cu", "cuda/mclg_writer.cu", "cuda/mclg_ctx.cu"]
 HEADERS = ["host/mclg_host.h", "host/mclg_ic.h", "cuda/mclg_dev.cuh", "cuda/cg_solve.cuh", "cuda/k_mg.cuh", "cuda/k_tile.cuh", "cuda/cnn.cuh", "cuda/mclg_writer.cuh", "cuda/k_qt.cuh", "cuda/team.cuh"]
 
 

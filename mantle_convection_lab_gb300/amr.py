@@ -11,6 +11,7 @@ device flags elements with |grad T| > frac * max, the host builds the new
 rebuilt on it in place with T carried over (mclg_amr_remesh).
 """
 import os
+import time
 
 import numpy as np
 
@@ -42,6 +43,7 @@ class AmrRun:
         self.steps = 0
         self.remeshes = 0
         self._pending = False
+        self.ms_begin, self.ms_end = [], []    # host wall time of each remesh_begin / remesh_end
 
     def remesh(self):
         n = self.model.remesh(self.frac, self.base, self.target)
@@ -51,12 +53,16 @@ class AmrRun:
     def step(self):
         k = self.steps % self.every
         if self._pending and k == self.lag:
+            t0 = time.perf_counter()
             self.model.remesh_end()
+            self.ms_end.append(1e3 * (time.perf_counter() - t0))
             self._pending = False
             self.remeshes += 1
         if k == 0:
             if self.lag > 0 and self.steps > 0:
+                t0 = time.perf_counter()
                 self.model.remesh_begin(self.frac, self.base, self.target)
+                self.ms_begin.append(1e3 * (time.perf_counter() - t0))
                 self._pending = True
             else:
                 self.remesh()

@@ -94,6 +94,8 @@ class StepStats(C.Structure):
         ("solver_kernel_launches", C.c_longlong), ("refine_passes", C.c_int),
         ("guess_used", C.c_int), ("res_guess_learned", C.c_double), ("res_guess_prev", C.c_double),
         ("ms_guess", C.c_double), ("warm_alpha", C.c_double), ("warm_beta", C.c_double),
+        ("remesh_ms_numbering", C.c_double), ("remesh_ms_lists", C.c_double), ("remesh_ms_state", C.c_double),
+        ("remesh_ms_wait", C.c_double), ("remesh_ms_carry", C.c_double),
     ]
 
     def as_dict(self):
@@ -154,6 +156,8 @@ def lib():
         "mclg_amr_remesh_begin": (C.c_int, [vp, C.c_double, C.c_int, C.c_int]),
         "mclg_amr_remesh_end": (C.c_int, [vp, C.POINTER(sz)]),
         "mclg_mesh_new_leaves": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
+        "mclg_mesh_new_leaves_device": (C.c_int, [C.POINTER(vp), vp, ip, sz]),
+        "mclg_mesh_diff": (C.c_int, [vp, vp, C.c_char_p, sz]),
         "mclg_mesh_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_amr_leaves": (C.c_int, [vp, C.POINTER(C.c_ubyte), sz, C.c_int, C.c_int, ip, sz, C.POINTER(sz)]),
         "mclg_mesh_transfer": (C.c_int, [vp, dp, sz, vp, dp, sz]),
@@ -317,17 +321,21 @@ class GrainSize:
 
 class Mesh:
     """Host-only mesh of Main.c:33-52 (quadtree, numbering, BC codes, hanging nodes).
-    leaves: build from finest-level Morton start codes instead of develop_mode."""
+    leaves: build from finest-level Morton start codes instead of develop_mode;
+    device=True numbers that leaf set on the current CUDA device instead (the
+    same arrays, byte for byte)."""
 
-    def __init__(self, config, leaves=None):
+    def __init__(self, config, leaves=None, device=False):
         self._h = C.c_void_p()
         self.config = config
         if leaves is None:
+            if device:
+                raise MclgError(BAD_INPUT, "the device numbering takes a leaf list")
             _check(lib().mclg_mesh_new(C.byref(self._h), C.byref(config)), "mesh_new")
         else:
             lv = np.ascontiguousarray(leaves, np.int32)
-            _check(lib().mclg_mesh_new_leaves(C.byref(self._h), C.byref(config), _iptr(lv), lv.size),
-                   "mesh_new_leaves")
+            fn = lib().mclg_mesh_new_leaves_device if device else lib().mclg_mesh_new_leaves
+            _check(fn(C.byref(self._h), C.byref(config), _iptr(lv), lv.size), "mesh_new_leaves")
         s = self.get("sizes")
         self.nel, self.nno, self.neq, self.heat_neq, self.nh, self.gnox, self.gnoz, self.max_level = map(int, s)
 
@@ -358,6 +366,12 @@ class Mesh:
         out = np.zeros(n, np.int32)
         _check(lib().mclg_mesh_get(self._h, MESH[which], lev, _iptr(out), n), "mesh_get")
         return out
+
+    def diff(self, other):
+        """None when every array of every level equals other's byte for byte,
+        else the name of the first one that differs."""
+        buf = C.create_string_buffer(128)
+        return buf.value.decode() if lib().mclg_mesh_diff(self._h, other._h, buf, 128) else None
 
     def initial_temperature(self, lev=-1):
         n = self._size("node", lev)

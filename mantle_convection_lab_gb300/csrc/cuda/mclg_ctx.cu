@@ -5,6 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <chrono>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -98,6 +99,7 @@ struct mclg_ctx {
 	double *tmpA, *tmpB;
 	// converged solvers on uniform meshes (precision 1 and 2)
 	int coop_mg;
+	double remesh_ms[5];   // the last remesh: numbering, lists, state, wait, carry (host ms)
 	MGArgs<float> mgf;
 	MGArgs<double> mgd;
 	void *mg_ptr[192];
@@ -1232,13 +1234,18 @@ static mclg_config mesh_config(const mclg_config *cfg)
 
 // The host structures of a model on a leaf set: the mesh and, for a converged
 // solver on a refined mesh, its constrained-space lists.  No device work.
-static int prebuild(Prebuilt *pb, const mclg_config *cfg, const int *leaves, long n)
+// have_mesh: pb->mesh was numbered already (on the device), only the lists
+// remain.
+static int prebuild(Prebuilt *pb, const mclg_config *cfg, const int *leaves, long n, bool have_mesh = false)
 {
-	memset(pb, 0, sizeof *pb);
-	const mclg_config mcfg = mesh_config(cfg);
-	int rc = mclg_mesh_build_leaves(&pb->mesh, &mcfg, leaves, n);
-	if (rc != MCLG_OK)
-		return rc;
+	int rc = MCLG_OK;
+	if (!have_mesh) {
+		memset(pb, 0, sizeof *pb);
+		const mclg_config mcfg = mesh_config(cfg);
+		rc = mclg_mesh_build_leaves(&pb->mesh, &mcfg, leaves, n);
+		if (rc != MCLG_OK)
+			return rc;
+	}
 	const int top = pb->mesh.max_level - 1, lo = pb->mesh.min_level, nlev = top - lo + 1;
 	if (cfg->precision != 0 && !pb->mesh.uniform && nlev >= 2 && nlev <= 16) {
 		rc = mclg_qt_build(&pb->mesh, lo, pb->q);
@@ -1288,7 +1295,8 @@ static int create_impl(mclg_ctx **out, const mclg_config *cfg, const int *leaves
 		c->mesh = pre->mesh;
 		memset(&pre->mesh, 0, sizeof pre->mesh);
 	} else {
-		rc = leaves ? mclg_mesh_build_leaves(&c->mesh, &mcfg, leaves, nleaves) : mclg_mesh_build(&c->mesh, &mcfg);
+		rc = leaves ? mclg_mesh_build_leaves_device(&c->mesh, &mcfg, leaves, nleaves, NULL)
+		            : mclg_mesh_build(&c->mesh, &mcfg);
 	}
 	if (rc != MCLG_OK) {
 		mclg_mesh_free(&c->mesh);
@@ -1691,6 +1699,8 @@ static void fill_stats_stokes(mclg_ctx *c, mclg_step_stats *st)
 	st->res_guess_prev = st->guess_used >= 0 ? s.res_prev : 0.0;
 	st->warm_alpha = c->cfg.warm_start == 4 ? s.warm_a : 0.0;
 	st->warm_beta = c->cfg.warm_start == 4 ? s.warm_b : 0.0;
+	for (int k = 0; k < 5; k++)
+		(&st->remesh_ms_numbering)[k] = c->remesh_ms[k];
 }
 
 int mclg_solve_velocity_pressure(mclg_ctx *c, mclg_step_stats *st)
@@ -3070,21 +3080,27 @@ int mclg_amr_leaves(mclg_ctx *c, const unsigned char *flags, size_t n, int base_
 // then the context is rebuilt on the new mesh in place: the handle stays
 // valid, time step and model time carry over, velocity and pressure restart
 // from zero.
-// A remesh in two halves: begin() computes the flags and the new tree on the
-// device and starts a worker thread that builds the new mesh, the solver's
-// lists and the new context's device state (on a stream of its own); end()
+// A remesh in two halves: begin() computes the flags, the new tree and the new
+// mesh's numbering on the device and starts a worker thread that builds the
+// solver's lists and the new context's device state (on a stream of its own); end()
 // waits for it, carries the fields over and swaps the new state in.  Between
 // them the caller may go on stepping the old mesh.
 struct RemeshJob {
 	std::thread th;
 	mclg_config cfg;
 	std::vector<int> leaves;
-	Prebuilt pb;
+	Prebuilt pb;       // its mesh numbered on the device by begin()
 	int device;        // the caller's device (the current device is per thread)
 	mclg_ctx *n;       // the new context, created by the worker
 	int rc;
 	char err[512];
+	double ms[3];      // numbering (begin), lists and state (worker)
 };
+
+static double ms_since(std::chrono::steady_clock::time_point t0)
+{
+	return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
 
 // The worker: the host structures, then the new context's device state on a
 // stream of its own (the old context keeps stepping on its stream meanwhile).
@@ -3093,10 +3109,14 @@ static void remesh_work(RemeshJob *j)
 	j->rc = cudaSetDevice(j->device) == cudaSuccess ? MCLG_OK : MCLG_CUDA_ERROR;
 	if (j->rc != MCLG_OK)
 		mclg_set_error("remesh worker: cannot select device %d", j->device);
+	auto t0 = std::chrono::steady_clock::now();
 	if (j->rc == MCLG_OK)
-		j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size());
+		j->rc = prebuild(&j->pb, &j->cfg, j->leaves.data(), (long)j->leaves.size(), true);
+	j->ms[1] = ms_since(t0);
+	t0 = std::chrono::steady_clock::now();
 	if (j->rc == MCLG_OK)
 		j->rc = create_impl(&j->n, &j->cfg, j->leaves.data(), (long)j->leaves.size(), &j->pb);
+	j->ms[2] = ms_since(t0);
 	if (j->rc != MCLG_OK)
 		snprintf(j->err, sizeof j->err, "%s", mclg_last_error());
 }
@@ -3144,6 +3164,16 @@ int mclg_amr_remesh_begin(mclg_ctx *c, double frac, int base_level, int target_l
 		delete j;
 		return cuda_fail(cudaErrorInvalidDevice, "mclg_amr_remesh_begin");
 	}
+	// the new mesh's numbering and hanging nodes on the device, on the model's
+	// stream (after the step in flight); the worker builds the solver's lists
+	const mclg_config mcfg = mesh_config(&c->cfg);
+	const auto t0 = std::chrono::steady_clock::now();
+	rc = mclg_mesh_build_leaves_device(&j->pb.mesh, &mcfg, j->leaves.data(), (long)j->leaves.size(), c->st);
+	j->ms[0] = ms_since(t0);
+	if (rc != MCLG_OK) {
+		delete j;
+		return rc;
+	}
 	c->rj = j;
 	try {
 		j->th = std::thread(remesh_work, j);
@@ -3160,8 +3190,12 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 		return MCLG_BAD_INPUT;
 	}
 	RemeshJob *j = c->rj;
+	const auto t_wait = std::chrono::steady_clock::now();
 	if (j->th.joinable())
 		j->th.join();
+	const double ms_wait = ms_since(t_wait);
+	const auto t_carry = std::chrono::steady_clock::now();
+	const double ms_job[3] = {j->ms[0], j->ms[1], j->ms[2]};
 	if (j->rc != MCLG_OK) {
 		const int rc = j->rc;
 		mclg_set_error("%s", j->err);
@@ -3250,6 +3284,10 @@ int mclg_amr_remesh_end(mclg_ctx *c, size_t *nel_out)
 	}
 	n->timestep = c->timestep;
 	n->launches = c->launches;
+	for (int k = 0; k < 3; k++)
+		n->remesh_ms[k] = ms_job[k];
+	n->remesh_ms[3] = ms_wait;
+	n->remesh_ms[4] = ms_since(t_carry);   // without the release of the old state below
 	// the caller's handle takes the new state; the old state is released
 	mclg_ctx tmp;
 	memcpy(&tmp, c, sizeof tmp);

@@ -66,6 +66,15 @@ typedef struct mclg_mesh {
 int mclg_mesh_build(mclg_mesh *m, const mclg_config *cfg);
 /* The same mesh stack from a given leaf set (finest-level Morton start codes). */
 int mclg_mesh_build_leaves(mclg_mesh *m, const mclg_config *cfg, const int *leaves, long n);
+/* The level-independent part (Mesh.c:396-428, one rank) and the configuration
+ * checks; clears m first. */
+int mclg_mesh_frame(mclg_mesh *m, const mclg_config *cfg);
+/* A leaf list: at least 2 strictly increasing codes within the finest level. */
+int mclg_mesh_check_leaves(const mclg_mesh *m, const int *leaves, long n);
+/* The same mesh stack as mclg_mesh_build_leaves, numbered on the current CUDA
+ * device (k_mesh.cu) and copied into host arrays that are equal byte for byte;
+ * st is the stream the device work runs on (0: a stream of its own). */
+int mclg_mesh_build_leaves_device(mclg_mesh *m, const mclg_config *cfg, const int *leaves, long n, void *st);
 /* |grad T| refinement (mclg_amr.c): leaves of a new tree from per-element flags
  * of the finest level of m; *leaves is malloc'ed. */
 int mclg_amr_build_leaves(const mclg_mesh *m, const unsigned char *flags, int base_level, int target_level,

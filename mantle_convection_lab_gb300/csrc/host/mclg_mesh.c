@@ -704,12 +704,9 @@ static void *level_worker(void *p)
 	return NULL;
 }
 
-static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves, long nleaves)
+int mclg_mesh_frame(mclg_mesh *m, const mclg_config *c)
 {
-	int lev, fl, rc;
-	ivec head = {0};
-	tree_ctx t;
-
+	int lev, fl;
 	memset(m, 0, sizeof *m);
 	if (c->nprox != 1 || c->nproz != 1) {
 		mclg_set_error("nprox=%d nproz=%d: one device holds the whole mesh, set nprox=nproz=1",
@@ -736,6 +733,34 @@ static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves
 	}
 	m->gnox = m->max_elx[fl] + 1;
 	m->gnoz = m->max_elx[fl] + 1;
+	return MCLG_OK;
+}
+
+int mclg_mesh_check_leaves(const mclg_mesh *m, const int *leaves, long n)
+{
+	const int cap = m->max_nel[m->max_level - 1];
+	for (long i = 0; i < n; i++)
+		if (leaves[i] < 0 || leaves[i] >= cap || (i > 0 && leaves[i] <= leaves[i - 1])) {
+			mclg_set_error("leaf %ld: codes must increase within [0, %d)", i, cap);
+			return MCLG_BAD_INPUT;
+		}
+	if (n < 2) {
+		mclg_set_error("refinement produced %ld elements", n);
+		return MCLG_BAD_INPUT;
+	}
+	return MCLG_OK;
+}
+
+static int mesh_build_impl(mclg_mesh *m, const mclg_config *c, const int *leaves, long nleaves)
+{
+	int lev, fl, rc;
+	ivec head = {0};
+	tree_ctx t;
+
+	rc = mclg_mesh_frame(m, c);
+	if (rc != MCLG_OK)
+		return rc;
+	fl = m->max_level - 1;
 
 	/* build_quad_tree (Tree.c:67-93) */
 	t.out = &head;

@@ -2,6 +2,7 @@
  * Host-only C ABI over the mesh builder: lets a caller (or a test on a
  * machine without a GPU) read the numbering that the device path uses.
  */
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include "mclg_host.h"
@@ -44,6 +45,102 @@ int mclg_mesh_new_leaves(mclg_mesh_handle **h, const mclg_config *cfg, const int
 	if (leaves == NULL)
 		return MCLG_BAD_INPUT;
 	return mesh_new(h, cfg, leaves, (long)n);
+}
+
+int mclg_mesh_new_leaves_device(mclg_mesh_handle **h, const mclg_config *cfg, const int *leaves, size_t n)
+{
+	int rc;
+	mclg_mesh_handle *p;
+	if (h == NULL || cfg == NULL || leaves == NULL)
+		return MCLG_BAD_INPUT;
+	*h = NULL;
+	p = (mclg_mesh_handle *)calloc(1, sizeof *p);
+	if (p == NULL)
+		return MCLG_BAD_INPUT;
+	p->cfg = *cfg;
+	rc = mclg_mesh_build_leaves_device(&p->mesh, cfg, leaves, (long)n, NULL);
+	if (rc != MCLG_OK) {
+		free(p);
+		return rc;
+	}
+	*h = p;
+	return MCLG_OK;
+}
+
+/* every array of every level, byte for byte (the lengths the builder fills) */
+int mclg_mesh_diff(const mclg_mesh_handle *ha, const mclg_mesh_handle *hb, char *what, size_t cap)
+{
+	const mclg_mesh *a, *b;
+	int lev;
+	char buf[128];
+	if (ha == NULL || hb == NULL)
+		return MCLG_BAD_INPUT;
+	a = &ha->mesh;
+	b = &hb->mesh;
+	buf[0] = 0;
+	if (a->min_level != b->min_level || a->max_level != b->max_level || a->gnox != b->gnox ||
+	    a->gnoz != b->gnoz || a->uniform != b->uniform)
+		snprintf(buf, sizeof buf, "mesh frame");
+	for (lev = a->min_level; lev < a->max_level && buf[0] == 0; lev++) {
+		const mclg_level *A = &a->lev[lev], *B = &b->lev[lev];
+		const size_t ne = (size_t)A->nel, nn = (size_t)A->nno, nh = (size_t)A->nh;
+		const int fine = lev == a->max_level - 1;
+		struct {
+			const char *name;
+			const void *x, *y;
+			size_t bytes;
+		} arr[] = {
+			{"Mcode", A->Mcode, B->Mcode, ne * sizeof(int)},
+			{"node", A->node, B->node, nn * sizeof(int)},
+			{"node_lut", A->node_lut, B->node_lut, (size_t)A->lut_n * sizeof(int)},
+			{"ien", A->ien, B->ien, 4 * ne * sizeof(int)},
+			{"ienl", A->ienl, B->ienl, 4 * ne * sizeof(int)},
+			{"elev", A->elev, B->elev, ne * sizeof(int)},
+			{"id", A->id, B->id, 2 * nn * sizeof(int)},
+			{"heat_id", A->heat_id, B->heat_id, nn * sizeof(int)},
+			{"v_bc", A->v_bc, B->v_bc, 2 * nn},
+			{"v_bc_val", A->v_bc_val, B->v_bc_val, 2 * nn * sizeof(double)},
+			{"T_bc", A->T_bc, B->T_bc, nn},
+			{"T_bc_val", A->T_bc_val, B->T_bc_val, nn * sizeof(double)},
+			{"X", A->X, B->X, 2 * nn * sizeof(double)},
+			{"dx_dxi", A->dx_dxi, B->dx_dxi, ne * sizeof(double)},
+			{"dz_deta", A->dz_deta, B->dz_deta, ne * sizeof(double)},
+			{"jacobi", A->jacobi, B->jacobi, ne * sizeof(double)},
+			{"area", A->area, B->area, ne * sizeof(double)},
+			{"hang_node", A->hang_node, B->hang_node, nh * sizeof(int)},
+			{"hang_c0", A->hang_c0, B->hang_c0, nh * sizeof(int)},
+			{"hang_c1", A->hang_c1, B->hang_c1, nh * sizeof(int)},
+			{"hang_ni", A->hang_ni, B->hang_ni, nh * sizeof(int)},
+			{"hang_ci0", A->hang_ci0, B->hang_ci0, nh * sizeof(int)},
+			{"hang_ci1", A->hang_ci1, B->hang_ci1, nh * sizeof(int)},
+			{"p2n_cnt", A->p2n_cnt, B->p2n_cnt, nn * sizeof(int)},
+			{"p2n_el", A->p2n_el, B->p2n_el, 4 * nn * sizeof(int)},
+			{"p2n_a", A->p2n_a, B->p2n_a, 4 * nn * sizeof(int)},
+			{"nb", A->nb, B->nb, (size_t)A->nbw * nn * sizeof(int)},
+			{"nb_cnt", A->nb_cnt, B->nb_cnt, nn * sizeof(int)},
+			{"kslot", A->kslot, B->kslot, 16 * ne},
+			{"cell_elem", fine ? A->cell_elem : NULL, fine ? B->cell_elem : NULL,
+			 fine ? (size_t)(a->gnox - 1) * (size_t)(a->gnoz - 1) * sizeof(int) : 0},
+		};
+		size_t k;
+		if (A->nel != B->nel || A->nno != B->nno || A->neq != B->neq || A->heat_neq != B->heat_neq ||
+		    A->nh != B->nh || A->hang_chained != B->hang_chained || A->nbw != B->nbw || A->lut_n != B->lut_n) {
+			snprintf(buf, sizeof buf, "level %d sizes", lev);
+			break;
+		}
+		for (k = 0; k < sizeof arr / sizeof arr[0]; k++) {
+			if (arr[k].bytes == 0)
+				continue;
+			if ((arr[k].x == NULL) != (arr[k].y == NULL) ||
+			    (arr[k].x != NULL && memcmp(arr[k].x, arr[k].y, arr[k].bytes) != 0)) {
+				snprintf(buf, sizeof buf, "level %d %s", lev, arr[k].name);
+				break;
+			}
+		}
+	}
+	if (what != NULL && cap > 0)
+		snprintf(what, cap, "%s", buf);
+	return buf[0] == 0 ? 0 : 1;
 }
 
 void mclg_mesh_delete(mclg_mesh_handle *h)

@@ -468,16 +468,62 @@ fail:
 	return -1;
 }
 
-/* Rows [A0, A1) of a level, on a thread of their own.  Pass 0 counts each
- * row's contributions and columns; pass 1 writes them at the offsets the
- * counts gave, into the level's arrays (rows are independent, so the result
- * does not depend on how the rows are split). */
+/* Rows [A0, A1) of a level, on a thread of their own.  Pass 0 builds each
+ * row, counts its contributions and columns and keeps both in the chunk's
+ * own lists; pass 1 copies them to the offsets the counts gave, into the
+ * level's arrays (rows are independent, so the result does not depend on how
+ * the rows are split). */
 typedef struct {
 	const mclg_level *L;
 	mclg_qt_level *q;
 	int A0, A1, pass, maxw, rc;
-	int *cnt;   /* pass 0: [nno] contributions per row; rcnt holds the columns */
+	int *cnt;           /* pass 0: [nno] contributions per row; rcnt holds the columns */
+	int *ktgt, *ksrc;   /* the chunk's rows as pass 0 built them */
+	double *kw;
+	int *kcol;
+	long kn, kcap, kc, kccap;
 } ro_chunk;
+
+static int keep_row(ro_chunk *o, const contrib *row, long rn, const int *cols, int ncols)
+{
+	if (o->kn + rn > o->kcap) {
+		long cap = o->kcap ? 2 * o->kcap : 4096;
+		while (cap < o->kn + rn)
+			cap *= 2;
+		int *t = (int *)realloc(o->ktgt, (size_t)cap * sizeof(int));
+		if (t == NULL)
+			return -1;
+		o->ktgt = t;
+		t = (int *)realloc(o->ksrc, (size_t)cap * sizeof(int));
+		if (t == NULL)
+			return -1;
+		o->ksrc = t;
+		double *w = (double *)realloc(o->kw, (size_t)cap * sizeof(double));
+		if (w == NULL)
+			return -1;
+		o->kw = w;
+		o->kcap = cap;
+	}
+	if (o->kc + ncols > o->kccap) {
+		long cap = o->kccap ? 2 * o->kccap : 4096;
+		while (cap < o->kc + ncols)
+			cap *= 2;
+		int *t = (int *)realloc(o->kcol, (size_t)cap * sizeof(int));
+		if (t == NULL)
+			return -1;
+		o->kcol = t;
+		o->kccap = cap;
+	}
+	for (long i = 0; i < rn; i++) {
+		o->ktgt[o->kn + i] = row[i].tgt;
+		o->ksrc[o->kn + i] = row[i].src;
+		o->kw[o->kn + i] = row[i].w;
+	}
+	o->kn += rn;
+	memcpy(o->kcol + o->kc, cols, (size_t)ncols * sizeof(int));
+	o->kc += ncols;
+	return 0;
+}
 
 static void *reduced_rows(void *arg)
 {
@@ -485,39 +531,59 @@ static void *reduced_rows(void *arg)
 	const mclg_level *L = o->L;
 	mclg_qt_level *q = o->q;
 	const int nno = L->nno;
+	o->rc = MCLG_BAD_INPUT;
+	if (o->pass == 1) {
+		long pk = 0, pc = 0;
+		for (int A = o->A0; A < o->A1; A++) {
+			const size_t at = (size_t)q->rc_off[A];
+			const int rn = o->cnt[A], ncols = q->rcnt[A];
+			memcpy(q->rc_tgt + at, o->ktgt + pk, (size_t)rn * sizeof(int));
+			memcpy(q->rc_src + at, o->ksrc + pk, (size_t)rn * sizeof(int));
+			memcpy(q->rc_w + at, o->kw + pk, (size_t)rn * sizeof(double));
+			pk += rn;
+			for (int u = 0; u < q->rnbw; u++)
+				q->rnb[(size_t)u * nno + A] = u < ncols ? o->kcol[pc + u] : A;
+			pc += ncols;
+		}
+		o->rc = MCLG_OK;
+		return NULL;
+	}
 	contrib *row = NULL;
 	long rn, rcap = 0;
 	int *cols = (int *)malloc(512 * sizeof(int)), ncols;
-	o->rc = MCLG_BAD_INPUT;
 	o->maxw = 1;
+	o->ktgt = o->ksrc = o->kcol = NULL;
+	o->kw = NULL;
+	o->kn = o->kcap = o->kc = o->kccap = 0;
 	if (cols == NULL)
 		goto out;
 	for (int A = o->A0; A < o->A1; A++) {
 		if (reduced_row(L, q, A, &row, &rcap, cols, &rn, &ncols))
 			goto out;
-		if (o->pass == 0) {
-			o->cnt[A] = (int)rn;
-			if (ncols > 255)
-				goto out;
-			q->rcnt[A] = (unsigned char)ncols;
-			if (ncols > o->maxw)
-				o->maxw = ncols;
-			continue;
-		}
-		const size_t at = (size_t)q->rc_off[A];
-		for (long i = 0; i < rn; i++) {
-			q->rc_tgt[at + i] = row[i].tgt;
-			q->rc_src[at + i] = row[i].src;
-			q->rc_w[at + i] = row[i].w;
-		}
-		for (int u = 0; u < q->rnbw; u++)
-			q->rnb[(size_t)u * nno + A] = u < ncols ? cols[u] : A;
+		o->cnt[A] = (int)rn;
+		if (ncols > 255)
+			goto out;
+		q->rcnt[A] = (unsigned char)ncols;
+		if (ncols > o->maxw)
+			o->maxw = ncols;
+		if (keep_row(o, row, rn, cols, ncols))
+			goto out;
 	}
 	o->rc = MCLG_OK;
 out:
 	free(cols);
 	free(row);
 	return NULL;
+}
+
+static void chunk_free(ro_chunk *o)
+{
+	free(o->ktgt);
+	free(o->ksrc);
+	free(o->kw);
+	free(o->kcol);
+	o->ktgt = o->ksrc = o->kcol = NULL;
+	o->kw = NULL;
 }
 
 static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
@@ -533,6 +599,7 @@ static int build_reduced_operator(const mclg_level *L, mclg_qt_level *q)
 	int rc = MCLG_BAD_INPUT, maxw = 1;
 	long tot = 0;
 	int *cnt = (int *)malloc(((size_t)nno + 1) * sizeof(int));
+	memset(ch, 0, sizeof ch);
 	q->rc_off = (int *)malloc(((size_t)nno + 1) * sizeof(int));
 	q->rcnt = (unsigned char *)malloc((size_t)nno + 1);
 	if (!cnt || !q->rc_off || !q->rcnt)
@@ -579,6 +646,8 @@ out:
 	if (rc != MCLG_OK)
 		mclg_set_error("refined-mesh operator of a %d-node level: a row with more than 255 reduced "
 		               "columns, or out of host memory", nno);
+	for (int i = 0; i < nch; i++)
+		chunk_free(&ch[i]);
 	free(cnt);
 	return rc;
 }

@@ -212,3 +212,25 @@ def test_transfers_on_meshes_split_across_threads():
     P = np.random.default_rng(7).standard_normal(a.nel)
     got = a.transfer_elem(P, b)
     assert np.abs(got - _raster_mean(a, P, b)).max() <= 1e-14 * np.abs(P).max()
+
+
+def test_mesh_diff_names_the_first_differing_array():
+    """mclg_mesh_diff, which the device-numbering tests use: equal builds give
+    None; a different boundary code shows up in the arrays it changes."""
+    c = cfg(7)
+    lv = uniform_leaves(6, 3)
+    a, b = Mesh(c, leaves=lv), Mesh(c, leaves=lv)
+    assert a.diff(b) is None
+    c2 = cfg(7)
+    c2.lef_T_bc_val = c.lef_T_bc_val + 0.5
+    assert Mesh(c2, leaves=lv).diff(a) == "level 2 T_bc_val"
+    c2.lef_T_bc = b"T"
+    assert Mesh(c2, leaves=lv).diff(a) == "level 2 sizes"      # fewer heat equations
+
+
+def test_device_numbering_fails_loudly_without_a_device():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a device is present: tests/test_gpu_mesh_numbering.py covers it")
+    with pytest.raises(MclgError):
+        Mesh(cfg(7), leaves=uniform_leaves(6, 3), device=True)
