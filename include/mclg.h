@@ -123,6 +123,12 @@ typedef struct mclg_config {
 	/* converged solvers on uniform meshes: damped-Jacobi sweeps per V-cycle side
 	 * on the levels below the two finest (0: mg_smooth) */
 	int mg_smooth_coarse;
+	/* converged solvers on uniform meshes with mg_smooth=2: 0 damped Jacobi (mg_omega),
+	 * 1 the degree-2 Chebyshev polynomial of D^-1 K on [mg_cheb_lmax / mg_cheb_ratio,
+	 * mg_cheb_lmax] (the same polynomial before and after the coarse correction, so
+	 * the V-cycle stays symmetric) */
+	int mg_smoother;
+	double mg_cheb_lmax, mg_cheb_ratio;   /* (2.5, 4.0) */
 } mclg_config;
 
 typedef struct mclg_step_stats {

@@ -67,7 +67,8 @@ class Config(C.Structure):
         ("mg_eta_avg", C.c_int), ("mg_block_n", C.c_int), ("guess_smooth", C.c_int),
         ("stokes_method", C.c_int), ("mg_cycle", C.c_int), ("mg_finest_iteration", C.c_int),
         ("mg_coarse_iteration", C.c_int), ("lowest_vis", C.c_double), ("highest_vis", C.c_double),
-        ("mg_smooth_coarse", C.c_int),
+        ("mg_smooth_coarse", C.c_int), ("mg_smoother", C.c_int), ("mg_cheb_lmax", C.c_double),
+        ("mg_cheb_ratio", C.c_double),
     ]
 
     @classmethod

@@ -298,10 +298,13 @@ __device__ void level_down(Sync &sy, unsigned char *sm, const MGHier<T> &H, int 
 			barrier(sy, grid);
 		}
 	} else {
-		// sweep 1 (from zero) fused into sweep 2
+		// sweep 1 (from zero) fused into sweep 2; the Chebyshev pair from zero is
+		// x1 = w1 D^-1 b, x2 = c1 x1 + w2 D^-1 (b - A x1)
+		const bool ch = H.cheb && nu == 2;
 		if (active) {
-			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH, H.omega, nullptr,
-			                xs0, rf, nf, nullptr, nullptr, nullptr, nullptr, bo);
+			tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, xt, b, L.invD, x, PASS_SMOOTH,
+			                ch ? H.w2 : H.omega, nullptr, xs0, rf, nf, nullptr, nullptr, nullptr, nullptr, bo, nullptr,
+			                ch ? H.w1 : T(-1), ch ? H.c1 : T(1));
 			barrier(sy, grid);
 		}
 		for (int s = 2; s < nu; s++) {
@@ -342,15 +345,23 @@ __device__ void level_up(Sync &sy, unsigned char *sm, const MGHier<T> &H, int l,
 	V *xt = (x == L.xa) ? L.xb : L.xa;
 	const MGLevel<T> &C = H.lv[l + 1];
 	const int nu = l < H.lfine ? H.nu : H.nu_c;
-	// the coarse-grid correction x + P xc is formed inside the first post-smoothing sweep
+	// the coarse-grid correction x + P xc is formed inside the first post-smoothing
+	// sweep; the Chebyshev pair keeps that iterate (x0) in L.r, free on the way up,
+	// for x2 = c1 x1 - c0 x0 + w2 D^-1 (b - A x1)
+	const bool ch = H.cheb && nu == 2;
 	for (int s = 0; s < nu; s++) {
 		const bool last = l == 0 && s == nu - 1;
 		V *dst = last ? out0 : xt;
 		double *dp = (last && dotv) ? dot : nullptr;
 		if (active) {
 			if (s == 0)
-				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, dp,
-				                XS_PROLONG, xcur[l + 1], C.n, dotv);
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH,
+				                ch ? H.w1 : H.omega, dp, XS_PROLONG, xcur[l + 1], C.n, dotv, nullptr, nullptr, nullptr,
+				                nullptr, ch ? L.r : nullptr);
+			else if (ch)
+				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.w2, dp,
+				                XS_PLAIN, nullptr, 0, dotv, nullptr, nullptr, nullptr, nullptr, nullptr, T(-1), H.c1,
+				                L.r, H.c0);
 			else
 				tile_pass<T, V>(sm, sy.part(grid), L.N, L.mask, L.eta, x, b, L.invD, dst, PASS_SMOOTH, H.omega, dp,
 				                XS_PLAIN, nullptr, 0, dotv);

@@ -32,6 +32,10 @@ struct MGHier {
 	int nu;                      // Jacobi sweeps per side on levels below lfine
 	int nu_c, lfine;             // ... and on levels lfine and coarser
 	int eta_avg;                 // coarse viscosity: 0 injection, 1 full-weighted mean, 2 full-weighted log-mean
+	// degree-2 Chebyshev smoothing (cheb != 0, nu == nu_c == 2): x1 = x0 + w1 D^-1 r0,
+	// x2 = c1 x1 - c0 x0 + w2 D^-1 r1
+	int cheb;
+	T w1, w2, c1, c0;
 	// inner CG vectors on level 0
 	typename V2T<T>::t *px, *pr, *pz, *pp, *pq;
 };

@@ -92,7 +92,8 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 // One pass of y = A x over a level, with a fused epilogue:
 //   MATVEC: out = A x            (*dot = this thread's share of x.(A x) when dot != nullptr)
 //   RESID:  out = b - A x        (with xout, x as formed is stored there too)
-//   SMOOTH: out = x + omega D^-1 (b - A x)
+//   SMOOTH: out = cx x - c0 x0 + omega D^-1 (b - A x)   (cx = 1, no x0: damped Jacobi;
+//           the Chebyshev recurrence otherwise; with xout, x as formed is stored there)
 //           (*dot = this thread's share of out.dotv when dot != nullptr)
 //   STOKES: out64 = A x + G gp, with G gp in FP64 from the element pressures
 //           gp (Morton order) and the corner coefficients gt of the fine
@@ -100,7 +101,8 @@ __device__ __forceinline__ V x_eff(int xs, int A, int gx, int gz, const V *__res
 //           rows of the Stokes operator applied to (x, gp), and their product
 //           with x).  G stays in FP64: applied in FP32 as well, it raised the
 //           MINRES iterations per step by half.
-// x at Dirichlet dofs is read as 0 and out is 0 there.
+// x at Dirichlet dofs is read as 0 and out is 0 there.  wload (when >= 0)
+// replaces omega in the XS_ZERO / XS_ZERO_R formation of x.
 template <class T, class V>
 __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, const unsigned char *__restrict__ mask,
                                        const T *__restrict__ eta, const V *__restrict__ x,
@@ -110,7 +112,8 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
                                        const double2 *__restrict__ dotv = nullptr,
                                        const double *__restrict__ gp = nullptr, const GTab *gt = nullptr,
                                        double2 *__restrict__ out64 = nullptr, V *__restrict__ bout = nullptr,
-                                       V *__restrict__ xout = nullptr)
+                                       V *__restrict__ xout = nullptr, T wload = T(-1), T cx = T(1),
+                                       const V *__restrict__ x0 = nullptr, T c0 = T(0))
 {
 	typedef TileSmem<T> SM;
 	constexpr int TX = SM::TX, PX = SM::PX, PZ = SM::PZ, EX = SM::EX, EZ = SM::EZ;
@@ -122,6 +125,7 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 	const int tz_tiles = (n + TZN - 1) / TZN, tx_tiles = (n + TX - 1) / TX, ntiles = tz_tiles * tx_tiles;
 	const int t0 = pt.rank, ts = pt.size;
 	const int lz = threadIdx.x & 31, lx0 = threadIdx.x >> 5;
+	const T wl = wload < T(0) ? omega : wload;
 	double dacc = 0.0;
 	T pu[PSLOTS], pw[PSLOTS], pe[PSLOTS];
 
@@ -136,7 +140,7 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 				const int gx = ix0 - 1 + px, gz = iz0 - 1 + pz;
 				if (gx >= 0 && gx < n && gz >= 0 && gz < n) {
 					const int A = gz + gx * n;
-					const V xv = x_eff<T, V>(xs, A, gx, gz, x, b, invD, omega, xc, nc);
+					const V xv = x_eff<T, V>(xs, A, gx, gz, x, b, invD, wl, xc, nc);
 					const unsigned m = mask[A];
 					uu = (m & 1u) ? T(0) : xv.x;
 					ww = (m & 2u) ? T(0) : xv.y;
@@ -165,7 +169,7 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 			}
 		}
 		// epilogue operands of this tile, and the next tile's patch, go in flight now
-		V eb[NPT], ed[NPT];
+		V eb[NPT], ed[NPT], e0[NPT];
 #pragma unroll
 		for (int j = 0; j < NPT; j++) {
 			const int gx = ix0 + lx0 + 8 * j, gz = iz0 + lz;
@@ -181,8 +185,11 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 				} else {
 					eb[j] = b[A];
 				}
-				if (mode == PASS_SMOOTH)
+				if (mode == PASS_SMOOTH) {
 					ed[j] = invD[A];
+					if (x0 != nullptr)
+						e0[j] = x0[A];
+				}
 			}
 		}
 		if (t + ts < ntiles)
@@ -279,8 +286,19 @@ __device__ __noinline__ void tile_pass(unsigned char *smraw, Part pt, int N, con
 					xout[A] = xv;
 				}
 			} else {
-				o.x = (m & 1u) ? T(0) : xu + omega * ed[j].x * (eb[j].x - fu);
-				o.y = (m & 2u) ? T(0) : xw + omega * ed[j].y * (eb[j].y - fw);
+				T px = cx * xu, pw = cx * xw;
+				if (x0 != nullptr) {
+					px -= c0 * e0[j].x;
+					pw -= c0 * e0[j].y;
+				}
+				o.x = (m & 1u) ? T(0) : px + omega * ed[j].x * (eb[j].x - fu);
+				o.y = (m & 2u) ? T(0) : pw + omega * ed[j].y * (eb[j].y - fw);
+				if (xout) {   // x as this pass formed it (the coarse-corrected iterate)
+					V xv;
+					xv.x = xu;
+					xv.y = xw;
+					xout[A] = xv;
+				}
 				if (dot) {
 					const double2 v = dotv[A];
 					dacc += (double)o.x * v.x + (double)o.y * v.y;

@@ -392,6 +392,25 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	a.H.nu_c = c->cfg.mg_smooth_coarse < 1 ? a.H.nu : c->cfg.mg_smooth_coarse;
 	a.H.lfine = 2;
 	a.H.eta_avg = c->cfg.mg_eta_avg;
+	// degree-2 Chebyshev on [lmax/ratio, lmax]: theta, delta the centre and half-width,
+	// rho_k the recurrence of the scaled polynomials (Saad, Iterative Methods for
+	// Sparse Linear Systems, Alg. 12.1)
+	a.H.cheb = 0;
+	a.H.w1 = a.H.w2 = a.H.c1 = a.H.c0 = (TI)0;
+	if (c->cfg.mg_smoother == 1) {
+		const double lmax = c->cfg.mg_cheb_lmax, ratio = c->cfg.mg_cheb_ratio;
+		if (!(lmax > 0.0) || !(ratio > 1.0)) {
+			mclg_set_error("mg_smoother=1 needs mg_cheb_lmax > 0 and mg_cheb_ratio > 1");
+			return MCLG_BAD_INPUT;
+		}
+		const double lo = lmax / ratio, th = 0.5 * (lmax + lo), de = 0.5 * (lmax - lo), sg = th / de;
+		const double r0 = 1.0 / sg, r1 = 1.0 / (2.0 * sg - r0);
+		a.H.cheb = 1;
+		a.H.w1 = (TI)(1.0 / th);
+		a.H.c0 = (TI)(r1 * r0);
+		a.H.c1 = (TI)(1.0 + r1 * r0);
+		a.H.w2 = (TI)(2.0 * r1 / de);
+	}
 	const size_t nn0 = (size_t)n0 * n0, ne = (size_t)N0 * N0;
 	CK(mg_alloc(c, &a.H.px, nn0));
 	CK(mg_alloc(c, &a.H.pr, nn0));

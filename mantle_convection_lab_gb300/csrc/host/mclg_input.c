@@ -222,6 +222,9 @@ void mclg_config_defaults(mclg_config *c)
 	c->mg_coarse_iteration = 4;
 	c->lowest_vis = 1.0;
 	c->highest_vis = 1.0;
+	c->mg_smoother = 0;
+	c->mg_cheb_lmax = 2.5;
+	c->mg_cheb_ratio = 4.0;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -321,6 +324,9 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_double(&pl, "lowest_vis", &c->lowest_vis, 1.0);
 	get_double(&pl, "highest_vis", &c->highest_vis, 1.0);
 	get_int(&pl, "mg_smooth_coarse", &c->mg_smooth_coarse, 0);
+	get_int(&pl, "mg_smoother", &c->mg_smoother, 0);
+	get_double(&pl, "mg_cheb_lmax", &c->mg_cheb_lmax, 2.5);
+	get_double(&pl, "mg_cheb_ratio", &c->mg_cheb_ratio, 4.0);
 	free(pl.e);
 	return MCLG_OK;
 }

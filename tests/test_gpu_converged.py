@@ -143,3 +143,31 @@ def test_converged_solution_equals_direct_solve_at_contrast_1e5(precision):
         assert st.status == 0 and max(st.res_momentum, st.res_continuity) < 1e-11
         assert rel(m.get("d"), d_ex) < 1e-8
         assert rel(_demean(m.get("P")), _demean(p_ex)) < 1e-8
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_chebyshev_smoother_matches_reference(precision):
+    """The degree-2 Chebyshev smoother (mg_smoother=1) changes only the
+    preconditioner: the same converged fields as the reference's on the 16x16
+    case, 4 steps."""
+    g = golden("cfg1_l5")
+    c = Config.from_input(golden_input("cfg1_l5"))
+    c.precision, c.stokes_method, c.warm_start = precision, 1, 3
+    c.stokes_rtol, c.outer_rtol, c.inner_rtol, c.max_outer, c.max_refine = 1e-8, 3e-3, 1e-2, 1000, 20
+    c.mg_coarse, c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio = 2, 1, 2.5, 4.0
+    with Model(c) as m:
+        m.initial_temperature()
+        for s in range(4):
+            st = m.step()
+            assert st.status == 0 and max(st.res_momentum, st.res_continuity) < 1e-8
+            for f in ("V0", "V1"):
+                assert rel(m.get(f), g[f"step{s:04d}/{f}"]) < 1e-8, (s, f)
+            assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < 1e-8
+
+
+def test_chebyshev_smoother_rejects_a_bad_interval():
+    from mantle_convection_lab_gb300 import MclgError
+    c = Config.from_input(golden_input("cfg1_l5"))
+    c.precision, c.stokes_method, c.mg_smoother, c.mg_cheb_ratio = 1, 1, 1, 0.5
+    with pytest.raises(MclgError):
+        Model(c)

@@ -65,6 +65,9 @@ def test_defaults_follow_input_c(tmp_path):
     assert (c.develop_mode, c.max_citcom_cycle, c.max_cg_cycle, c.zero_P) == (1, 375, 200, 1)
     assert c.precision == 0 and c.warm_start == 0
     assert (c.grain_damage, c.lowest_vis, c.highest_vis) == (0, 1.0, 1.0)     # Input.c:58-59, 95
+    assert (c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio) == (0, 2.5, 4.0)  # engine's own options
+    c = Config.from_input(write(tmp_path, "mg_smoother=1\nmg_cheb_lmax=2.2\nmg_cheb_ratio=5\n"))
+    assert (c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio) == (1, 2.2, 5.0)
 
 
 def test_getpar_tokenisation(tmp_path):
