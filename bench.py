@@ -154,11 +154,13 @@ def replica_bytes(st, neq, nno, nel, w=8):
             + 2 * (w * (10 * neq + nno) + nno))
 
 
-def converged_bytes(st, N, method=0, w=4):
+def converged_bytes(st, N, method=0, w=4, cheb=False):
     """Mixed solver, per launch.  V(2,2) cycle: 4 tile passes per level (read x,
     b, D^-1 as 2w each, eta w, mask 1; write 2w: 9w+1 B/node) and the transfer
     (restriction reads 9 fine residuals per coarse node, prolongation 4 coarse
-    values per fine node, cached: counted as 4w B per fine node).
+    values per fine node, cached: counted as 4w B per fine node); the Chebyshev
+    smoother also writes and reads back the coarse-corrected iterate on the way
+    up (4w B/node).
     Uzawa (method 0), per inner MG-PCG iteration: the CG part w*(10 n_v + nn) +
     nn plus a V-cycle; per Uzawa iteration: FP64 G s, G^T u and the pressure
     updates, 8*(4 n_v + 8 ne).
@@ -172,7 +174,7 @@ def converged_bytes(st, N, method=0, w=4):
     vcyc, n = 0, N
     while n >= 4:
         m = (n + 1) ** 2
-        vcyc += 4 * (9 * w + 1) * m + 4 * w * m
+        vcyc += 4 * (9 * w + 1) * m + 4 * w * m + (4 * w * m if cheb else 0)
         n //= 2
     refine = 8 * (3 * nv + nn) + 8 * 3 * ne
     if method == 1:
@@ -779,7 +781,8 @@ def run_gpu(args, wl):
     peak, peak_kind = load_peaks()
     n_launch = max(len(acc["stats"]), 1)
     if wl["kind"] == "converged":
-        alg = sum(converged_bytes(s, cfg_N(cfg), cfg.stokes_method) for s in acc["stats"]) / n_launch
+        alg = sum(converged_bytes(s, cfg_N(cfg), cfg.stokes_method, cheb=cfg.mg_smoother == 1)
+                  for s in acc["stats"]) / n_launch
         kname = "k_stokes_mg<float> (persistent mixed-precision Stokes solve)"
         dtype = "f32 inner / f64 outer"
     else:
