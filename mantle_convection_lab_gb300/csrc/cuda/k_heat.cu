@@ -87,12 +87,53 @@ __device__ __forceinline__ void heat_rows(const DevLevel &L, const double2 *__re
 	}
 }
 
+// The same rows with the common factors taken out of the Gauss-point loop:
+// u.grad N_b per (b, g) once, one reciprocal of the Jacobian instead of a
+// division per term, and the terms multiplied by the reference's zero
+// off-diagonal conductivity dropped.  About a third of the FP64 operations of
+// heat_rows (FP64 runs at 1/64 of FP32 on GB300); the rows differ from the
+// reference's in the last bits, so the converged solvers use it and the FP64
+// replica keeps heat_rows.
+__device__ __forceinline__ void heat_rows_fast(const DevLevel &L, const double2 *__restrict__ V, double t0,
+                                               double t1, int e, int a, double (&kr)[4], double (&cr)[4])
+{
+	double u1 = 0.0, u2 = 0.0;
+#pragma unroll
+	for (int b = 0; b < 4; b++) {
+		const double2 v = V[L.ienl[b * L.nel + e]];
+		u1 += v.x * 0.25;
+		u2 += v.y * 0.25;
+	}
+	const double dzh = L.dzh[e], dxh = L.dxh[e], jac = L.jac[e], ijac = 1.0 / jac;
+	double ax[4], az[4], ah[4], an[4];
+#pragma unroll
+	for (int g = 0; g < 4; g++) {
+		ax[g] = cS.dNdxi[a][g] * dzh;
+		az[g] = cS.dNdeta[a][g] * dxh;
+		ah[g] = t0 * ax[g] + t1 * az[g];
+		an[g] = cS.N[a][g];
+	}
+#pragma unroll
+	for (int b = 0; b < 4; b++) {
+		double k = 0.0, c = 0.0;
+#pragma unroll
+		for (int g = 0; g < 4; g++) {
+			const double bx = cS.dNdxi[b][g] * dzh, bz = cS.dNdeta[b][g] * dxh;
+			const double ub = u1 * bx + u2 * bz;
+			k += an[g] * ub + (ah[g] * ub + ax[g] * bx + az[g] * bz) * ijac;
+			c += (an[g] + ah[g]) * cS.N[b][g];
+		}
+		kr[b] = k;
+		cr[b] = c * jac;
+	}
+}
+
 // One thread per node: rows of heat K, C (same slots as the Stokes blocks) and F.
-__global__ void __launch_bounds__(kBlock) k_assemble_heat(DevLevel L, const double2 *__restrict__ V,
-                                                          const double *__restrict__ tau0,
-                                                          const double *__restrict__ tau1, double Q,
-                                                          double *__restrict__ HK, double *__restrict__ HC,
-                                                          double *__restrict__ HF)
+template <bool FAST>
+__device__ __forceinline__ void assemble_heat_node(DevLevel L, const double2 *__restrict__ V,
+                                                   const double *__restrict__ tau0, const double *__restrict__ tau1,
+                                                   double Q, double *__restrict__ HK, double *__restrict__ HC,
+                                                   double *__restrict__ HF)
 {
 	const int A = blockIdx.x * blockDim.x + threadIdx.x;
 	if (A >= L.nno)
@@ -111,7 +152,10 @@ __global__ void __launch_bounds__(kBlock) k_assemble_heat(DevLevel L, const doub
 	for (int s = 0; s < cnt; s++) {
 		const int e = L.p2n_el[s * nno + A], a = L.p2n_a[s * nno + A];
 		double kr[4], cr[4];
-		heat_rows(L, V, tau0[e], tau1[e], e, a, kr, cr);
+		if (FAST)
+			heat_rows_fast(L, V, tau0[e], tau1[e], e, a, kr, cr);
+		else
+			heat_rows(L, V, tau0[e], tau1[e], e, a, kr, cr);
 #pragma unroll
 		for (int b = 0; b < 4; b++) {
 			const int B = L.ienl[b * nel + e];
@@ -154,31 +198,74 @@ __global__ void __launch_bounds__(kBlock) k_assemble_heat(DevLevel L, const doub
 	HF[A] = f;
 }
 
+__global__ void __launch_bounds__(kBlock) k_assemble_heat(DevLevel L, const double2 *__restrict__ V,
+                                                          const double *__restrict__ tau0,
+                                                          const double *__restrict__ tau1, double Q,
+                                                          double *__restrict__ HK, double *__restrict__ HC,
+                                                          double *__restrict__ HF)
+{
+	assemble_heat_node<false>(L, V, tau0, tau1, Q, HK, HC, HF);
+}
+
+__global__ void __launch_bounds__(kBlock) k_assemble_heat_fast(DevLevel L, const double2 *__restrict__ V,
+                                                               const double *__restrict__ tau0,
+                                                               const double *__restrict__ tau1, double Q,
+                                                               double *__restrict__ HK, double *__restrict__ HC,
+                                                               double *__restrict__ HF)
+{
+	assemble_heat_node<true>(L, V, tau0, tau1, Q, HK, HC, HF);
+}
+
 // advection_dt (:135-177): min over elements of L^2 and of 0.5/(|u|/L0 + |w|/L1),
 // where L0, L1 in the CFL term are those of the LAST element (the reference
 // reuses the variable left by its first loop).  Positive doubles order like
-// their bit patterns, so an integer atomicMin gives the exact minimum.
+// their bit patterns, so an integer minimum is the exact minimum: each block
+// reduces its elements' bit patterns (a NaN step contributes nothing, as
+// ULLONG_MAX) and one atomicMin per block and value merges the blocks.
 __global__ void __launch_bounds__(kBlock) k_heat_dt(DevLevel L, const double2 *__restrict__ V,
                                                     unsigned long long *__restrict__ mins)
 {
+	__shared__ unsigned long long sh[2][kBlock / 32];
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= L.nel)
-		return;
-	const int lv = L.elev[e], lvl = L.elev[L.nel - 1];
-	const double dx = L.dx[lv], dz = L.dz[lv];
-	const double diff = fmin(dx * dx, dz * dz);
-	double u1 = 0.0, u2 = 0.0;
+	unsigned long long bd = ~0ULL, bs = ~0ULL;
+	if (e < L.nel) {
+		const int lv = L.elev[e], lvl = L.elev[L.nel - 1];
+		const double dx = L.dx[lv], dz = L.dz[lv];
+		const double diff = fmin(dx * dx, dz * dz);
+		double u1 = 0.0, u2 = 0.0;
 #pragma unroll
-	for (int a = 0; a < 4; a++) {
-		const double2 v = V[L.ienl[a * L.nel + e]];
-		u1 += 0.25 * v.x;
-		u2 += 0.25 * v.y;
+		for (int a = 0; a < 4; a++) {
+			const double2 v = V[L.ienl[a * L.nel + e]];
+			u1 += 0.25 * v.x;
+			u2 += 0.25 * v.y;
+		}
+		const double u = fabs(u1) / L.dx[lvl] + fabs(u2) / L.dz[lvl];
+		const double step = 0.5 / u;
+		bd = (unsigned long long)__double_as_longlong(diff);
+		if (!isnan(step))
+			bs = (unsigned long long)__double_as_longlong(step);
 	}
-	const double u = fabs(u1) / L.dx[lvl] + fabs(u2) / L.dz[lvl];
-	const double step = 0.5 / u;
-	atomicMin(&mins[0], (unsigned long long)__double_as_longlong(diff));
-	if (!isnan(step))
-		atomicMin(&mins[1], (unsigned long long)__double_as_longlong(step));
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		const unsigned long long od = __shfl_xor_sync(0xffffffffu, bd, o), os = __shfl_xor_sync(0xffffffffu, bs, o);
+		bd = od < bd ? od : bd;
+		bs = os < bs ? os : bs;
+	}
+	const int w = threadIdx.x >> 5;
+	if ((threadIdx.x & 31) == 0) {
+		sh[0][w] = bd;
+		sh[1][w] = bs;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int k = 1; k < kBlock / 32; k++) {
+			bd = sh[0][k] < bd ? sh[0][k] : bd;
+			bs = sh[1][k] < bs ? sh[1][k] : bs;
+		}
+		atomicMin(&mins[0], bd);
+		if (bs != ~0ULL)
+			atomicMin(&mins[1], bs);
+	}
 }
 
 // dt = 0.75 * advection_dt (:37); model_time += dt; A = C/(theta dt) + K;

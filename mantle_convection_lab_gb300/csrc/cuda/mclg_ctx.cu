@@ -51,6 +51,8 @@ __global__ void k_tau(DevLevel L, const double2 *V, double accuracy, double *tau
                       unsigned long long *mins, int safe);
 __global__ void k_assemble_heat(DevLevel L, const double2 *V, const double *tau0, const double *tau1, double Q,
                                 double *HK, double *HC, double *HF);
+__global__ void k_assemble_heat_fast(DevLevel L, const double2 *V, const double *tau0, const double *tau1,
+                                     double Q, double *HK, double *HC, double *HF);
 __global__ void k_heat_dt(DevLevel L, const double2 *V, unsigned long long *mins);
 __global__ void k_heat_system(DevLevel L, const unsigned long long *mins, double theta, const double *T,
                               const double *HK, const double *HC, const double *HF, double *HA, double *B,
@@ -1760,7 +1762,13 @@ static int launch_heat(mclg_ctx *c)
 	                                                f.precision != 0);
 	if ((rc = check_launch(c, "k_tau")))
 		return rc;
-	k_assemble_heat<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->V, c->tau0, c->tau1, f.Q, c->HK, c->HC, c->HF);
+	// the converged solvers take the heat rows with fewer FP64 operations (equal to
+	// the reference's to the last bits); the FP64 replica keeps its operation order
+	if (c->cfg.precision != 0)
+		k_assemble_heat_fast<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->V, c->tau0, c->tau1, f.Q, c->HK, c->HC,
+		                                                              c->HF);
+	else
+		k_assemble_heat<<<blocks_for(L.nno), kBlock, 0, c->st>>>(L, c->V, c->tau0, c->tau1, f.Q, c->HK, c->HC, c->HF);
 	if ((rc = check_launch(c, "k_assemble_heat")))
 		return rc;
 	k_heat_dt<<<blocks_for(L.nel), kBlock, 0, c->st>>>(L, c->V, c->mins);
