@@ -154,13 +154,14 @@ def replica_bytes(st, neq, nno, nel, w=8):
             + 2 * (w * (10 * neq + nno) + nno))
 
 
-def converged_bytes(st, N, method=0, w=4, cheb=False):
-    """Mixed solver, per launch.  V(2,2) cycle: 4 tile passes per level (read x,
-    b, D^-1 as 2w each, eta w, mask 1; write 2w: 9w+1 B/node) and the transfer
-    (restriction reads 9 fine residuals per coarse node, prolongation 4 coarse
-    values per fine node, cached: counted as 4w B per fine node); the Chebyshev
-    smoother also writes and reads back the coarse-corrected iterate on the way
-    up (4w B/node).
+def converged_bytes(st, N, method=0, w=4, cheb=False, nu=2, nu_c=2, lfine=2):
+    """Mixed solver, per launch.  V-cycle: 2 nu tile passes per level (nu sweeps
+    per side: nu on the lfine finest levels, nu_c below; read x, b, D^-1 as 2w
+    each, eta w, mask 1; write 2w: 9w+1 B/node) and the transfer (restriction
+    reads 9 fine residuals per coarse node, prolongation 4 coarse values per fine
+    node, cached: counted as 4w B per fine node); the Chebyshev pairs (levels
+    with 2 sweeps) also write and read back the coarse-corrected iterate on the
+    way up (4w B/node).
     Uzawa (method 0), per inner MG-PCG iteration: the CG part w*(10 n_v + nn) +
     nn plus a V-cycle; per Uzawa iteration: FP64 G s, G^T u and the pressure
     updates, 8*(4 n_v + 8 ne).
@@ -171,11 +172,13 @@ def converged_bytes(st, N, method=0, w=4, cheb=False):
     nn = (N + 1) ** 2
     nv = 2 * nn
     ne = N * N
-    vcyc, n = 0, N
+    vcyc, n, lev = 0, N, 0
     while n >= 4:
         m = (n + 1) ** 2
-        vcyc += 4 * (9 * w + 1) * m + 4 * w * m + (4 * w * m if cheb else 0)
+        sweeps = nu if lev < lfine else nu_c
+        vcyc += 2 * sweeps * (9 * w + 1) * m + 4 * w * m + (4 * w * m if cheb and sweeps == 2 else 0)
         n //= 2
+        lev += 1
     refine = 8 * (3 * nv + nn) + 8 * 3 * ne
     if method == 1:
         it = vcyc + (5 * w + 1) * nn + (225 + 10 * w) * nn + 136 * ne
@@ -781,7 +784,10 @@ def run_gpu(args, wl):
     peak, peak_kind = load_peaks()
     n_launch = max(len(acc["stats"]), 1)
     if wl["kind"] == "converged":
-        alg = sum(converged_bytes(s, cfg_N(cfg), cfg.stokes_method, cheb=cfg.mg_smoother == 1)
+        nu = max(cfg.mg_smooth, 1)
+        alg = sum(converged_bytes(s, cfg_N(cfg), cfg.stokes_method, cheb=cfg.mg_smoother == 1, nu=nu,
+                                  nu_c=cfg.mg_smooth_coarse if cfg.mg_smooth_coarse > 0 else nu,
+                                  lfine=cfg.mg_fine_levels)
                   for s in acc["stats"]) / n_launch
         kname = "k_stokes_mg<float> (persistent mixed-precision Stokes solve)"
         dtype = "f32 inner / f64 outer"

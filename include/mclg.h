@@ -120,8 +120,8 @@ typedef struct mclg_config {
 	/* grain-size rheology (grain_damage=1, Grain_size_evolution.c:3-123): the clip of
 	 * the viscosity it sets */
 	double lowest_vis, highest_vis;   /* (1.0, 1.0)  Input.c:58-59 */
-	/* converged solvers on uniform meshes: damped-Jacobi sweeps per V-cycle side
-	 * on the levels below the two finest (0: mg_smooth) */
+	/* converged solvers on uniform meshes: smoothing sweeps per V-cycle side on the
+	 * levels below the mg_fine_levels finest (0: mg_smooth) */
 	int mg_smooth_coarse;
 	/* converged solvers on uniform meshes with mg_smooth=2: 0 damped Jacobi (mg_omega),
 	 * 1 the degree-2 Chebyshev polynomial of D^-1 K on [mg_cheb_lmax / mg_cheb_ratio,
@@ -129,6 +129,9 @@ typedef struct mclg_config {
 	 * the V-cycle stays symmetric) */
 	int mg_smoother;
 	double mg_cheb_lmax, mg_cheb_ratio;   /* (2.5, 4.0) */
+	/* the number of finest levels that take mg_smooth sweeps per side; the coarser
+	 * ones take mg_smooth_coarse (2) */
+	int mg_fine_levels;
 } mclg_config;
 
 typedef struct mclg_step_stats {

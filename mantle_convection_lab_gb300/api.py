@@ -68,7 +68,7 @@ class Config(C.Structure):
         ("stokes_method", C.c_int), ("mg_cycle", C.c_int), ("mg_finest_iteration", C.c_int),
         ("mg_coarse_iteration", C.c_int), ("lowest_vis", C.c_double), ("highest_vis", C.c_double),
         ("mg_smooth_coarse", C.c_int), ("mg_smoother", C.c_int), ("mg_cheb_lmax", C.c_double),
-        ("mg_cheb_ratio", C.c_double),
+        ("mg_cheb_ratio", C.c_double), ("mg_fine_levels", C.c_int),
     ]
 
     @classmethod

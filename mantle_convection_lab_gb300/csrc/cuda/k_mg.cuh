@@ -29,8 +29,8 @@ struct MGHier {
 	double *cwork;               // [cnd * 2*cnd] scratch for the inversion
 	int cnd;                     // 2 * n_coarsest^2
 	T omega;
-	int nu;                      // Jacobi sweeps per side on levels below lfine
-	int nu_c, lfine;             // ... and on levels lfine and coarser
+	int nu;                      // smoothing sweeps per side on the lfine finest levels
+	int nu_c, lfine;             // ... and on the coarser ones
 	int eta_avg;                 // coarse viscosity: 0 injection, 1 full-weighted mean, 2 full-weighted log-mean
 	// degree-2 Chebyshev smoothing (cheb != 0, nu == nu_c == 2): x1 = x0 + w1 D^-1 r0,
 	// x2 = c1 x1 - c0 x0 + w2 D^-1 r1

@@ -392,7 +392,7 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 	a.H.omega = (TI)c->cfg.mg_omega;
 	a.H.nu = c->cfg.mg_smooth < 1 ? 1 : c->cfg.mg_smooth;
 	a.H.nu_c = c->cfg.mg_smooth_coarse < 1 ? a.H.nu : c->cfg.mg_smooth_coarse;
-	a.H.lfine = 2;
+	a.H.lfine = c->cfg.mg_fine_levels < 0 ? 0 : c->cfg.mg_fine_levels;
 	a.H.eta_avg = c->cfg.mg_eta_avg;
 	// degree-2 Chebyshev on [lmax/ratio, lmax]: theta, delta the centre and half-width,
 	// rho_k the recurrence of the scaled polynomials (Saad, Iterative Methods for

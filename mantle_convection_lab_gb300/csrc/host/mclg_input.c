@@ -225,6 +225,7 @@ void mclg_config_defaults(mclg_config *c)
 	c->mg_smoother = 0;
 	c->mg_cheb_lmax = 2.5;
 	c->mg_cheb_ratio = 4.0;
+	c->mg_fine_levels = 2;
 }
 
 int mclg_config_from_input(const char *path, mclg_config *c)
@@ -327,6 +328,7 @@ int mclg_config_from_input(const char *path, mclg_config *c)
 	get_int(&pl, "mg_smoother", &c->mg_smoother, 0);
 	get_double(&pl, "mg_cheb_lmax", &c->mg_cheb_lmax, 2.5);
 	get_double(&pl, "mg_cheb_ratio", &c->mg_cheb_ratio, 4.0);
+	get_int(&pl, "mg_fine_levels", &c->mg_fine_levels, 2);
 	free(pl.e);
 	return MCLG_OK;
 }

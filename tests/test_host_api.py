@@ -66,6 +66,7 @@ def test_defaults_follow_input_c(tmp_path):
     assert c.precision == 0 and c.warm_start == 0
     assert (c.grain_damage, c.lowest_vis, c.highest_vis) == (0, 1.0, 1.0)     # Input.c:58-59, 95
     assert (c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio) == (0, 2.5, 4.0)  # engine's own options
+    assert c.mg_fine_levels == 2
     c = Config.from_input(write(tmp_path, "mg_smoother=1\nmg_cheb_lmax=2.2\nmg_cheb_ratio=5\n"))
     assert (c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio) == (1, 2.2, 5.0)
 
