@@ -92,7 +92,7 @@ WORKLOADS["cfg2_amr_128"] = {
 ENSEMBLE_METRIC = "aggregate model-steps/s at Stokes residual 1e-8"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one steady launch
 # of the workload's solver kernel, from the ncu capture summarised in profiles/
-TRAFFIC = {"cfg3_mg_1024": (46.38e9, "profiles/k_stokes_mg_f32_1024.md (one steady launch, ncu --set full)")}
+TRAFFIC = {"cfg3_mg_1024": (45.78e9, "profiles/k_stokes_mg_f32_1024.md (one steady launch, ncu --set full)")}
 DEFAULT_WORKLOAD = "cfg3_mg_1024"
 GUESS_NET = os.path.join(ROOT, "mantle_convection_lab_gb300", "weights", "guess_cfg3.bin")
 GUESS_GRID = 128
