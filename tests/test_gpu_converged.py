@@ -165,6 +165,27 @@ def test_chebyshev_smoother_matches_reference(precision):
             assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < 1e-8
 
 
+@pytest.mark.parametrize("fine", [1, 2])
+def test_single_fine_sweeps_match_reference(fine):
+    """One Jacobi sweep per side on the `fine` finest levels and Chebyshev pairs
+    below (configuration 3's V-cycle) change only the preconditioner: the same
+    converged fields as the reference's on the 16x16 case, 4 steps."""
+    g = golden("cfg1_l5")
+    c = Config.from_input(golden_input("cfg1_l5"))
+    c.precision, c.stokes_method, c.warm_start = 1, 1, 3
+    c.stokes_rtol, c.outer_rtol, c.inner_rtol, c.max_outer, c.max_refine = 1e-8, 3e-3, 1e-2, 1000, 20
+    c.mg_coarse, c.mg_smoother, c.mg_cheb_lmax, c.mg_cheb_ratio = 2, 1, 2.2, 8.0
+    c.mg_smooth, c.mg_smooth_coarse, c.mg_fine_levels, c.mg_eta_avg = 1, 2, fine, 1
+    with Model(c) as m:
+        m.initial_temperature()
+        for s in range(4):
+            st = m.step()
+            assert st.status == 0 and max(st.res_momentum, st.res_continuity) < 1e-8
+            for f in ("V0", "V1"):
+                assert rel(m.get(f), g[f"step{s:04d}/{f}"]) < 1e-8, (s, f)
+            assert rel(m.get("T"), g[f"heat{s:04d}/T"]) < 1e-8
+
+
 def test_chebyshev_smoother_rejects_a_bad_interval():
     from mantle_convection_lab_gb300 import MclgError
     c = Config.from_input(golden_input("cfg1_l5"))
