@@ -1195,9 +1195,9 @@ static int launch_stokes_mg(mclg_ctx *c)
 	return stokes_mg_finish(c);
 }
 
-// Switch the network off for 16 steps after 3 consecutive steps on which its
-// guess won the residual test but took more inner iterations than the last
-// step solved from the previous solution.
+// Switch the network off for 16 steps after 3 consecutive judged steps on which
+// it did not pay: its guess lost the residual test, or won it but took more
+// inner iterations than the last step solved from the previous solution.
 static void guess_bookkeeping(mclg_ctx *c)
 {
 	if (c->gmode != MCLG_GUESS_LEARNED || c->cfg.precision == 0)
@@ -1208,14 +1208,16 @@ static void guess_bookkeeping(mclg_ctx *c)
 			c->gbad++;
 		else
 			c->gbad = 0;
-		if (c->gbad >= 3) {
-			c->goff = 16;
-			c->gbad = 0;
-		}
 	} else {
+		if (s.guess_used == 0)   // judged, and the previous solution was the better start
+			c->gbad++;
 		c->git_prev = s.cg_cycles;
 		if (c->goff > 0)
 			c->goff--;
+	}
+	if (c->gbad >= 3) {
+		c->goff = 16;
+		c->gbad = 0;
 	}
 }
 

@@ -192,7 +192,24 @@ def test_learned_guess_in_the_solver():
     for f in ("T", "V0", "P"):
         assert rel(ev["learned"][f], ev["base"][f]) < 1e-6, f
     used = [r["used"] for r in ev["learned"]["rows"]]
-    assert used[:2] == [-1, -1] and all(u in (0, 1) for u in used[2:])
+    assert used[:2] == [-1, -1] and all(u in (0, 1) for u in used[2:5])
+    # the network is judged on every step unless 3 judged steps in a row did not
+    # pay (it lost the residual test, or won it and took more inner iterations
+    # than the last step solved from the previous solution), which switches it
+    # off for 16 steps (mclg_ctx.cu guess_bookkeeping)
+    run, off, prev = 0, 0, None
+    for k, r in enumerate(ev["learned"]["rows"]):
+        u = r["used"]
+        if k >= 2:
+            assert (u == -1) if off > 0 else (u in (0, 1)), (k, used)
+        if u == 1:
+            run = run + 1 if prev is not None and r["inner"] > prev else 0
+        else:
+            run += u == 0
+            prev = r["inner"]
+            off = max(off - 1, 0)
+        if run >= 3:
+            run, off = 0, 16
     # the extrapolated start (the base of the learned guess) beats the last solution
     assert s["base"]["inner"] < s["previous"]["inner"], s
     gain = s["base"]["inner"] - s["learned"]["inner"]
