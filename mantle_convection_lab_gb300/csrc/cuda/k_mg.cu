@@ -581,6 +581,49 @@ __device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask
 	return s;
 }
 
+// a + b = s + e exactly (Knuth's TwoSum, six FP32 additions)
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
+{
+	s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sh, sl) += (gh + gl) x in double-float arithmetic: the product gh x and its
+// rounding error (by FMA), gl x, and a TwoSum into the running pair.
+__device__ __forceinline__ void df_axpy(float &sh, float &sl, float gh, float gl, float x)
+{
+	const float p = __fmul_rn(gh, x);
+	float pe = __fmaf_rn(gh, x, -p);
+	pe = __fmaf_rn(gl, x, pe);
+	float t;
+	two_sum_f(sh, p, sh, t);
+	sl = __fadd_rn(sl, __fadd_rn(t, pe));
+}
+
+// (G^T u)_e for an FP32 velocity field: the eight products and their sum in
+// double-float arithmetic on the FP32 pipe (about 48 bits, in the same corner
+// order as the FP64 form), so that the FP64 pipe -- 1/64 of FP32 on GB300 --
+// only converts and adds the final pair.
+__device__ __forceinline__ double gtmul_elem_t(int N0, const unsigned char *mask, const GTab &gt, const float2 *u,
+                                               int ex, int ez)
+{
+	const int n = N0 + 1;
+	const int cn[4] = {ez + ex * n, ez + 1 + ex * n, ez + 1 + (ex + 1) * n, ez + (ex + 1) * n};
+	float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		const int a = kSortedCorner[c];
+		const float2 ua = u[cn[a]];
+		const unsigned m = mask[cn[a]];
+		if (!(m & 1u))
+			df_axpy(sh, sl, gt.g0h[a], gt.g0l[a], ua.x);
+		if (!(m & 2u))
+			df_axpy(sh, sl, gt.g1h[a], gt.g1l[a], ua.y);
+	}
+	return (double)sh + (double)sl;
+}
+
 // ---- MINRES vector kernels (FP64), kVecU elements per thread and trip ---------
 // Separate functions so that their registers do not compete with the solver's
 // state; every load of a trip is issued before its arithmetic.

@@ -44,6 +44,7 @@ struct MGHier {
 // element of the uniform mesh, filled on the host.
 struct GTab {
 	double g0[4], g1[4];
+	float g0h[4], g0l[4], g1h[4], g1l[4];   // the same as float pairs: g = h + l
 };
 
 // The converged Stokes solve of one time step (FP64 state, TI inner solves).

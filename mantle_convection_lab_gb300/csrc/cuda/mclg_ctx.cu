@@ -434,6 +434,10 @@ static int mg_setup(mclg_ctx *c, MGArgs<TI> &a)
 			}
 			a.gt.g0[k] = g0;
 			a.gt.g1[k] = g1;
+			a.gt.g0h[k] = (float)g0;
+			a.gt.g0l[k] = (float)(g0 - (double)a.gt.g0h[k]);
+			a.gt.g1h[k] = (float)g1;
+			a.gt.g1l[k] = (float)(g1 - (double)a.gt.g1h[k]);
 		}
 	}
 	a.vis = c->vis;
