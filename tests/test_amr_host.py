@@ -234,3 +234,19 @@ def test_device_numbering_fails_loudly_without_a_device():
         pytest.skip("a device is present: tests/test_gpu_mesh_numbering.py covers it")
     with pytest.raises(MclgError):
         Mesh(cfg(7), leaves=uniform_leaves(6, 3), device=True)
+
+
+@pytest.mark.parametrize("bad", ["decreasing", "out_of_range", "one_leaf"])
+def test_leaf_list_checks(bad):
+    """The leaf-list checks shared by the host and the device builders."""
+    c = cfg(7)
+    lv = uniform_leaves(6, 3)
+    if bad == "decreasing":
+        lv = lv[::-1].copy()
+    elif bad == "out_of_range":
+        lv = lv.copy()
+        lv[-1] = 1 << 12
+    else:
+        lv = lv[:1].copy()
+    with pytest.raises(MclgError):
+        Mesh(c, leaves=lv)
